@@ -1,0 +1,196 @@
+/*
+ * k2g.h -- C ABI of the GB300 Kraken 2 classification library (libk2g.so).
+ *
+ * The library keeps a Kraken 2 database (hash.k2d / taxo.k2d / opts.k2d)
+ * resident in HBM and runs the classification hot path as sm_103a CUDA
+ * kernels: spaced-seed minimizer scan, compact-hash probing, per-read hit
+ * counting with ResolveTree, HyperLogLog++ minimizer counters and the
+ * CompareAndSet-with-LCA table insert.  Results are bit-identical to the
+ * reference CPU implementation on the same inputs.
+ *
+ * Conventions
+ *  - Every entry point returns a k2g_status and never aborts; the message of
+ *    the last failure on the calling thread is available from k2g_last_error().
+ *  - "d_" arguments are device pointers on the database's device; plain
+ *    pointers are host memory.  Device-pointer calls are asynchronous on the
+ *    given cudaStream_t (passed as void*, NULL = legacy default stream).
+ *  - Taxon ids are the reference's internal ids (BFS order, parent < child,
+ *    0 = none).  Map to external ids with the taxonomy's external_id field.
+ *  - A database handle may be used concurrently from several host threads on
+ *    distinct streams for read-only calls (lookup, scan, classify).
+ */
+#ifndef K2G_H_
+#define K2G_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  K2G_OK = 0,
+  K2G_ERR_ARG = 1,          /* invalid argument                             */
+  K2G_ERR_IO = 2,           /* file could not be opened / read / written    */
+  K2G_ERR_FORMAT = 3,       /* malformed or inconsistent database file      */
+  K2G_ERR_CUDA = 4,         /* CUDA runtime failure                         */
+  K2G_ERR_NOMEM = 5,        /* device or pinned host allocation failed      */
+  K2G_ERR_CAPACITY = 6,     /* hash table full / output buffer too small    */
+  K2G_ERR_UNSUPPORTED = 7,  /* database variant not handled (e.g. protein)  */
+  K2G_ERR_TIMEOUT = 8,      /* a bounded device wait gave up                */
+  K2G_ERR_BUDGET = 9        /* request exceeds the serving HBM budget       */
+} k2g_status;
+
+/* Codes of the per-k-mer hit list besides taxon ids (src/classify.cc:33-35). */
+#define K2G_CODE_MATE_BORDER 0xFFFFFFFFu
+#define K2G_CODE_AMBIGUOUS   0xFFFFFFFDu
+
+typedef struct k2g_db k2g_db;
+
+/* Semantic copy of IndexOptions (src/kraken2_data.h:15-25). */
+typedef struct {
+  uint64_t k, l;
+  uint64_t spaced_seed_mask;
+  uint64_t toggle_mask;
+  int32_t dna_db;
+  int32_t revcom_version;
+  uint64_t minimum_acceptable_hash_value;
+} k2g_index_options;
+
+typedef struct {
+  uint64_t capacity, size, key_bits, value_bits, node_count;
+  k2g_index_options opts;
+  const uint32_t *d_cells;      /* the compact hash table in HBM           */
+  const uint32_t *d_parent;     /* parent id per internal taxon id         */
+  int device;
+} k2g_db_info;
+
+const char *k2g_last_error(void);
+const char *k2g_version(void);
+
+/* Loads the three database files and uploads the table and the taxonomy's
+ * parent array.  Replaces load_index (src/classify.cc:269-302): the opts
+ * file read (:272-279), Taxonomy::Init (src/taxonomy.cc:195-238) and
+ * CompactHashTable::LoadTable (src/compact_hash.h:279-341). */
+k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
+                       const char *opts_k2d, int device, k2g_db **out);
+
+/* An empty table for building: CompactHashTable(capacity, key_bits,
+ * value_bits) (src/compact_hash.h:164-192) plus the parent array of a
+ * taxonomy (parent[0] = 0, parent[i] < i). */
+k2g_status k2g_db_create(const k2g_index_options *opts, uint64_t capacity,
+                         uint32_t key_bits, uint32_t value_bits,
+                         const uint64_t *parent, uint64_t node_count,
+                         int device, k2g_db **out);
+
+k2g_status k2g_db_close(k2g_db *db);
+k2g_status k2g_db_info_get(const k2g_db *db, k2g_db_info *out);
+
+/* Copies the table back to the host and writes hash.k2d in the reference
+ * layout -- CompactHashTable::WriteTable (src/compact_hash.h:344-352). */
+k2g_status k2g_db_write_hash(const k2g_db *db, const char *hash_k2d);
+/* Copies the table (capacity cells) into host memory. */
+k2g_status k2g_db_download(const k2g_db *db, uint32_t *cells, uint64_t *size);
+
+/* Batched lookup -- KeyValueStore::GetBatch (src/kv_store.h:29,
+ * src/compact_hash.h:380-392): vals[i] = Get(keys[i]), 0 when absent. */
+k2g_status k2g_lookup(const k2g_db *db, const uint64_t *d_keys, uint32_t *d_vals,
+                      uint64_t n, void *stream);
+/* Same with host arrays (synchronous); the drop-in for a CPU caller of
+ * KeyValueStore::GetBatch. */
+k2g_status k2g_lookup_host(const k2g_db *db, const uint64_t *keys, uint32_t *vals,
+                           uint64_t n);
+
+/* Minimizer scan -- MinimizerScanner::NextMinimizer / is_ambiguous
+ * (src/mmscanner.cc:114-189, src/mmscanner.h:47-49) for every k-mer of every
+ * sequence.  Sequence i occupies d_bases[d_seq_off[i], d_seq_off[i+1]); its
+ * k-mer j (j < len-k+1) is written at index d_seq_off[i] + j of d_mins and
+ * d_ambig. */
+k2g_status k2g_scan(const k2g_db *db, const char *d_bases, const uint64_t *d_seq_off,
+                    uint64_t n_seqs, uint64_t *d_mins, uint8_t *d_ambig, void *stream);
+
+/* ---- classification (src/classify.cc:773-991, ResolveTree :710-762) */
+
+typedef struct {
+  double confidence;          /* -T, in [0, 1]                              */
+  int32_t min_hit_groups;     /* -g                                         */
+  int32_t quick;              /* -q                                         */
+  int32_t paired;             /* -P / -S: fragment = 2 consecutive seqs     */
+  int32_t min_quality;        /* -Q, applied where quals are given          */
+} k2g_classify_params;
+
+typedef struct {
+  const char *d_bases;        /* concatenated sequences, ASCII              */
+  const char *d_quals;        /* NULL, or qualities in the same layout      */
+  const uint64_t *d_seq_off;  /* n_seqs + 1 offsets                         */
+  uint64_t n_frags;           /* n_seqs = n_frags * (paired ? 2 : 1)        */
+  uint64_t max_seq_len;       /* longest sequence (sizes scratch)           */
+  const uint32_t *d_frag_block; /* reader block of each fragment (HLL), or NULL */
+  uint64_t frag_base;         /* ordinal of fragment 0 in the whole run     */
+} k2g_reads;
+
+typedef struct {
+  uint32_t *d_call;           /* [n_frags] internal taxid, 0 = unclassified */
+  uint32_t *d_hit_groups;     /* [n_frags] minimizer hit groups, or NULL    */
+  uint64_t *d_hitlist_off;    /* [n_frags] index of the first run, or NULL  */
+  uint32_t *d_hitlist_len;    /* [n_frags] number of runs, or NULL          */
+  /* Hit-list runs, (code << 32 | count), the RLE of the per-k-mer taxa list
+   * printed by AddHitlistString.  Fragment i's runs start at index
+   * d_seq_off[i * (paired ? 2 : 1)] + 2 * i, so runs_cap must be at least
+   * d_seq_off[n_seqs] + 2 * n_frags. */
+  uint64_t *d_runs;
+  uint64_t runs_cap;
+  uint64_t *d_taxon_reads;    /* [node_count] += calls per taxon, or NULL   */
+  /* add_kmer events for HyperLogLog++ (-K), or NULL: one record per LOOKUP
+   * token whose taxon is nonzero (src/classify.cc:869-873). */
+  uint64_t *d_hit_keys;       /* the minimizer                              */
+  uint32_t *d_hit_taxa;       /* its taxon                                  */
+  uint64_t *d_hit_order;      /* (frag_base + fragment) << 32 | key ordinal */
+  uint64_t hits_cap;
+  uint64_t *d_hits_used;      /* event counter (caller zeroes)              */
+  uint32_t *d_status;         /* error word (caller zeroes); nonzero = overflow */
+} k2g_results;
+
+typedef enum {
+  K2G_MODE_PLAIN = 0,         /* one launch per batch, fixed fragment map   */
+  K2G_MODE_PERSISTENT = 1     /* persistent work-stealing kernel (default)  */
+} k2g_mode;
+
+/* Classifies a batch of fragments held in device memory. */
+k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
+                        const k2g_classify_params *params, k2g_results *out,
+                        int mode, void *stream);
+
+/* Host-buffer classification: copies the reads in, classifies, and copies
+ * the per-fragment results back, overlapping transfers with compute over
+ * internal chunks (pinned buffers from k2g_host_alloc make the copies
+ * asynchronous).  runs receives the hit-list runs of all fragments back to
+ * back in fragment order, hitlist_len[i] of them for fragment i.  Any output
+ * may be NULL except call.  *n_runs: in = capacity of runs, out = used.
+ * taxon_reads (node_count entries) is incremented by the calls per taxon. */
+k2g_status k2g_classify_host(const k2g_db *db, const char *bases, const char *quals,
+                             const uint64_t *seq_off, uint64_t n_frags,
+                             const k2g_classify_params *params, uint32_t *call,
+                             uint32_t *hit_groups, uint32_t *hitlist_len, uint64_t *runs,
+                             uint64_t *n_runs, uint64_t *taxon_reads);
+
+/* Pinned host memory helpers for callers that stage their own buffers. */
+k2g_status k2g_host_alloc(void **ptr, size_t bytes);
+k2g_status k2g_host_free(void *ptr);
+
+/* ---- build: CompareAndSet with LCA merge (src/compact_hash.h:417-462,
+ * src/build_db.h:187-194, :217-326) */
+
+/* Inserts (key, taxid) pairs with SetMinimizerLCA semantics.  ordered != 0
+ * reproduces sequential insertion in list order (safe-prefix rounds of
+ * src/build_db.h:286-321); ordered == 0 is the fast unordered insert of
+ * ProcessSequenceFast (src/build_db.h:196-214), whose key->taxid map can
+ * differ only when compacted keys collide along a probe path. */
+k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
+                            uint64_t n, int ordered, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,199 @@
+"""GB300 Kraken 2 classification: Python mirror of the libk2g C ABI.
+
+The product is libk2g.so (include/k2g.h); this module binds it with ctypes for
+tests, the benchmark and Python callers.  It never falls back to a CPU path:
+if the library is missing or no GPU is present, calls raise.
+
+Device buffers are passed as integer device pointers (e.g. torch's
+``tensor.data_ptr()``); streams as integer ``cudaStream_t`` handles.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import formats  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libk2g.so")
+
+OK = 0
+STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_FORMAT", 4: "ERR_CUDA",
+                5: "ERR_NOMEM", 6: "ERR_CAPACITY", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT",
+                9: "ERR_BUDGET"}
+MODE_PLAIN = 0
+MODE_PERSISTENT = 1
+CODE_MATE_BORDER = 0xFFFFFFFF
+CODE_AMBIGUOUS = 0xFFFFFFFD
+
+# Every symbol include/k2g.h declares.
+EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g_db_close",
+           "k2g_db_info_get", "k2g_db_write_hash", "k2g_db_download", "k2g_lookup",
+           "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
+           "k2g_host_alloc", "k2g_host_free", "k2g_build_insert"]
+
+
+class K2GError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class IndexOptions(C.Structure):
+    _fields_ = [("k", C.c_uint64), ("l", C.c_uint64), ("spaced_seed_mask", C.c_uint64),
+                ("toggle_mask", C.c_uint64), ("dna_db", C.c_int32), ("revcom_version", C.c_int32),
+                ("minimum_acceptable_hash_value", C.c_uint64)]
+
+
+class DbInfo(C.Structure):
+    _fields_ = [("capacity", C.c_uint64), ("size", C.c_uint64), ("key_bits", C.c_uint64),
+                ("value_bits", C.c_uint64), ("node_count", C.c_uint64), ("opts", IndexOptions),
+                ("d_cells", C.c_void_p), ("d_parent", C.c_void_p), ("device", C.c_int)]
+
+
+class ClassifyParams(C.Structure):
+    _fields_ = [("confidence", C.c_double), ("min_hit_groups", C.c_int32), ("quick", C.c_int32),
+                ("paired", C.c_int32), ("min_quality", C.c_int32)]
+
+
+class Reads(C.Structure):
+    _fields_ = [("d_bases", C.c_void_p), ("d_quals", C.c_void_p), ("d_seq_off", C.c_void_p),
+                ("n_frags", C.c_uint64), ("max_seq_len", C.c_uint64),
+                ("d_frag_block", C.c_void_p), ("frag_base", C.c_uint64)]
+
+
+class Results(C.Structure):
+    _fields_ = [("d_call", C.c_void_p), ("d_hit_groups", C.c_void_p),
+                ("d_hitlist_off", C.c_void_p), ("d_hitlist_len", C.c_void_p),
+                ("d_runs", C.c_void_p), ("runs_cap", C.c_uint64), ("d_taxon_reads", C.c_void_p), ("d_hit_keys", C.c_void_p),
+                ("d_hit_taxa", C.c_void_p), ("d_hit_order", C.c_void_p), ("hits_cap", C.c_uint64),
+                ("d_hits_used", C.c_void_p), ("d_status", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libk2g.so, building it first if this tree has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build as _b
+            _b.build()
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libk2g.so not found at {LIB_PATH}")
+        L = C.CDLL(LIB_PATH)
+        L.k2g_last_error.restype = C.c_char_p
+        L.k2g_version.restype = C.c_char_p
+        vp, u64, i32 = C.c_void_p, C.c_uint64, C.c_int
+        sig = {
+            "k2g_db_open": [C.c_char_p, C.c_char_p, C.c_char_p, i32, C.POINTER(vp)],
+            "k2g_db_create": [C.POINTER(IndexOptions), u64, C.c_uint32, C.c_uint32, vp, u64, i32,
+                              C.POINTER(vp)],
+            "k2g_db_close": [vp],
+            "k2g_db_info_get": [vp, C.POINTER(DbInfo)],
+            "k2g_db_write_hash": [vp, C.c_char_p],
+            "k2g_db_download": [vp, vp, C.POINTER(u64)],
+            "k2g_lookup": [vp, vp, vp, u64, vp],
+            "k2g_lookup_host": [vp, vp, vp, u64],
+            "k2g_scan": [vp, vp, vp, u64, vp, vp, vp],
+            "k2g_classify": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams), C.POINTER(Results),
+                             i32, vp],
+            "k2g_classify_host": [vp, vp, vp, vp, u64, C.POINTER(ClassifyParams), vp, vp, vp,
+                                  vp, C.POINTER(u64), vp],
+            "k2g_host_alloc": [C.POINTER(vp), C.c_size_t],
+            "k2g_host_free": [vp],
+            "k2g_build_insert": [vp, vp, vp, u64, i32, vp],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != OK:
+        raise K2GError(status, lib().k2g_last_error().decode(errors="replace"))
+
+
+def version() -> str:
+    return lib().k2g_version().decode()
+
+
+class Database:
+    """A Kraken 2 database resident in HBM (k2g_db)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    @classmethod
+    def open(cls, directory_or_paths, device: int = 0) -> "Database":
+        if isinstance(directory_or_paths, (tuple, list)):
+            hp, tp, op = directory_or_paths
+        else:
+            d = directory_or_paths
+            hp, tp, op = (os.path.join(d, n) for n in ("hash.k2d", "taxo.k2d", "opts.k2d"))
+        h = C.c_void_p()
+        check(lib().k2g_db_open(hp.encode(), tp.encode(), op.encode(), device, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def create(cls, opts: IndexOptions, capacity: int, key_bits: int, value_bits: int,
+               parent: np.ndarray, device: int = 0) -> "Database":
+        parent = np.ascontiguousarray(parent, dtype=np.uint64)
+        h = C.c_void_p()
+        check(lib().k2g_db_create(C.byref(opts), capacity, key_bits, value_bits,
+                                  parent.ctypes.data, len(parent), device, C.byref(h)))
+        return cls(h)
+
+    def close(self):
+        if self.h:
+            lib().k2g_db_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> DbInfo:
+        i = DbInfo()
+        check(lib().k2g_db_info_get(self.h, C.byref(i)))
+        return i
+
+    def download(self):
+        inf = self.info()
+        cells = np.zeros(inf.capacity, np.uint32)
+        size = C.c_uint64()
+        check(lib().k2g_db_download(self.h, cells.ctypes.data, C.byref(size)))
+        return cells, size.value
+
+    def write_hash(self, path: str):
+        check(lib().k2g_db_write_hash(self.h, path.encode()))
+
+    def lookup(self, d_keys: int, d_vals: int, n: int, stream: int = 0):
+        check(lib().k2g_lookup(self.h, d_keys, d_vals, n, stream))
+
+    def lookup_host(self, keys: np.ndarray) -> np.ndarray:
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        vals = np.zeros(len(keys), np.uint32)
+        check(lib().k2g_lookup_host(self.h, keys.ctypes.data, vals.ctypes.data, len(keys)))
+        return vals
+
+    def scan(self, d_bases: int, d_seq_off: int, n_seqs: int, d_mins: int, d_ambig: int,
+             stream: int = 0):
+        check(lib().k2g_scan(self.h, d_bases, d_seq_off, n_seqs, d_mins, d_ambig, stream))
+
+    def classify(self, reads: Reads, params: ClassifyParams, results: Results,
+                 mode: int = MODE_PERSISTENT, stream: int = 0):
+        check(lib().k2g_classify(self.h, C.byref(reads), C.byref(params), C.byref(results),
+                                 mode, stream))
+
+    def build_insert(self, d_keys: int, d_taxids: int, n: int, ordered: bool = False,
+                     stream: int = 0):
+        check(lib().k2g_build_insert(self.h, d_keys, d_taxids, n, int(ordered), stream))

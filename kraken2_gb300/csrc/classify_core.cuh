@@ -1,0 +1,505 @@
+// The per-fragment classification machine shared by the classify kernels.
+//
+// One thread owns one fragment (a read or a read pair) and walks it in
+// segments.  Each segment runs three phases in lock step across the warp:
+//   scan    minimizers of the next stretch of bases, grouped into the
+//           reference's token kinds (src/classify.cc:797-838), distinct
+//           lookup keys appended to a per-lane key list;
+//   probe   CompactHashTable::Get for every key of the segment with several
+//           table loads in flight per lane (src/compact_hash.h:355-392);
+//   replay  hit counting, minimizer hit groups, quick mode and the hit-list
+//           runs (src/classify.cc:847-888, :950-991).
+// When a fragment's last segment has been replayed, ResolveTree
+// (src/classify.cc:710-762) picks the call.
+//
+// Per-lane buffers live in shared memory interleaved by lane (element j of
+// lane i at j*32+i), so any per-lane index is bank-conflict free.
+#pragma once
+
+#include "k2g_device.cuh"
+
+namespace k2g {
+
+// Group kinds of the compressed token stream.  A group is a run of tokens
+// with one taxon: KEY (a LOOKUP token and the REPEAT tokens after it), SKIP
+// (min-hash subsampled minimizer and its repeats), CONT (repeats continuing
+// the previous KEY/SKIP group after a segment boundary, an ambiguous stretch
+// or the group length limit), AMBIG (ambiguous k-mers) and BORDER (the mate
+// pair marker).
+enum : uint32_t { G_NONE = 0, G_KEY = 1, G_SKIP = 2, G_CONT = 3, G_AMBIG = 4, G_BORDER = 5 };
+constexpr uint32_t kGroupLenBits = 13;
+constexpr uint32_t kGroupMaxLen = (1u << kGroupLenBits) - 1;
+
+__device__ __forceinline__ uint16_t make_group(uint32_t kind, uint32_t len) {
+  return (uint16_t)((kind << kGroupLenBits) | len);
+}
+
+// Sliding window of the last W l-mer candidates; W == 0 means the window is
+// a runtime value w <= 16.
+template <int W>
+struct Window {
+  static constexpr int N = W > 0 ? W : 16;
+  uint64_t r[N];
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int i = 0; i < N; i++) r[i] = ~0ull;
+  }
+  __device__ __forceinline__ void push(uint64_t c) {
+#pragma unroll
+    for (int i = 0; i + 1 < N; i++) r[i] = r[i + 1];
+    r[N - 1] = c;
+  }
+  __device__ __forceinline__ uint64_t min(int w) const {
+    uint64_t m = r[N - 1];
+#pragma unroll
+    for (int i = 0; i + 1 < N; i++)
+      if (W > 0 || i >= N - w) m = r[i] < m ? r[i] : m;
+    return m;
+  }
+};
+
+// Everything a classify kernel needs, passed by value.
+struct ClassifyArgs {
+  TableView table;
+  ScanView scan;
+  ClassifyView cls;
+  const uint32_t *parent;
+  const uint8_t *bases;
+  const uint8_t *quals;            // may be null
+  const uint64_t *seq_off;
+  uint64_t n_frags;
+  uint64_t frag_base;
+  // outputs
+  uint32_t *call;
+  uint32_t *hit_groups;
+  uint64_t *hitlist_off;
+  uint32_t *hitlist_len;
+  uint64_t *runs;
+  uint64_t runs_cap;
+  unsigned long long *taxon_reads;
+  uint64_t *hit_keys;
+  uint32_t *hit_taxa;
+  uint64_t *hit_order;
+  uint64_t hits_cap;
+  unsigned long long *hits_used;
+  uint32_t *status;
+  // scheduling
+  unsigned long long *next_frag;   // persistent work counter
+  unsigned long long *defer_count; // fragments whose taxon map overflowed
+  uint64_t *defer_list;
+  uint64_t defer_cap;
+  const uint64_t *frag_list;       // optional indirection (slow path)
+  // slow-path scratch (global memory per thread)
+  uint64_t *scratch;
+  uint64_t scratch_stride;         // 64-bit words per thread
+};
+
+// Per-lane storage accessors.  Shared-memory flavour: interleaved by lane.
+template <int KCAP, int GCAP, int MCAP>
+struct SmemStore {
+  static constexpr int kKeys = KCAP, kGroups = GCAP, kMap = MCAP;
+  uint64_t *keys;     // [KCAP][32]
+  uint16_t *groups;   // [GCAP][32]
+  uint32_t *mkey;     // [MCAP][32]
+  uint32_t *mcnt;     // [MCAP][32]
+  int lane;
+  __device__ __forceinline__ uint64_t &key(int j) { return keys[j * 32 + lane]; }
+  __device__ __forceinline__ uint32_t &val(int j) { return reinterpret_cast<uint32_t *>(keys)[(j * 32 + lane) * 2]; }
+  __device__ __forceinline__ uint16_t &group(int g) { return groups[g * 32 + lane]; }
+  __device__ __forceinline__ uint32_t &map_key(int s) { return mkey[s * 32 + lane]; }
+  __device__ __forceinline__ uint32_t &map_cnt(int s) { return mcnt[s * 32 + lane]; }
+  __host__ __device__ static constexpr int map_cap() { return MCAP; }
+  __host__ __device__ static constexpr size_t bytes_per_warp() {
+    return (size_t)32 * (KCAP * 8 + GCAP * 2 + MCAP * 8);
+  }
+};
+
+// Global-memory flavour for the slow path: one contiguous region per thread.
+template <int KCAP, int GCAP>
+struct GlobalStore {
+  static constexpr int kKeys = KCAP, kGroups = GCAP;
+  uint64_t *keys;
+  uint16_t *groups;
+  uint32_t *mkey;
+  uint32_t *mcnt;
+  int mcap;
+  __device__ __forceinline__ uint64_t &key(int j) { return keys[j]; }
+  __device__ __forceinline__ uint32_t &val(int j) { return reinterpret_cast<uint32_t *>(keys)[j * 2]; }
+  __device__ __forceinline__ uint16_t &group(int g) { return groups[g]; }
+  __device__ __forceinline__ uint32_t &map_key(int s) { return mkey[s]; }
+  __device__ __forceinline__ uint32_t &map_cnt(int s) { return mcnt[s]; }
+  __device__ __forceinline__ int map_cap() const { return mcap; }
+};
+
+// Per-lane fragment state carried across segments (registers).
+template <int W>
+struct Lane {
+  uint64_t frag;          // fragment index within the batch, ~0 = none
+  // scan position
+  const uint8_t *seq;
+  const uint8_t *qual;
+  uint32_t len, pos;
+  uint32_t len2;          // second mate length (paired)
+  const uint8_t *seq2;
+  const uint8_t *qual2;
+  uint32_t mate;
+  uint32_t word, qword;   // cached 4 bytes of bases / qualities
+  uint64_t fwd, rc;
+  int32_t run, last_amb;
+  Window<W> win;
+  uint64_t last_min;
+  uint32_t gkind, glen;   // open group
+  bool scan_done;
+  // replay
+  uint32_t cur_taxon;
+  uint32_t run_code, run_cnt, n_runs;
+  uint32_t hit_groups;
+  uint32_t total_tokens;
+  uint32_t key_ordinal;
+  uint32_t distinct;
+  bool quick_stop;
+  uint64_t run_base;
+};
+
+template <int W>
+__device__ __forceinline__ void lane_reset_mate(Lane<W> &s) {
+  s.pos = 0;
+  s.fwd = s.rc = 0;
+  s.run = 0;
+  s.last_amb = -1;
+  s.win.reset();
+  s.last_min = ~0ull;
+}
+
+template <int W>
+__device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, uint64_t f) {
+  s.frag = f;
+  const int per = a.cls.paired ? 2 : 1;
+  uint64_t o0 = a.seq_off[f * per], o1 = a.seq_off[f * per + 1];
+  s.seq = a.bases + o0;
+  s.qual = a.quals ? a.quals + o0 : nullptr;
+  s.len = (uint32_t)(o1 - o0);
+  if (per == 2) {
+    uint64_t o2 = a.seq_off[f * per + 2];
+    s.seq2 = a.bases + o1;
+    s.qual2 = a.quals ? a.quals + o1 : nullptr;
+    s.len2 = (uint32_t)(o2 - o1);
+  } else {
+    s.seq2 = nullptr;
+    s.qual2 = nullptr;
+    s.len2 = 0;
+  }
+  s.mate = 0;
+  lane_reset_mate(s);
+  s.gkind = G_NONE;
+  s.glen = 0;
+  s.scan_done = false;
+  s.cur_taxon = 0;
+  s.run_code = 0;
+  s.run_cnt = 0;
+  s.n_runs = 0;
+  s.hit_groups = 0;
+  s.total_tokens = 0;
+  s.key_ordinal = 0;
+  s.distinct = 0;
+  s.quick_stop = false;
+  s.run_base = o0 + 2 * f;
+}
+
+// Byte p of a sequence through a 4-byte cache of aligned words.  Aligned
+// 4-byte loads never leave the allocation that holds byte p.
+__device__ __forceinline__ uint32_t fetch_byte(const uint8_t *base, uint32_t p, uint32_t &cache) {
+  uintptr_t addr = (uintptr_t)(base + p);
+  uint32_t sh = (uint32_t)(addr & 3u);
+  if (p == 0 || sh == 0) cache = __ldg(reinterpret_cast<const uint32_t *>(addr & ~(uintptr_t)3));
+  return (cache >> (8 * sh)) & 0xFFu;
+}
+
+// ---- scan phase ----------------------------------------------------------
+// Scans until the fragment ends or the segment buffers are (nearly) full.
+// The closed form used here is equivalent to MinimizerScanner::NextMinimizer
+// (src/mmscanner.cc:114-189): the k-mer ending at base p is ambiguous iff an
+// ambiguous base lies in [p-k+2, p] (k > l) or [p-k+1, p] (k == l), and its
+// minimizer is the minimum over the l-mers ending in [p-w+1, p] whose bases
+// are all unambiguous, of (canonical(l-mer) & mask) ^ toggle, xor toggle.
+template <int W, class Store>
+__device__ __forceinline__ void scan_segment(Lane<W> &s, Store &st, const ClassifyArgs &a,
+                                             int &ng, int &nk) {
+  const ScanView &sv = a.scan;
+  const int k = sv.k, l = sv.l;
+  const int amb_span = (k == l) ? k - 1 : k - 2;   // p - last_amb <= amb_span -> ambiguous
+  const uint64_t top_shift = 2ull * (l - 1);
+  const bool use_quals = a.cls.min_quality > 0;
+  ng = 0;
+  nk = 0;
+  while (true) {
+    if (ng >= Store::kGroups - 2 || nk >= Store::kKeys) break;
+    if (s.pos >= s.len) {
+      if (s.gkind != G_NONE) { st.group(ng++) = make_group(s.gkind, s.glen); s.gkind = G_NONE; }
+      if (a.cls.paired && s.mate == 0) {
+        st.group(ng++) = make_group(G_BORDER, 1);
+        s.mate = 1;
+        s.seq = s.seq2;
+        s.qual = s.qual2;
+        s.len = s.len2;
+        lane_reset_mate(s);
+        continue;
+      }
+      s.scan_done = true;
+      break;
+    }
+    const uint32_t p = s.pos;
+    uint32_t c = fetch_byte(s.seq, p, s.word);
+    uint32_t code = dna_code(c);
+    if (use_quals && s.qual) {
+      int q = (int)(signed char)fetch_byte(s.qual, p, s.qword);
+      if (q - '!' < a.cls.min_quality) code = 0xFFu;     // masked to 'x'
+    }
+    uint64_t cand = ~0ull;
+    if (code != 0xFFu) {
+      s.fwd = ((s.fwd << 2) | code) & sv.lmer_mask;
+      s.rc = (s.rc >> 2) | ((uint64_t)(code ^ 3u) << top_shift);
+      s.run++;
+      if (s.run >= l) {
+        uint64_t rcv = sv.revcom_version ? s.rc : revcomp_v0(s.fwd, sv.lmer_mask);
+        uint64_t canon = s.fwd < rcv ? s.fwd : rcv;
+        if (sv.spaced_mask) canon &= sv.spaced_mask;
+        cand = canon ^ sv.toggle;
+      }
+    } else {
+      s.run = 0;
+      s.last_amb = (int32_t)p;
+    }
+    s.win.push(cand);
+    s.pos = p + 1;
+    if ((int)p < k - 1) continue;
+    // one token for the k-mer ending at p
+    if ((int32_t)p - s.last_amb <= amb_span) {
+      if (s.gkind == G_AMBIG && s.glen < kGroupMaxLen) {
+        s.glen++;
+      } else {
+        if (s.gkind != G_NONE) st.group(ng++) = make_group(s.gkind, s.glen);
+        s.gkind = G_AMBIG;
+        s.glen = 1;
+      }
+      continue;
+    }
+    uint64_t m = s.win.min(sv.w) ^ sv.toggle;
+    if (m != s.last_min) {
+      s.last_min = m;
+      if (s.gkind != G_NONE) st.group(ng++) = make_group(s.gkind, s.glen);
+      s.glen = 1;
+      if (sv.min_hash && murmur3(m) < sv.min_hash) {
+        s.gkind = G_SKIP;
+      } else {
+        s.gkind = G_KEY;
+        st.key(nk++) = m;
+      }
+    } else if ((s.gkind == G_KEY || s.gkind == G_SKIP || s.gkind == G_CONT) &&
+               s.glen < kGroupMaxLen) {
+      s.glen++;
+    } else {
+      if (s.gkind != G_NONE) st.group(ng++) = make_group(s.gkind, s.glen);
+      s.gkind = G_CONT;
+      s.glen = 1;
+    }
+  }
+  // close the open group at a segment boundary; a following REPEAT opens CONT
+  if (s.gkind != G_NONE) {
+    st.group(ng++) = make_group(s.gkind, s.glen);
+    s.gkind = G_NONE;
+  }
+}
+
+// ---- probe phase ---------------------------------------------------------
+// With -K, every key whose value is nonzero becomes an add_kmer event
+// (src/classify.cc:869-873) tagged with (fragment ordinal, key ordinal); the
+// key ordinal is monotone in token order within the fragment.
+__device__ __forceinline__ void emit_hit(const ClassifyArgs &a, uint64_t frag, uint32_t ordinal,
+                                         uint64_t key, uint32_t taxon) {
+  unsigned long long at = atomicAdd(a.hits_used, 1ull);
+  if (at < a.hits_cap) {
+    a.hit_keys[at] = key;
+    a.hit_taxa[at] = taxon;
+    a.hit_order[at] = ((a.frag_base + frag) << 32) | ordinal;
+  } else {
+    atomicOr(a.status, STATUS_HITS_OVERFLOW);
+  }
+}
+
+template <class Store>
+__device__ __forceinline__ void probe_segment(Store &st, const ClassifyArgs &a, int nk,
+                                              uint64_t frag, uint32_t key_ordinal) {
+  constexpr int B = 4;
+  const TableView &t = a.table;
+  for (int j0 = 0; j0 < nk; j0 += B) {
+    uint64_t hc[B], idx[B];
+    uint32_t cell[B];
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+      if (j0 + b < nk) {
+        hc[b] = murmur3(st.key(j0 + b));
+        idx[b] = fast_mod(hc[b], t.div);
+        cell[b] = load_cell(t.cells + idx[b]);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+      if (j0 + b < nk) {
+        uint32_t v = probe_from(t, hc[b], idx[b], cell[b]);
+        if (a.hit_keys && v) emit_hit(a, frag, key_ordinal + j0 + b, st.key(j0 + b), v);
+        st.val(j0 + b) = v;
+      }
+    }
+  }
+}
+
+// Per-lane taxon -> count map (open addressing, key 0 = empty).  Returns
+// false when the map is too full; the fragment then takes the slow path.
+template <class Store>
+__device__ __forceinline__ bool map_add(Store &st, uint32_t &distinct, uint32_t taxon,
+                                        uint32_t n) {
+  const int cap = st.map_cap();
+  int i = (int)((taxon * 0x9E3779B1u) >> 16) & (cap - 1);
+  while (true) {
+    uint32_t k = st.map_key(i);
+    if (k == taxon) { st.map_cnt(i) += n; return true; }
+    if (k == 0) {
+      if (4 * (distinct + 1) > 3 * (uint32_t)cap) return false;
+      st.map_key(i) = taxon;
+      st.map_cnt(i) = n;
+      distinct++;
+      return true;
+    }
+    i = (i + 1) & (cap - 1);
+  }
+}
+
+template <class Store>
+__device__ __forceinline__ uint32_t map_get(Store &st, uint32_t taxon) {
+  if (!taxon) return 0;
+  const int cap = st.map_cap();
+  int i = (int)((taxon * 0x9E3779B1u) >> 16) & (cap - 1);
+  while (true) {
+    uint32_t k = st.map_key(i);
+    if (k == taxon) return st.map_cnt(i);
+    if (k == 0) return 0;
+    i = (i + 1) & (cap - 1);
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void emit_run(Lane<W> &s, const ClassifyArgs &a, uint32_t code,
+                                         uint32_t n) {
+  if (s.run_cnt && s.run_code == code) {
+    s.run_cnt += n;
+    return;
+  }
+  if (s.run_cnt) {
+    uint64_t at = s.run_base + s.n_runs;
+    if (at < a.runs_cap) a.runs[at] = ((uint64_t)s.run_code << 32) | s.run_cnt;
+    else atomicOr(a.status, STATUS_RUNS_OVERFLOW);
+    s.n_runs++;
+  }
+  s.run_code = code;
+  s.run_cnt = n;
+}
+
+// ---- replay phase --------------------------------------------------------
+// Returns false if the taxon map overflowed.
+template <int W, class Store>
+__device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const ClassifyArgs &a,
+                                               int ng) {
+  int ki = 0;
+  for (int g = 0; g < ng; g++) {
+    uint32_t grp = st.group(g);
+    uint32_t kind = grp >> kGroupLenBits, len = grp & kGroupMaxLen;
+    uint32_t taxon;
+    if (kind == G_AMBIG) {
+      emit_run(s, a, K2G_CODE_AMBIGUOUS, len);
+      s.total_tokens += len;
+      continue;
+    }
+    if (kind == G_BORDER) {
+      emit_run(s, a, K2G_CODE_MATE_BORDER, 1);
+      s.total_tokens += 1;
+      continue;
+    }
+    if (kind == G_KEY) {
+      taxon = st.val(ki);
+      s.cur_taxon = taxon;
+      if (taxon) {
+        s.hit_groups++;
+        if (a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
+          s.quick_stop = true;
+          return true;
+        }
+      }
+      ki++;
+    } else if (kind == G_SKIP) {
+      taxon = 0;
+      s.cur_taxon = 0;
+    } else {
+      taxon = s.cur_taxon;
+    }
+    if (taxon && !map_add(st, s.distinct, taxon, len)) return false;
+    emit_run(s, a, taxon, len);
+    s.total_tokens += len;
+  }
+  return true;
+}
+
+// ---- resolve and write -------------------------------------------------
+template <int W, class Store>
+__device__ __forceinline__ void finish_fragment(Lane<W> &s, Store &st, const ClassifyArgs &a) {
+  const uint32_t *parent = a.parent;
+  uint32_t total = s.total_tokens;
+  if (a.cls.paired) total -= 1;
+  // ResolveTree (src/classify.cc:710-762)
+  uint32_t max_taxon = 0, max_score = 0;
+  const uint32_t required =
+      (uint32_t)ceil(__dmul_rn(a.cls.confidence, (double)total));
+  const int cap = st.map_cap();
+  for (int i = 0; i < cap; i++) {
+    uint32_t t = st.map_key(i);
+    if (!t) continue;
+    uint32_t score = 0;
+    for (uint32_t x = t; x; x = __ldg(parent + x)) score += map_get(st, x);
+    if (score > max_score) {
+      max_score = score;
+      max_taxon = t;
+    } else if (score == max_score) {
+      max_taxon = lca(parent, max_taxon, t);
+    }
+  }
+  max_score = map_get(st, max_taxon);
+  uint32_t call = max_taxon;
+  while (call && max_score < required) {
+    max_score = 0;
+    for (int i = 0; i < cap; i++) {
+      uint32_t t = st.map_key(i);
+      if (t && is_ancestor(parent, call, t)) max_score += st.map_cnt(i);
+    }
+    if (max_score >= required) break;
+    call = __ldg(parent + call);
+  }
+  if (call && (int32_t)s.hit_groups < a.cls.min_hit_groups) call = 0;
+  // close the last run
+  if (s.run_cnt) {
+    uint64_t at = s.run_base + s.n_runs;
+    if (at < a.runs_cap) a.runs[at] = ((uint64_t)s.run_code << 32) | s.run_cnt;
+    else atomicOr(a.status, STATUS_RUNS_OVERFLOW);
+    s.n_runs++;
+    s.run_cnt = 0;
+  }
+  const uint64_t f = s.frag;
+  a.call[f] = call;
+  if (a.hit_groups) a.hit_groups[f] = s.hit_groups;
+  if (a.hitlist_off) a.hitlist_off[f] = s.run_base;
+  if (a.hitlist_len) a.hitlist_len[f] = s.n_runs;
+  if (call && a.taxon_reads) atomicAdd(a.taxon_reads + call, 1ull);
+  // clear this lane's map for the next fragment
+  for (int i = 0; i < cap; i++) st.map_key(i) = 0;
+}
+
+}  // namespace k2g

@@ -1,0 +1,288 @@
+// k2g_classify_host: classification of reads held in host memory.
+//
+// The input is cut into chunks.  Each chunk is copied in, classified and its
+// results copied out on one of two streams, so the copies of one chunk
+// overlap the kernels of the other.  Hit-list runs are compacted on the
+// device (exclusive scan of the per-fragment run counts, then a gather) so
+// only the used runs cross back to the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "k2g_internal.h"
+
+namespace k2g {
+
+constexpr int kScanBlock = 1024;
+
+// Block-level exclusive scan of n counts; block totals to sums[].
+__global__ void scan_blocks_kernel(const uint32_t *in, uint64_t *out, uint64_t *sums, uint64_t n) {
+  __shared__ uint64_t warp_tot[32];
+  uint64_t i = blockIdx.x * (uint64_t)kScanBlock + threadIdx.x;
+  uint64_t v = i < n ? in[i] : 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint64_t t = warp_tot[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      uint64_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    warp_tot[lane] = t;
+  }
+  __syncthreads();
+  uint64_t excl = x - v + (w ? warp_tot[w - 1] : 0);
+  if (i < n) out[i] = excl;
+  if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = excl + v;
+}
+
+// Exclusive scan of up to kScanBlock*kScanBlock block sums in one block.
+__global__ void scan_sums_kernel(uint64_t *sums, uint64_t nb, uint64_t *total) {
+  __shared__ uint64_t buf[kScanBlock];
+  uint64_t carry = 0;
+  for (uint64_t base = 0; base < nb; base += kScanBlock) {
+    uint64_t i = base + threadIdx.x;
+    uint64_t v = i < nb ? sums[i] : 0;
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+      uint64_t y = threadIdx.x >= (unsigned)o ? buf[threadIdx.x - o] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += y;
+      __syncthreads();
+    }
+    uint64_t incl = buf[threadIdx.x];
+    if (i < nb) sums[i] = carry + incl - v;
+    __syncthreads();
+    carry += buf[kScanBlock - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+// Adds block offsets and gathers each fragment's runs into the dense array.
+__global__ void gather_runs_kernel(const uint64_t *sparse, const uint64_t *seq_off, int per,
+                                   const uint32_t *len, uint64_t *excl, const uint64_t *sums,
+                                   uint64_t n, uint64_t *dense) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t o = excl[i] + sums[i / kScanBlock];
+  const uint64_t src = seq_off[i * per] + 2 * i;
+  for (uint32_t r = 0; r < len[i]; r++) dense[o + r] = sparse[src + r];
+}
+
+__global__ void rebase_kernel(uint64_t *off, uint64_t n, uint64_t base) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n) off[i] -= base;
+}
+
+k2g_status compact_runs(const uint64_t *d_sparse, const uint64_t *d_seq_off, int per,
+                        const uint32_t *d_len, uint64_t n, uint64_t *d_excl, uint64_t *d_sums,
+                        uint64_t *d_total, uint64_t *d_dense, cudaStream_t st) {
+  uint64_t nb = (n + kScanBlock - 1) / kScanBlock;
+  scan_blocks_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(d_len, d_excl, d_sums, n);
+  scan_sums_kernel<<<1, kScanBlock, 0, st>>>(d_sums, nb, d_total);
+  gather_runs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_sparse, d_seq_off, per, d_len,
+                                                                 d_excl, d_sums, n, d_dense);
+  K2G_CUDA_TRY(cudaGetLastError());
+  return K2G_OK;
+}
+
+}  // namespace k2g
+
+using namespace k2g;
+
+namespace {
+
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  char *bases = nullptr, *quals = nullptr;
+  uint64_t *off = nullptr;
+  uint32_t *call = nullptr, *hg = nullptr, *hlen = nullptr, *status = nullptr;
+  uint64_t *sparse = nullptr, *dense = nullptr, *excl = nullptr, *sums = nullptr;
+  uint64_t *total = nullptr;       // device
+  uint64_t *h_total = nullptr;     // pinned
+  // chunk bookkeeping for the deferred runs copy
+  bool pending = false;
+  uint64_t f0 = 0, nf = 0;
+};
+
+void free_slot(Slot &s) {
+  if (s.st) cudaStreamSynchronize(s.st);
+  void *dev[] = {s.bases, s.quals, s.off, s.call, s.hg, s.hlen, s.status, s.sparse,
+                 s.dense, s.excl, s.sums, s.total};
+  for (void *p : dev)
+    if (p) cudaFree(p);
+  if (s.h_total) cudaFreeHost(s.h_total);
+  if (s.done) cudaEventDestroy(s.done);
+  if (s.st) cudaStreamDestroy(s.st);
+}
+
+}  // namespace
+
+extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, const char *quals,
+                                        const uint64_t *seq_off, uint64_t n_frags,
+                                        const k2g_classify_params *params, uint32_t *call,
+                                        uint32_t *hit_groups, uint32_t *hitlist_len,
+                                        uint64_t *runs, uint64_t *n_runs,
+                                        uint64_t *taxon_reads) {
+  if (!db || !bases || !seq_off || !params || !call) return fail(K2G_ERR_ARG, "null argument");
+  if (runs && !n_runs) return fail(K2G_ERR_ARG, "runs given without n_runs capacity");
+  const uint64_t runs_cap = runs ? *n_runs : 0;
+  if (n_runs) *n_runs = 0;
+  if (!n_frags) return K2G_OK;
+  K2G_CUDA_TRY(cudaSetDevice(db->device));
+  const int per = params->paired ? 2 : 1;
+  const uint64_t n_seqs = n_frags * per;
+
+  // chunk plan: ~256 MB of bases or 2M fragments per chunk
+  const uint64_t max_bases = 256ull << 20, max_frags = 2ull << 20;
+  std::vector<uint64_t> cuts{0};
+  {
+    uint64_t f = 0;
+    while (f < n_frags) {
+      uint64_t g = f;
+      uint64_t b0 = seq_off[f * per];
+      while (g < n_frags && g - f < max_frags && seq_off[(g + 1) * per] - b0 <= max_bases) g++;
+      if (g == f) g = f + 1;   // a single oversized fragment forms its own chunk
+      cuts.push_back(g);
+      f = g;
+    }
+  }
+  uint64_t chunk_frags = 0, chunk_bases = 0, max_len = 0;
+  for (size_t c = 0; c + 1 < cuts.size(); c++) {
+    chunk_frags = std::max(chunk_frags, cuts[c + 1] - cuts[c]);
+    chunk_bases = std::max(chunk_bases, seq_off[cuts[c + 1] * per] - seq_off[cuts[c] * per]);
+  }
+  for (uint64_t i = 0; i < n_seqs; i++) max_len = std::max(max_len, seq_off[i + 1] - seq_off[i]);
+
+  unsigned long long *d_taxon_reads = nullptr;
+  if (taxon_reads) {
+    K2G_CUDA_TRY(cudaMalloc(&d_taxon_reads, db->node_count * 8));
+    K2G_CUDA_TRY(cudaMemset(d_taxon_reads, 0, db->node_count * 8));
+  }
+  Slot slots[2];
+  k2g_status status = K2G_OK;
+  auto cleanup = [&]() {
+    for (auto &s : slots) free_slot(s);
+    if (d_taxon_reads) cudaFree(d_taxon_reads);
+  };
+#define SLOT_TRY(call_)                                     \
+  do {                                                      \
+    cudaError_t _e = (call_);                               \
+    if (_e != cudaSuccess) {                                \
+      status = cuda_fail((int)_e, #call_);                  \
+      cleanup();                                            \
+      return status;                                        \
+    }                                                       \
+  } while (0)
+  const uint64_t sparse_cap = chunk_bases + 2 * chunk_frags + 8;
+  for (auto &s : slots) {
+    SLOT_TRY(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    SLOT_TRY(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    SLOT_TRY(cudaMalloc(&s.bases, chunk_bases + 16));
+    if (quals) SLOT_TRY(cudaMalloc(&s.quals, chunk_bases + 16));
+    SLOT_TRY(cudaMalloc(&s.off, (chunk_frags * per + 1) * 8));
+    SLOT_TRY(cudaMalloc(&s.call, chunk_frags * 4));
+    SLOT_TRY(cudaMalloc(&s.hg, chunk_frags * 4));
+    SLOT_TRY(cudaMalloc(&s.hlen, chunk_frags * 4));
+    SLOT_TRY(cudaMalloc(&s.status, 4));
+    SLOT_TRY(cudaMalloc(&s.sparse, sparse_cap * 8));
+    SLOT_TRY(cudaMalloc(&s.dense, sparse_cap * 8));
+    SLOT_TRY(cudaMalloc(&s.excl, chunk_frags * 8));
+    SLOT_TRY(cudaMalloc(&s.sums, ((chunk_frags + kScanBlock - 1) / kScanBlock + 1) * 8));
+    SLOT_TRY(cudaMalloc(&s.total, 8));
+    SLOT_TRY(cudaHostAlloc(&s.h_total, 8, cudaHostAllocDefault));
+  }
+
+  uint64_t runs_written = 0;
+  // Copies the runs of a finished chunk (needs its run total on the host).
+  auto drain = [&](Slot &s) -> k2g_status {
+    if (!s.pending) return K2G_OK;
+    cudaError_t e = cudaEventSynchronize(s.done);
+    if (e != cudaSuccess) return cuda_fail(e, "chunk completion");
+    s.pending = false;
+    uint32_t st_word = 0;
+    e = cudaMemcpy(&st_word, s.status, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "status readback");
+    if (st_word) return fail(K2G_ERR_CAPACITY, "classification buffer overflow");
+    uint64_t nr = *s.h_total;
+    if (runs) {
+      if (runs_written + nr > runs_cap) return fail(K2G_ERR_CAPACITY, "runs buffer too small");
+      e = cudaMemcpy(runs + runs_written, s.dense, nr * 8, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "runs copy");
+    }
+    runs_written += nr;
+    return K2G_OK;
+  };
+
+  for (size_t c = 0; c + 1 < cuts.size(); c++) {
+    Slot &s = slots[c & 1];
+    status = drain(s);
+    if (status != K2G_OK) { cleanup(); return status; }
+    const uint64_t f0 = cuts[c], nf = cuts[c + 1] - f0;
+    const uint64_t b0 = seq_off[f0 * per], nb = seq_off[(f0 + nf) * per] - b0;
+    SLOT_TRY(cudaMemcpyAsync(s.bases, bases + b0, nb, cudaMemcpyHostToDevice, s.st));
+    if (quals) SLOT_TRY(cudaMemcpyAsync(s.quals, quals + b0, nb, cudaMemcpyHostToDevice, s.st));
+    SLOT_TRY(cudaMemcpyAsync(s.off, seq_off + f0 * per, (nf * per + 1) * 8,
+                             cudaMemcpyHostToDevice, s.st));
+    rebase_kernel<<<(unsigned)((nf * per + 1 + 255) / 256), 256, 0, s.st>>>(s.off, nf * per + 1, b0);
+    SLOT_TRY(cudaMemsetAsync(s.status, 0, 4, s.st));
+    k2g_reads rd{};
+    rd.d_bases = s.bases;
+    rd.d_quals = quals ? s.quals : nullptr;
+    rd.d_seq_off = s.off;
+    rd.n_frags = nf;
+    rd.max_seq_len = max_len;
+    rd.frag_base = f0;
+    k2g_results rs{};
+    rs.d_call = s.call;
+    rs.d_hit_groups = s.hg;
+    rs.d_hitlist_len = s.hlen;
+    rs.d_runs = s.sparse;
+    rs.runs_cap = sparse_cap;
+    rs.d_taxon_reads = reinterpret_cast<uint64_t *>(d_taxon_reads);
+    rs.d_status = s.status;
+    status = k2g_classify(db, &rd, params, &rs, K2G_MODE_PERSISTENT, s.st);
+    if (status != K2G_OK) { cleanup(); return status; }
+    status = compact_runs(s.sparse, s.off, per, s.hlen, nf, s.excl, s.sums, s.total, s.dense, s.st);
+    if (status != K2G_OK) { cleanup(); return status; }
+    SLOT_TRY(cudaMemcpyAsync(s.h_total, s.total, 8, cudaMemcpyDeviceToHost, s.st));
+    SLOT_TRY(cudaMemcpyAsync(call + f0, s.call, nf * 4, cudaMemcpyDeviceToHost, s.st));
+    if (hit_groups)
+      SLOT_TRY(cudaMemcpyAsync(hit_groups + f0, s.hg, nf * 4, cudaMemcpyDeviceToHost, s.st));
+    if (hitlist_len)
+      SLOT_TRY(cudaMemcpyAsync(hitlist_len + f0, s.hlen, nf * 4, cudaMemcpyDeviceToHost, s.st));
+    SLOT_TRY(cudaEventRecord(s.done, s.st));
+    s.pending = true;
+    s.f0 = f0;
+    s.nf = nf;
+    // keep chunk order for the runs: drain the other slot (older chunk) now
+    Slot &o = slots[(c + 1) & 1];
+    status = drain(o);
+    if (status != K2G_OK) { cleanup(); return status; }
+  }
+  for (size_t c = cuts.size() - 1; c < cuts.size() + 1; c++) {
+    status = drain(slots[c & 1]);
+    if (status != K2G_OK) { cleanup(); return status; }
+  }
+  if (taxon_reads) {
+    std::vector<uint64_t> tr(db->node_count);
+    cudaError_t e = cudaMemcpy(tr.data(), d_taxon_reads, db->node_count * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { status = cuda_fail(e, "taxon reads"); cleanup(); return status; }
+    for (uint64_t i = 0; i < db->node_count; i++) taxon_reads[i] += tr[i];
+  }
+  if (n_runs) *n_runs = runs_written;
+  cleanup();
+  return K2G_OK;
+#undef SLOT_TRY
+}

@@ -1,0 +1,86 @@
+// Device-side building blocks shared by the libk2g kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "k2g_internal.h"
+
+namespace k2g {
+
+// 64-bit MurmurHash3 finalizer (src/kv_store.h:59-67).
+__device__ __forceinline__ uint64_t murmur3(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdULL;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ULL;
+  k ^= k >> 33;
+  return k;
+}
+
+// n % d through the invariant-divisor magic (see DivMagic).
+__device__ __forceinline__ uint64_t fast_mod(uint64_t n, const DivMagic &m) {
+  uint64_t t = __umul64hi(m.m, n);
+  uint64_t q = (t + ((n - t) >> m.sh1)) >> m.sh2;
+  return n - q * m.d;
+}
+
+// Read-only, L1-cached load of one table cell.
+__device__ __forceinline__ uint32_t load_cell(const uint32_t *p) { return __ldg(p); }
+
+// CompactHashTable::Get with linear probing (src/compact_hash.h:355-374),
+// continuing from an already loaded home cell.
+__device__ __forceinline__ uint32_t probe_from(const TableView &t, uint64_t hc, uint64_t idx,
+                                               uint32_t cell) {
+  const uint32_t ck = (uint32_t)(hc >> t.key_shift);
+  const uint64_t first = idx;
+  while (true) {
+    uint32_t v = cell & t.value_mask;
+    if (!v) return 0;
+    if ((cell >> t.value_bits) == ck) return v;
+    idx = (idx + 1 == t.capacity) ? 0 : idx + 1;
+    if (idx == first) return 0;
+    cell = load_cell(t.cells + idx);
+  }
+}
+
+__device__ __forceinline__ uint32_t table_get(const TableView &t, uint64_t key) {
+  uint64_t hc = murmur3(key);
+  uint64_t idx = fast_mod(hc, t.div);
+  return probe_from(t, hc, idx, load_cell(t.cells + idx));
+}
+
+// DNA code of an ASCII base (src/mmscanner.cc:20-46): ACGT in either case map
+// to 0..3; anything else is ambiguous (returns 0xFF).
+__device__ __forceinline__ uint32_t dna_code(uint32_t c) {
+  uint32_t lower = c | 0x20u;
+  bool ok = (lower == 'a') | (lower == 'c') | (lower == 'g') | (lower == 't');
+  uint32_t code = ((c >> 1) ^ (c >> 2)) & 3u;
+  return ok ? code : 0xFFu;
+}
+
+// reverse_complement for revcom_version 0 (src/mmscanner.cc:210-211):
+// pairwise reversal of the whole 64-bit word, complement, low 2n bits.
+__device__ __forceinline__ uint64_t revcomp_v0(uint64_t x, uint64_t lmer_mask) {
+  uint64_t r = __brevll(x);
+  r = ((r >> 1) & 0x5555555555555555ULL) | ((r & 0x5555555555555555ULL) << 1);
+  return (~r) & lmer_mask;
+}
+
+// Taxonomy::LowestCommonAncestor (src/taxonomy.cc:262-272).
+__device__ __forceinline__ uint32_t lca(const uint32_t *parent, uint32_t a, uint32_t b) {
+  if (!a || !b) return a ? a : b;
+  while (a != b) {
+    if (a > b) a = __ldg(parent + a);
+    else b = __ldg(parent + b);
+  }
+  return a;
+}
+
+// Taxonomy::IsAAncestorOfB (src/taxonomy.cc:251-258).
+__device__ __forceinline__ bool is_ancestor(const uint32_t *parent, uint32_t a, uint32_t b) {
+  if (!a || !b) return false;
+  while (b > a) b = __ldg(parent + b);
+  return b == a;
+}
+
+}  // namespace k2g

@@ -1,0 +1,91 @@
+// Internal definitions shared by the host code and the CUDA kernels of libk2g.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "k2g.h"
+
+namespace k2g {
+
+// Exact unsigned 64-bit division by an invariant divisor, after Granlund &
+// Montgomery, "Division by Invariant Integers using Multiplication" (PLDI
+// 1994), Figure 4.1: with l = ceil(log2 d), m = floor(2^64 (2^l - d) / d) + 1,
+//   q = (t + ((n - t) >> sh1)) >> sh2,  t = mulhi(m, n),
+// sh1 = min(l, 1), sh2 = max(l - 1, 0).  Used for the reference's
+// `hash % capacity` (src/compact_hash.h:358) with a 64-bit capacity.
+struct DivMagic {
+  uint64_t d;
+  uint64_t m;
+  uint32_t sh1, sh2;
+};
+
+DivMagic make_div_magic(uint64_t d);
+
+// Read-only view of the table passed to kernels by value.
+struct TableView {
+  const uint32_t *cells;
+  uint64_t capacity;
+  DivMagic div;
+  uint32_t key_shift;     // 64 - key_bits
+  uint32_t value_bits;
+  uint32_t value_mask;    // (1 << value_bits) - 1
+};
+
+// Scanner parameters (IndexOptions + derived masks).
+struct ScanView {
+  int32_t k, l, w;        // w = k - l + 1 window of l-mers per k-mer
+  int32_t revcom_version;
+  uint64_t spaced_mask;   // 0 = none
+  uint64_t toggle;        // toggle_mask & lmer_mask (src/mmscanner.cc:34)
+  uint64_t lmer_mask;
+  uint64_t min_hash;      // minimum_acceptable_hash_value
+};
+
+// Classification parameters as kernels see them.
+struct ClassifyView {
+  double confidence;
+  int32_t min_hit_groups;
+  int32_t quick;
+  int32_t paired;
+  int32_t min_quality;
+};
+
+// Status word bits written by kernels into k2g_results::d_status.
+enum : uint32_t {
+  STATUS_RUNS_OVERFLOW = 1u,
+  STATUS_HITS_OVERFLOW = 2u,
+  STATUS_DEFER_OVERFLOW = 4u,
+  STATUS_BUILD_FULL = 8u,
+  STATUS_BUILD_VALUE = 16u,
+  STATUS_TIMEOUT = 32u,
+};
+
+}  // namespace k2g
+
+struct k2g_db {
+  int device = 0;
+  uint64_t capacity = 0, size = 0, key_bits = 0, value_bits = 0, node_count = 0;
+  k2g_index_options opts{};
+  uint32_t *d_cells = nullptr;    // capacity cells, padded to a multiple of 8
+  uint32_t *d_parent = nullptr;   // node_count entries
+  uint64_t *d_size = nullptr;     // device-side size counter used by builds
+  k2g::DivMagic div{};
+  bool owns_table = true;
+
+  k2g::TableView table_view() const;
+  k2g::ScanView scan_view() const;
+};
+
+namespace k2g {
+// Thread-local error message plumbing.
+k2g_status fail(k2g_status s, const std::string &msg);
+k2g_status cuda_fail(int err, const char *what);
+}  // namespace k2g
+
+#define K2G_CUDA_TRY(call)                                        \
+  do {                                                            \
+    cudaError_t _e = (call);                                      \
+    if (_e != cudaSuccess) return k2g::cuda_fail((int)_e, #call); \
+  } while (0)

@@ -28,6 +28,18 @@ SE_BLOCK_BYTES = 3 * 1024 * 1024      # src/classify.cc:527
 PE_BLOCK_FRAGS = 10000                # src/classify.cc:32
 
 
+def murmur3_np(keys: np.ndarray) -> np.ndarray:
+    """Vectorised MurmurHash3 finalizer (src/kv_store.h:59-67)."""
+    k = np.asarray(keys, dtype=np.uint64).copy()
+    with np.errstate(over="ignore"):
+        k ^= k >> np.uint64(33)
+        k *= np.uint64(0xff51afd7ed558ccd)
+        k ^= k >> np.uint64(33)
+        k *= np.uint64(0xc4ceb9fe1a85ec53)
+        k ^= k >> np.uint64(33)
+    return k
+
+
 def manifest():
     with open(os.path.join(GOLDEN, "manifest.json")) as f:
         return json.load(f)
