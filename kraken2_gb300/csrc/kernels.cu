@@ -266,13 +266,13 @@ __device__ __forceinline__ uint32_t insert_lca(const TableView &t, uint32_t *cel
 }
 
 __global__ void insert_kernel(TableView t, uint32_t *cells, const uint32_t *parent,
-                              const uint64_t *keys, const uint32_t *taxids, uint64_t n,
-                              unsigned long long *size, uint32_t *status) {
+                              uint64_t node_count, const uint64_t *keys, const uint32_t *taxids,
+                              uint64_t n, unsigned long long *size, uint32_t *status) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t tx = taxids[i];
     if (!tx) continue;
-    if (tx > t.value_mask) {
+    if (tx > t.value_mask || tx >= node_count) {
       atomicOr(status, STATUS_BUILD_VALUE);
       continue;
     }
@@ -496,7 +496,7 @@ extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const
   TableView t = db->table_view();
   uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count(db->device) * 32);
   insert_kernel<<<(unsigned)std::max<uint64_t>(1, blocks), 256, 0, st>>>(
-      t, db->d_cells, db->d_parent, d_keys, d_taxids, n,
+      t, db->d_cells, db->d_parent, db->node_count, d_keys, d_taxids, n,
       reinterpret_cast<unsigned long long *>(db->d_size), d_status);
   uint32_t status = 0;
   cudaError_t e = cudaGetLastError();
@@ -505,6 +505,7 @@ extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const
   cudaFree(d_status);
   if (e != cudaSuccess) return cuda_fail(e, "insert_kernel");
   if (status & STATUS_BUILD_FULL) return fail(K2G_ERR_CAPACITY, "compact hash table capacity exceeded");
-  if (status & STATUS_BUILD_VALUE) return fail(K2G_ERR_ARG, "taxid too wide for the table's value bits");
+  if (status & STATUS_BUILD_VALUE)
+    return fail(K2G_ERR_ARG, "taxid outside the taxonomy or too wide for the value bits");
   return K2G_OK;
 }
