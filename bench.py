@@ -193,3 +193,448 @@ class Workload:
         self.seq_off = torch.arange(R + 1, dtype=torch.int64, device=self.dev) * L
         self._sync()
         log(f"reads: {R} x {L} bp, {self.n_hit_reads} from sources")
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class DeviceRunner:
+    """Classifies the resident reads batch by batch through k2g_classify."""
+
+    def __init__(self, wl: Workload, mode: int):
+        torch, cfg, k2g = wl.torch, wl.cfg, wl.k2g
+        self.wl, self.mode = wl, mode
+        B, L = cfg.batch, cfg.read_len
+        dev = wl.dev
+        self.off = torch.arange(B + 1, dtype=torch.int64, device=dev) * L
+        self.call = torch.empty(B, dtype=torch.int32, device=dev)
+        self.hg = torch.empty(B, dtype=torch.int32, device=dev)
+        self.hoff = torch.empty(B, dtype=torch.int64, device=dev)
+        self.hlen = torch.empty(B, dtype=torch.int32, device=dev)
+        self.runs_cap = B * (L + 2) + 8
+        self.runs = torch.empty(self.runs_cap, dtype=torch.int64, device=dev)
+        self.tr = torch.zeros(cfg.nodes, dtype=torch.int64, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.params = k2g.ClassifyParams(cfg.confidence, cfg.min_hit_groups, 0, 0, 0)
+        self.launches = 0
+        self.call_ms = []
+
+    def batches(self):
+        cfg = self.wl.cfg
+        for b0 in range(0, cfg.n_reads, cfg.batch):
+            yield b0, min(cfg.batch, cfg.n_reads - b0)
+
+    def classify(self, b0, n, events=None):
+        wl, k2g, cfg = self.wl, self.wl.k2g, self.wl.cfg
+        reads = k2g.Reads(wl.reads.data_ptr() + b0 * cfg.read_len, None, self.off.data_ptr(), n,
+                          cfg.read_len, None, b0)
+        res = k2g.Results(self.call.data_ptr(), self.hg.data_ptr(), self.hoff.data_ptr(),
+                          self.hlen.data_ptr(), self.runs.data_ptr(), self.runs_cap,
+                          self.tr.data_ptr(), None, None, None, 0, None, self.status.data_ptr())
+        if events is not None:
+            events[0].record(wl.stream)
+        wl.db.classify(reads, self.params, res, mode=self.mode, stream=wl.stream.cuda_stream)
+        if events is not None:
+            events[1].record(wl.stream)
+        self.launches += 2   # classify kernel + slow-path kernel
+
+    def step(self, timed_calls=None):
+        for b0, n in self.batches():
+            ev = None
+            if timed_calls is not None:
+                ev = (self.wl.torch.cuda.Event(enable_timing=True),
+                      self.wl.torch.cuda.Event(enable_timing=True))
+                timed_calls.append((n, ev))
+            self.classify(b0, n, ev)
+
+
+def murmur3_np(keys: np.ndarray) -> np.ndarray:
+    """MurmurHash3 finalizer (src/kv_store.h:59-67), vectorised."""
+    k = keys.astype(np.uint64).copy()
+    with np.errstate(over="ignore"):
+        k ^= k >> np.uint64(33)
+        k *= np.uint64(0xff51afd7ed558ccd)
+        k ^= k >> np.uint64(33)
+        k *= np.uint64(0xc4ceb9fe1a85ec53)
+        k ^= k >> np.uint64(33)
+    return k
+
+
+def sample_lookup_keys(wl: Workload, n_reads: int) -> np.ndarray:
+    """The LOOKUP keys of the first n_reads reads (distinct consecutive
+    non-ambiguous minimizers), scanned on the device with k2g_scan."""
+    torch, cfg = wl.torch, wl.cfg
+    L = cfg.read_len
+    off = torch.arange(n_reads + 1, dtype=torch.int64, device=wl.dev) * L
+    mins = torch.empty(n_reads * L, dtype=torch.int64, device=wl.dev)
+    amb = torch.zeros(n_reads * L, dtype=torch.uint8, device=wl.dev)
+    wl.db.scan(wl.reads.data_ptr(), off.data_ptr(), n_reads, mins.data_ptr(), amb.data_ptr(),
+               wl.stream.cuda_stream)
+    wl.torch.cuda.synchronize(wl.dev)
+    K = L - cfg.k + 1
+    m = mins.view(n_reads, L)[:, :K].cpu().numpy().view(np.uint64)
+    a = amb.view(n_reads, L)[:, :K].cpu().numpy()
+    new = np.ones_like(m, dtype=bool)
+    new[:, 1:] = m[:, 1:] != m[:, :-1]
+    return m[new & (a == 0)]
+
+
+def probe_sectors(cells: np.ndarray, cap: int, kb: int, vb: int, keys: np.ndarray):
+    """Replays CompactHashTable::Get for keys on the host copy of the table and
+    returns (32-byte sectors touched per key, hit mask)."""
+    hc = murmur3_np(keys)
+    ck = hc >> np.uint64(64 - kb)
+    idx = hc % np.uint64(cap)
+    start = idx.copy()
+    length = np.zeros(len(keys), np.int64)
+    hit = np.zeros(len(keys), bool)
+    active = np.arange(len(keys))
+    vmask = np.uint32((1 << vb) - 1)
+    while len(active):
+        c = cells[idx[active].astype(np.int64)]
+        length[active] += 1
+        v = c & vmask
+        match = (v != 0) & ((c >> np.uint32(vb)).astype(np.uint64) == ck[active])
+        hit[active[match]] = True
+        cont = (v != 0) & ~match
+        active = active[cont]
+        nxt = idx[active] + np.uint64(1)
+        nxt[nxt == np.uint64(cap)] = 0
+        idx[active] = nxt
+    first = (start % np.uint64(8)).astype(np.int64)
+    sectors = (first + length - 1) // 8 + 1
+    return sectors, hit
+
+
+def cpu_classify(wl: Workload, cells: np.ndarray, n_reads: int, threads: int):
+    """Times the oracle restatement on the host (the CPU baseline)."""
+    import oracle
+    cfg = wl.cfg
+    L = cfg.read_len
+    bases = wl.reads[:n_reads * L].cpu().numpy().tobytes()
+    off = np.arange(n_reads + 1, dtype=np.uint64) * L
+    o = oracle.Oracle(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, wl.parent,
+                      oracle.index_opts(cfg.k, cfg.l, spaced_mask(SEED_TEMPLATE), TOGGLE))
+    t0 = time.perf_counter()
+    calls, hg, nr, runs, base = o.classify(bases, None, off, n_reads, threads=threads,
+                                           confidence=cfg.confidence,
+                                           min_hit_groups=cfg.min_hit_groups)
+    dt = time.perf_counter() - t0
+    return dt, calls, hg, nr, runs, base
+
+
+def e2e_run(wl: Workload, n_reads: int, steps: int):
+    """k2g_classify_host over pinned host buffers, copies inside the timing."""
+    torch, cfg, k2g = wl.torch, wl.cfg, wl.k2g
+    L = cfg.read_len
+    bases = torch.empty(n_reads * L + 16, dtype=torch.uint8, pin_memory=True)
+    bases.copy_(wl.reads[:n_reads * L + 16])
+    off = (torch.arange(n_reads + 1, dtype=torch.int64) * L).pin_memory()
+    call = torch.empty(n_reads, dtype=torch.int32, pin_memory=True)
+    hg = torch.empty(n_reads, dtype=torch.int32, pin_memory=True)
+    hlen = torch.empty(n_reads, dtype=torch.int32, pin_memory=True)
+    runs_cap = n_reads * 16
+    runs = torch.empty(runs_cap, dtype=torch.int64, pin_memory=True)
+    params = k2g.ClassifyParams(cfg.confidence, cfg.min_hit_groups, 0, 0, 0)
+    times, used = [], 0
+    for _ in range(steps + 1):
+        nr = C.c_uint64(runs_cap)
+        t0 = time.perf_counter()
+        k2g.check(k2g.lib().k2g_classify_host(wl.db.h, bases.data_ptr(), None, off.data_ptr(),
+                                              n_reads, C.byref(params), call.data_ptr(),
+                                              hg.data_ptr(), hlen.data_ptr(), runs.data_ptr(),
+                                              C.byref(nr), None))
+        times.append(time.perf_counter() - t0)
+        used = nr.value
+    t = float(np.median(times[1:]))
+    h2d = n_reads * L + (n_reads + 1) * 8
+    d2h = n_reads * 12 + used * 8
+    return t, h2d, d2h, call.numpy().view(np.uint32).copy()
+
+
+def dist_setup(n_gpus: int):
+    """One process per GPU under torchrun; replicas, no data-path collective."""
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    return rank, world, local, pg
+
+
+def max_over_ranks(pg, value: float) -> float:
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    import torch
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize()
+
+
+def run_ours(args, log):
+    import torch
+    rank, world, local, pg = dist_setup(args.gpus)
+    cfg = Config(args.scale)
+    wl = Workload(cfg, local, log=log if rank == 0 else (lambda *_: None))
+    mode = wl.k2g.MODE_PLAIN if args.mode == "plain" else wl.k2g.MODE_PERSISTENT
+    runner = DeviceRunner(wl, mode)
+    for _ in range(args.warmup):
+        runner.step()
+    barrier(pg)
+    calls = []
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    runner.launches = 0
+    with Clocks(local) as clk:
+        start.record(wl.stream)
+        for s in range(args.steps):
+            runner.step(calls if s == args.steps - 1 else None)
+        end.record(wl.stream)
+        torch.cuda.synchronize()
+    launches = runner.launches
+    ms_total = max_over_ranks(pg, start.elapsed_time(end))
+    ms_step = ms_total / args.steps
+    if int(runner.status.cpu()[0]):
+        raise RuntimeError("classification reported a buffer overflow")
+    reads_total = cfg.n_reads * world
+    reads_s = reads_total / (ms_step / 1e3)
+    call_ms = [(n, a.elapsed_time(b)) for n, (a, b) in calls]
+    if rank != 0:
+        barrier(pg)
+        return None
+
+    # plain one-batch-per-launch form, timed once for the ratio
+    plain = None
+    if args.mode != "plain" and not args.skip_plain:
+        pr = DeviceRunner(wl, wl.k2g.MODE_PLAIN)
+        pr.step()
+        ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ps.record(wl.stream)
+        pr.step()
+        pe.record(wl.stream)
+        torch.cuda.synchronize()
+        plain = cfg.n_reads / (ps.elapsed_time(pe) / 1e3)
+
+    # host copy of the table: algorithmic bytes, parity sample, CPU baseline
+    t0 = time.time()
+    cells, _ = wl.db.download()
+    log(f"table download {time.time() - t0:.1f}s")
+    n_sample = min(cfg.n_reads, 50_000)
+    keys = sample_lookup_keys(wl, n_sample)
+    sectors, hit = probe_sectors(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, keys)
+    lookups_per_read = len(keys) / n_sample
+    sectors_per_read = float(sectors.sum()) / n_sample
+    runs_per_read = float(runner.hlen[:cfg.batch].float().mean().item()) if cfg.batch else 0.0
+    in_bytes = cfg.read_len + 8
+    out_bytes = 4 + 4 + 8 + 4 + 8 * runs_per_read
+    bytes_per_read = 32 * sectors_per_read + in_bytes + out_bytes
+
+    # roofline of the dominant kernel (the classify launch of each batch)
+    peak, peak_kind = hbm_peak()
+    kern_reads = sum(n for n, _ in call_ms)
+    kern_ms = sum(ms for _, ms in call_ms)
+    achieved = bytes_per_read * kern_reads / (kern_ms / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "classify_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tj = json.load(f)
+        traffic = tj.get("bytes_per_read", 0) * (kern_reads / max(len(call_ms), 1)) or None
+
+    # CPU baseline: the oracle restatement with every host thread
+    threads = os.cpu_count() or 1
+    cpu_n = min(cfg.n_reads, 200_000)
+    dt, ocalls, ohg, onr, oruns, obase = cpu_classify(wl, cells, cpu_n, threads)
+    rate = cpu_n / dt
+    target = args.cpu_seconds
+    if dt < target / 4:
+        cpu_n = int(min(cfg.n_reads, cpu_n * target / max(dt, 1e-3), 8_000_000))
+        dt, ocalls, ohg, onr, oruns, obase = cpu_classify(wl, cells, cpu_n, threads)
+        rate = cpu_n / dt
+    # parity of the GPU calls on the same reads (bit-exact)
+    pr = DeviceRunner(wl, mode)
+    gpu_calls = []
+    for b0 in range(0, cpu_n, cfg.batch):
+        n = min(cfg.batch, cpu_n - b0)
+        pr.classify(b0, n)
+        torch.cuda.synchronize()
+        gpu_calls.append(pr.call[:n].cpu().numpy().view(np.uint32).copy())
+    gpu_calls = np.concatenate(gpu_calls)
+    mismatches = int((gpu_calls.astype(np.uint64) != ocalls).sum())
+    del cells
+
+    e2e_t, h2d, d2h, e2e_calls = e2e_run(wl, cfg.e2e_reads, max(2, min(args.steps, 5)))
+    e2e_rate = cfg.e2e_reads / e2e_t
+
+    out = {
+        "metric": "Mreads/min at 40GB table, bit-exact",
+        "value": round(reads_s * 60 / 1e6, 3),
+        "unit": "Mreads/min",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic (seeded, generated on the device)",
+        "config": {"workload": cfg.workload(), "mode": args.mode, "batch_reads": cfg.batch,
+                   "confidence": cfg.confidence, "min_hit_groups": cfg.min_hit_groups,
+                   "k": cfg.k, "l": cfg.l, "table_gb": round(cfg.capacity * 4 / 1e9, 1),
+                   "load": round(wl.size / cfg.capacity, 4),
+                   "l2": "inputs (table + reads) far larger than L2; no flush needed",
+                   "parallelism": f"replicas x{world}"},
+        "reads_per_s": round(reads_s),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "bytes_per_read": round(bytes_per_read, 1),
+                     "sectors_per_read": round(sectors_per_read, 3),
+                     "lookups_per_read": round(lookups_per_read, 3),
+                     "hit_fraction_of_lookups": round(float(hit.mean()), 4),
+                     "kernel_ms_per_launch": round(kern_ms / max(len(call_ms), 1), 3),
+                     "reads_per_launch": int(kern_reads / max(len(call_ms), 1))},
+        "cpu_baseline": {"value": round(rate * 60 / 1e6, 3), "unit": "Mreads/min",
+                         "cores": threads, "kind": "port",
+                         "sample": f"first {cpu_n} reads of the workload, same table (host copy)"},
+        "parity": {"reads": cpu_n, "call_mismatches_vs_oracle": mismatches},
+        "e2e": {"value": round(e2e_rate * 60 / 1e6, 3), "unit": "Mreads/min",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "reads_per_step": cfg.e2e_reads, "s_per_step": round(e2e_t, 4)},
+        "plain_vs_batched": ({"plain_mreads_min": round(plain * 60 / 1e6, 3),
+                              "batched_over_plain": round(reads_s / plain, 3)} if plain else None),
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    barrier(pg)
+    return out
+
+
+def run_reference(args, log):
+    """CPU arm: the oracle port on the host cores, same workload and metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    cfg = Config(args.scale)
+    wl = Workload(cfg, 0, log=log)
+    cells, _ = wl.db.download()
+    threads = os.cpu_count() or 1
+    n = min(cfg.n_reads, 200_000)
+    dt, *_ = cpu_classify(wl, cells, n, threads)
+    n = int(min(cfg.n_reads, n * args.cpu_seconds / 4 / max(dt, 1e-3), 4_000_000))
+    for _ in range(args.warmup):
+        cpu_classify(wl, cells, min(n, 100_000), threads)
+    times = []
+    for _ in range(args.steps):
+        dt, *_ = cpu_classify(wl, cells, n, threads)
+        times.append(dt)
+    t = float(np.mean(times))
+    v = round(n / t * 60 / 1e6, 3)
+    return {"impl": "reference", "metric": "Mreads/min at 40GB table, bit-exact", "value": v,
+            "unit": "Mreads/min", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded, generated on the device)",
+            "config": {"workload": cfg.workload(), "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "Mreads/min", "cores": threads, "kind": "port",
+                             "sample": f"{n} reads of the workload per step"},
+            "e2e": {"value": v, "unit": "Mreads/min", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the full-size workload (tests and probes only)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--skip-plain", action="store_true")
+    args = ap.parse_args()
+    log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
+    out = run_reference(args, log) if args.impl == "reference" else run_ours(args, log)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -237,7 +237,8 @@ static inline int scanner_ambig(const ko_scanner *s) {
 #define QBACK(s) (((s)->qh + (s)->qn - 1) % KO_QCAP)
 
 /* NextMinimizer -- mmscanner.cc:114-189; the monotone deque is a ring buffer.
- * Returns 1 with *mn/*amb set, or 0 when the interval is exhausted. */
+ * Returns 1 with the minimizer and ambiguity set, or 0 when the interval is
+ * exhausted. */
 static int scanner_next(ko_scanner *s, uint64_t *mn, int *amb) {
   if (s->pos >= s->finish) return 0;
   int changed = 0;
@@ -322,14 +323,6 @@ enum { TOK_LOOKUP, TOK_SKIP, TOK_REPEAT, TOK_AMBIG, TOK_BORDER_MATE };
 
 /* Small open-addressing taxon->count map standing in for taxon_counts_t. */
 typedef struct { uint64_t *key; uint64_t *val; size_t cap, n; } cmap;
-static void cmap_init(cmap *m, size_t want) {
-  size_t cap = 16;
-  while (cap < 2 * want + 2) cap <<= 1;
-  m->cap = cap; m->n = 0;
-  m->key = (uint64_t *)calloc(cap, sizeof(uint64_t));
-  m->val = (uint64_t *)calloc(cap, sizeof(uint64_t));
-}
-static void cmap_free(cmap *m) { free(m->key); free(m->val); }
 /* keys are never 0 in use; slot key 0 marks empty */
 static uint64_t *cmap_slot(cmap *m, uint64_t key) {
   size_t i = (size_t)(ko_murmur3(key) & (m->cap - 1));
@@ -374,33 +367,55 @@ static uint64_t resolve_tree(const cmap *hits, const uint64_t *parent,
   return max_taxon;
 }
 
-/* MaskLowQualityBases -- classify.cc:1061-1071 (FASTQ only). */
-static const char *mask_quality(const char *seq, const char *qual, size_t len,
-                                int minq, char **owned) {
-  *owned = NULL;
-  if (minq <= 0 || !qual) return seq;
-  char *m = (char *)malloc(len + 1);
-  for (size_t i = 0; i < len; i++)
-    m[i] = ((qual[i] - '!') < minq) ? 'x' : seq[i];
-  *owned = m;
-  return m;
+/* MaskLowQualityBases -- classify.cc:1061-1071 (FASTQ only): mask_into below. */
+
+/* Per-thread scratch reused across fragments, as the reference reuses its
+ * thread-local vectors (classify.cc:792-795, :841). */
+typedef struct {
+  size_t cap;
+  uint8_t *kind; uint32_t *kidx; uint64_t *keys; uint32_t *vals; uint64_t *taxa;
+  char *m1, *m2;
+  uint64_t *mkey, *mval; size_t mcap;
+  ko_scanner *sc;
+} ko_ws;
+
+static void ws_init(ko_ws *w) { memset(w, 0, sizeof(*w)); w->sc = (ko_scanner *)malloc(sizeof(ko_scanner)); }
+static void ws_free(ko_ws *w) {
+  free(w->kind); free(w->kidx); free(w->keys); free(w->vals); free(w->taxa);
+  free(w->m1); free(w->m2); free(w->mkey); free(w->mval); free(w->sc);
+}
+static void ws_reserve(ko_ws *w, size_t n) {
+  if (n <= w->cap) return;
+  w->cap = n;
+  w->kind = (uint8_t *)realloc(w->kind, n);
+  w->kidx = (uint32_t *)realloc(w->kidx, n * sizeof(uint32_t));
+  w->keys = (uint64_t *)realloc(w->keys, n * sizeof(uint64_t));
+  w->vals = (uint32_t *)realloc(w->vals, n * sizeof(uint32_t));
+  w->taxa = (uint64_t *)realloc(w->taxa, n * sizeof(uint64_t));
+  w->m1 = (char *)realloc(w->m1, n);
+  w->m2 = (char *)realloc(w->m2, n);
 }
 
-void ko_classify_fragment(const ko_ctx *c, const char *seq1, size_t len1,
-                          const char *qual1, const char *seq2, size_t len2,
-                          const char *qual2, ko_frag_result *res,
-                          ko_run *runs, ko_hit *hits) {
-  char *own1, *own2 = NULL;
-  const char *s1 = mask_quality(seq1, qual1, len1, c->min_quality, &own1);
-  const char *s2 = c->paired ? mask_quality(seq2, qual2, len2, c->min_quality, &own2) : NULL;
+static const char *mask_into(const char *seq, const char *qual, size_t len, int minq, char *buf) {
+  if (minq <= 0 || !qual) return seq;
+  for (size_t i = 0; i < len; i++) buf[i] = ((qual[i] - '!') < minq) ? 'x' : seq[i];
+  return buf;
+}
+
+static void classify_ws(const ko_ctx *c, const char *seq1, size_t len1, const char *qual1,
+                        const char *seq2, size_t len2, const char *qual2, ko_frag_result *res,
+                        ko_run *runs, ko_hit *hits, ko_ws *w) {
   size_t maxtok = len1 + len2 + 2;
-  uint8_t *kind = (uint8_t *)malloc(maxtok);
-  uint32_t *kidx = (uint32_t *)malloc(maxtok * sizeof(uint32_t));
-  uint64_t *keys = (uint64_t *)malloc(maxtok * sizeof(uint64_t));
-  uint32_t *vals = (uint32_t *)malloc(maxtok * sizeof(uint32_t));
-  uint64_t *taxa = (uint64_t *)malloc(maxtok * sizeof(uint64_t));
+  ws_reserve(w, maxtok);
+  const char *s1 = mask_into(seq1, qual1, len1, c->min_quality, w->m1);
+  const char *s2 = c->paired ? mask_into(seq2, qual2, len2, c->min_quality, w->m2) : NULL;
+  uint8_t *kind = w->kind;
+  uint32_t *kidx = w->kidx;
+  uint64_t *keys = w->keys;
+  uint32_t *vals = w->vals;
+  uint64_t *taxa = w->taxa;
   size_t ntok = 0, nkeys = 0, ntaxa = 0, nhits = 0;
-  ko_scanner *sc = (ko_scanner *)malloc(sizeof(ko_scanner));
+  ko_scanner *sc = w->sc;
   scanner_init(sc, &c->idx);
 
   /* Phase 1: token stream (classify.cc:797-838). */
@@ -435,7 +450,17 @@ void ko_classify_fragment(const ko_ctx *c, const char *seq1, size_t len1,
 
   /* Phase 3: replay (classify.cc:847-888). */
   cmap hit_counts;
-  cmap_init(&hit_counts, nkeys + 1);
+  {
+    size_t cap = 16;
+    while (cap < 2 * (nkeys + 1) + 2) cap <<= 1;
+    if (cap > w->mcap) {
+      w->mcap = cap;
+      w->mkey = (uint64_t *)realloc(w->mkey, cap * sizeof(uint64_t));
+      w->mval = (uint64_t *)realloc(w->mval, cap * sizeof(uint64_t));
+    }
+    memset(w->mkey, 0, cap * sizeof(uint64_t));
+    hit_counts.key = w->mkey; hit_counts.val = w->mval; hit_counts.cap = cap; hit_counts.n = 0;
+  }
   int64_t hit_groups = 0;
   uint64_t last_taxon = 0;
   for (size_t ti = 0; ti < ntok; ti++) {
@@ -478,9 +503,16 @@ finished:;
   res->n_runs = nr;
   res->n_hits = nhits;
   res->total_kmers = total_kmers;
-  cmap_free(&hit_counts);
-  free(sc); free(kind); free(kidx); free(keys); free(vals); free(taxa);
-  free(own1); free(own2);
+}
+
+void ko_classify_fragment(const ko_ctx *c, const char *seq1, size_t len1,
+                          const char *qual1, const char *seq2, size_t len2,
+                          const char *qual2, ko_frag_result *res,
+                          ko_run *runs, ko_hit *hits) {
+  ko_ws w;
+  ws_init(&w);
+  classify_ws(c, seq1, len1, qual1, seq2, len2, qual2, res, runs, hits, &w);
+  ws_free(&w);
 }
 
 typedef struct {
@@ -492,19 +524,22 @@ typedef struct {
 static void *cm_thread(void *p) {
   cm_job *j = (cm_job *)p;
   int per = j->c->paired ? 2 : 1;
+  ko_ws w;
+  ws_init(&w);
   for (uint64_t f = j->lo; f < j->hi; f++) {
     uint64_t a = j->seq_off[f * per], b = j->seq_off[f * per + 1];
     uint64_t a2 = 0, b2 = 0;
     if (per == 2) { a2 = j->seq_off[f * per + 1]; b2 = j->seq_off[f * per + 2]; }
     ko_frag_result r;
-    ko_classify_fragment(j->c, j->bases + a, b - a, j->quals ? j->quals + a : NULL,
-                         per == 2 ? j->bases + a2 : NULL, b2 - a2,
-                         (per == 2 && j->quals) ? j->quals + a2 : NULL, &r,
-                         j->runs + j->seq_off[f * per] + 2 * f, NULL);
+    classify_ws(j->c, j->bases + a, b - a, j->quals ? j->quals + a : NULL,
+                per == 2 ? j->bases + a2 : NULL, b2 - a2,
+                (per == 2 && j->quals) ? j->quals + a2 : NULL, &r,
+                j->runs + j->seq_off[f * per] + 2 * f, NULL, &w);
     j->calls[f] = r.call;
     if (j->hit_groups) j->hit_groups[f] = r.hit_groups;
     j->n_runs[f] = (uint32_t)r.n_runs;
   }
+  ws_free(&w);
   return NULL;
 }
 
