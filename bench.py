@@ -455,6 +455,13 @@ def run_ours(args, log):
     wl = Workload(cfg, local, log=log if rank == 0 else (lambda *_: None))
     mode = wl.k2g.MODE_PLAIN if args.mode == "plain" else wl.k2g.MODE_PERSISTENT
     runner = DeviceRunner(wl, mode)
+    if args.profile:
+        # for ncu: setup, then exactly two classification steps
+        runner.step()
+        runner.step()
+        torch.cuda.synchronize()
+        log("profile steps done")
+        return None
     for _ in range(args.warmup):
         runner.step()
     barrier(pg)
@@ -637,6 +644,8 @@ def main():
                     help="fraction of the full-size workload (tests and probes only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="setup plus two classification steps only (for ncu captures)")
     args = ap.parse_args()
     log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
     out = run_reference(args, log) if args.impl == "reference" else run_ours(args, log)
