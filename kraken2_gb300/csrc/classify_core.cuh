@@ -132,18 +132,27 @@ struct GlobalStore {
 };
 
 // Per-lane fragment state carried across segments (registers).
+//
+// Bases are read as 16-byte aligned chunks of the concatenated sequence
+// buffer.  Chunk 0 of a mate starts at the aligned address at or before the
+// first base; its `head` leading bytes belong to the previous sequence and
+// are treated as ambiguous, which leaves the scanner in exactly the state of
+// a fresh LoadSequence (src/mmscanner.cc:98-112) when base 0 arrives.  Bytes
+// after the mate's end are scanned but emit no token.  Two chunks are held
+// ahead so the global loads overlap the arithmetic of the current chunk.
 template <int W>
 struct Lane {
   uint64_t frag;          // fragment index within the batch, ~0 = none
-  // scan position
-  const uint8_t *seq;
-  const uint8_t *qual;
-  uint32_t len, pos;
+  const uint8_t *ap;      // aligned chunk stream of the current mate
+  const uint8_t *aq;      // same for qualities (or null)
+  uint32_t head;          // bytes of chunk 0 before base 0
+  uint32_t nchunks, ci;   // chunks of this mate, next chunk to scan
+  uint32_t len;           // bases of the current mate
   uint32_t len2;          // second mate length (paired)
   const uint8_t *seq2;
   const uint8_t *qual2;
   uint32_t mate;
-  uint32_t word, qword;   // cached 4 bytes of bases / qualities
+  uint4 c0, c1, q0, q1;   // chunks ci and ci+1
   uint64_t fwd, rc;
   int32_t run, last_amb;
   Window<W> win;
@@ -161,9 +170,28 @@ struct Lane {
   uint64_t run_base;
 };
 
+__device__ __forceinline__ uint4 load_chunk(const uint8_t *ap, uint32_t i, uint32_t n) {
+  if (i < n) return __ldg(reinterpret_cast<const uint4 *>(ap) + i);
+  return make_uint4(0, 0, 0, 0);
+}
+
+// Points the chunk stream at a mate and resets the per-mate scanner state.
 template <int W>
-__device__ __forceinline__ void lane_reset_mate(Lane<W> &s) {
-  s.pos = 0;
+__device__ __forceinline__ void lane_start_mate(Lane<W> &s, const uint8_t *seq, const uint8_t *qual,
+                                                uint32_t len) {
+  const uint32_t head = (uint32_t)((uintptr_t)seq & 15u);
+  s.head = head;
+  s.ap = seq - head;
+  s.aq = qual ? qual - head : nullptr;
+  s.len = len;
+  s.nchunks = (head + len + 15) / 16;
+  s.ci = 0;
+  s.c0 = load_chunk(s.ap, 0, s.nchunks);
+  s.c1 = load_chunk(s.ap, 1, s.nchunks);
+  if (qual) {
+    s.q0 = load_chunk(s.aq, 0, s.nchunks);
+    s.q1 = load_chunk(s.aq, 1, s.nchunks);
+  }
   s.fwd = s.rc = 0;
   s.run = 0;
   s.last_amb = -1;
@@ -176,9 +204,6 @@ __device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, ui
   s.frag = f;
   const int per = a.cls.paired ? 2 : 1;
   uint64_t o0 = a.seq_off[f * per], o1 = a.seq_off[f * per + 1];
-  s.seq = a.bases + o0;
-  s.qual = a.quals ? a.quals + o0 : nullptr;
-  s.len = (uint32_t)(o1 - o0);
   if (per == 2) {
     uint64_t o2 = a.seq_off[f * per + 2];
     s.seq2 = a.bases + o1;
@@ -190,7 +215,7 @@ __device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, ui
     s.len2 = 0;
   }
   s.mate = 0;
-  lane_reset_mate(s);
+  lane_start_mate(s, a.bases + o0, a.quals ? a.quals + o0 : nullptr, (uint32_t)(o1 - o0));
   s.gkind = G_NONE;
   s.glen = 0;
   s.scan_done = false;
@@ -206,103 +231,135 @@ __device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, ui
   s.run_base = o0 + 2 * f;
 }
 
-// Byte p of a sequence through a 4-byte cache of aligned words.  Aligned
-// 4-byte loads never leave the allocation that holds byte p.
-__device__ __forceinline__ uint32_t fetch_byte(const uint8_t *base, uint32_t p, uint32_t &cache) {
-  uintptr_t addr = (uintptr_t)(base + p);
-  uint32_t sh = (uint32_t)(addr & 3u);
-  if (p == 0 || sh == 0) cache = __ldg(reinterpret_cast<const uint32_t *>(addr & ~(uintptr_t)3));
-  return (cache >> (8 * sh)) & 0xFFu;
-}
-
 // ---- scan phase ----------------------------------------------------------
-// Scans until the fragment ends or the segment buffers are (nearly) full.
 // The closed form used here is equivalent to MinimizerScanner::NextMinimizer
 // (src/mmscanner.cc:114-189): the k-mer ending at base p is ambiguous iff an
 // ambiguous base lies in [p-k+2, p] (k > l) or [p-k+1, p] (k == l), and its
 // minimizer is the minimum over the l-mers ending in [p-w+1, p] whose bases
 // are all unambiguous, of (canonical(l-mer) & mask) ^ toggle, xor toggle.
-template <int W, class Store>
+// The token kinds follow ClassifySequence (src/classify.cc:812-831).
+
+constexpr int kSegChunks = 6;   // 96 bases per segment
+
+struct ScanConst {
+  int32_t k, l, amb_span, w;
+  uint32_t top_shift;
+  uint64_t lmer_mask, smask, toggle, min_hash;
+  uint32_t qthr4;     // 4 copies of the lowest unmasked quality (signed bytes)
+  bool qall;          // every quality is masked (threshold above 127)
+};
+
+__device__ __forceinline__ ScanConst scan_const(const ClassifyArgs &a) {
+  const ScanView &sv = a.scan;
+  ScanConst c;
+  c.k = sv.k;
+  c.l = sv.l;
+  c.amb_span = (sv.k == sv.l) ? sv.k - 1 : sv.k - 2;
+  c.w = sv.w;
+  c.top_shift = 2u * (uint32_t)(sv.l - 1);
+  c.lmer_mask = sv.lmer_mask;
+  c.smask = sv.spaced_mask ? sv.spaced_mask : ~0ull;
+  c.toggle = sv.toggle;
+  c.min_hash = sv.min_hash;
+  // (signed char)q - '!' < min_quality  <=>  (signed char)q < '!' + min_quality
+  int thr = 33 + a.cls.min_quality;
+  c.qall = thr > 127;
+  uint32_t t = (uint32_t)(thr > 127 ? 127 : thr) & 0xFFu;
+  c.qthr4 = t * 0x01010101u;
+  return c;
+}
+
+// One base of the scan; branch-free so that the lanes of a warp stay in step.
+template <int W, bool RC1, class Store>
+__device__ __forceinline__ void scan_base(Lane<W> &s, Store &st, const ScanConst &c, int32_t p,
+                                          uint32_t valid, uint32_t code, int &ng, int &nk) {
+  s.fwd = ((s.fwd << 2) | code) & c.lmer_mask;
+  s.rc = (s.rc >> 2) | ((uint64_t)(code ^ 3u) << c.top_shift);
+  s.run = valid ? s.run + 1 : 0;
+  s.last_amb = valid ? s.last_amb : p;
+  const uint64_t rcv = RC1 ? s.rc : revcomp_v0(s.fwd, c.lmer_mask);
+  uint64_t cand = ((s.fwd < rcv ? s.fwd : rcv) & c.smask) ^ c.toggle;
+  cand = (s.run >= c.l) ? cand : ~0ull;
+  s.win.push(cand);
+  const bool emit = (p >= c.k - 1) && (p < (int32_t)s.len);
+  const bool amb = (p - s.last_amb) <= c.amb_span;
+  const uint64_t m = s.win.min(c.w) ^ c.toggle;
+  const bool nonamb = emit && !amb;
+  const bool is_new = nonamb && (m != s.last_min);
+  s.last_min = nonamb ? m : s.last_min;
+  bool skip = false;
+  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  const bool is_key = is_new && !skip;
+  const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
+  const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
+                                       : (tkind == G_CONT && s.gkind != G_AMBIG && s.gkind != G_NONE);
+  const bool newg = emit && !cont;
+  const bool close = newg && (s.gkind != G_NONE);
+  if (close) st.group(ng) = make_group(s.gkind, s.glen);
+  ng += close ? 1 : 0;
+  s.glen = emit ? (newg ? 1u : s.glen + 1u) : s.glen;
+  s.gkind = newg ? tkind : s.gkind;
+  if (is_key) st.key(nk) = m;
+  nk += is_key ? 1 : 0;
+}
+
+// Scans up to kSegChunks chunks, stopping early at the fragment end or when
+// the segment buffers could not take another chunk.
+template <int W, bool QUAL, bool RC1, class Store>
 __device__ __forceinline__ void scan_segment(Lane<W> &s, Store &st, const ClassifyArgs &a,
                                              int &ng, int &nk) {
-  const ScanView &sv = a.scan;
-  const int k = sv.k, l = sv.l;
-  const int amb_span = (k == l) ? k - 1 : k - 2;   // p - last_amb <= amb_span -> ambiguous
-  const uint64_t top_shift = 2ull * (l - 1);
-  const bool use_quals = a.cls.min_quality > 0;
+  const ScanConst c = scan_const(a);
   ng = 0;
   nk = 0;
+  int done = 0;
   while (true) {
-    if (ng >= Store::kGroups - 2 || nk >= Store::kKeys) break;
-    if (s.pos >= s.len) {
+    if (s.ci >= s.nchunks) {
       if (s.gkind != G_NONE) { st.group(ng++) = make_group(s.gkind, s.glen); s.gkind = G_NONE; }
       if (a.cls.paired && s.mate == 0) {
         st.group(ng++) = make_group(G_BORDER, 1);
         s.mate = 1;
-        s.seq = s.seq2;
-        s.qual = s.qual2;
-        s.len = s.len2;
-        lane_reset_mate(s);
+        lane_start_mate(s, s.seq2, QUAL ? s.qual2 : nullptr, s.len2);
         continue;
       }
       s.scan_done = true;
       break;
     }
-    const uint32_t p = s.pos;
-    uint32_t c = fetch_byte(s.seq, p, s.word);
-    uint32_t code = dna_code(c);
-    if (use_quals && s.qual) {
-      int q = (int)(signed char)fetch_byte(s.qual, p, s.qword);
-      if (q - '!' < a.cls.min_quality) code = 0xFFu;     // masked to 'x'
+    if (done == kSegChunks || ng > Store::kGroups - 19 || nk > Store::kKeys - 16) break;
+    const uint4 cur = s.c0;
+    s.c0 = s.c1;
+    s.c1 = load_chunk(s.ap, s.ci + 2, s.nchunks);
+    uint4 qc = make_uint4(0, 0, 0, 0);
+    if (QUAL) {
+      qc = s.q0;
+      s.q0 = s.q1;
+      s.q1 = load_chunk(s.aq, s.ci + 2, s.nchunks);
     }
-    uint64_t cand = ~0ull;
-    if (code != 0xFFu) {
-      s.fwd = ((s.fwd << 2) | code) & sv.lmer_mask;
-      s.rc = (s.rc >> 2) | ((uint64_t)(code ^ 3u) << top_shift);
-      s.run++;
-      if (s.run >= l) {
-        uint64_t rcv = sv.revcom_version ? s.rc : revcomp_v0(s.fwd, sv.lmer_mask);
-        uint64_t canon = s.fwd < rcv ? s.fwd : rcv;
-        if (sv.spaced_mask) canon &= sv.spaced_mask;
-        cand = canon ^ sv.toggle;
+    const int32_t pbase = (int32_t)(16 * s.ci) - (int32_t)s.head;
+    const uint32_t words[4] = {cur.x, cur.y, cur.z, cur.w};
+    const uint32_t qwords[4] = {qc.x, qc.y, qc.z, qc.w};
+#pragma unroll
+    for (int wi = 0; wi < 4; wi++) {
+      const uint32_t wd = words[wi];
+      const uint32_t lower = wd | 0x20202020u;
+      uint32_t ok = __vcmpeq4(lower, 0x61616161u) | __vcmpeq4(lower, 0x63636363u) |
+                    __vcmpeq4(lower, 0x67676767u) | __vcmpeq4(lower, 0x74747474u);
+      if (QUAL) {
+        ok &= ~__vcmplts4(qwords[wi], c.qthr4);
+        if (c.qall) ok = 0;
       }
-    } else {
-      s.run = 0;
-      s.last_amb = (int32_t)p;
-    }
-    s.win.push(cand);
-    s.pos = p + 1;
-    if ((int)p < k - 1) continue;
-    // one token for the k-mer ending at p
-    if ((int32_t)p - s.last_amb <= amb_span) {
-      if (s.gkind == G_AMBIG && s.glen < kGroupMaxLen) {
-        s.glen++;
-      } else {
-        if (s.gkind != G_NONE) st.group(ng++) = make_group(s.gkind, s.glen);
-        s.gkind = G_AMBIG;
-        s.glen = 1;
+      // bytes before base 0 of the mate read as ambiguous
+      const int32_t before = -(pbase + 4 * wi);
+      if (before > 0) ok = before >= 4 ? 0u : (ok & (0xFFFFFFFFu << (8 * before)));
+      const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        const uint32_t valid = (ok >> (8 * b)) & 1u;
+        const uint32_t code = (codes >> (8 * b)) & 3u;
+        scan_base<W, RC1>(s, st, c, pbase + 4 * wi + b, valid, code, ng, nk);
       }
-      continue;
     }
-    uint64_t m = s.win.min(sv.w) ^ sv.toggle;
-    if (m != s.last_min) {
-      s.last_min = m;
-      if (s.gkind != G_NONE) st.group(ng++) = make_group(s.gkind, s.glen);
-      s.glen = 1;
-      if (sv.min_hash && murmur3(m) < sv.min_hash) {
-        s.gkind = G_SKIP;
-      } else {
-        s.gkind = G_KEY;
-        st.key(nk++) = m;
-      }
-    } else if ((s.gkind == G_KEY || s.gkind == G_SKIP || s.gkind == G_CONT) &&
-               s.glen < kGroupMaxLen) {
-      s.glen++;
-    } else {
-      if (s.gkind != G_NONE) st.group(ng++) = make_group(s.gkind, s.glen);
-      s.gkind = G_CONT;
-      s.glen = 1;
-    }
+    s.ci++;
+    done++;
   }
   // close the open group at a segment boundary; a following REPEAT opens CONT
   if (s.gkind != G_NONE) {

@@ -6,8 +6,26 @@
 #include <mutex>
 #include <vector>
 
-#include "classify_core.cuh"
+#include "classify_kernels.cuh"
 #include "k2g_internal.h"
+
+namespace k2g {
+// compiled in classify_w5.cu / classify_misc.cu
+extern template cudaError_t launch_fast<5, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<5, true, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<1, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<1, true, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<7, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<7, true, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<0, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<0, true, true>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<0, false, false>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_fast<0, true, false>(const ClassifyArgs &, int, int, cudaStream_t);
+extern template cudaError_t launch_slow<false, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
+extern template cudaError_t launch_slow<true, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
+extern template cudaError_t launch_slow<false, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
+extern template cudaError_t launch_slow<true, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
+}  // namespace k2g
 
 namespace k2g {
 
@@ -68,6 +86,15 @@ __global__ void lookup_kernel(TableView t, const uint64_t *keys, uint32_t *vals,
 // Scan: per-k-mer minimizers (MinimizerScanner)
 // ---------------------------------------------------------------------------
 
+// Byte p of a sequence through a 4-byte cache of aligned words.  Aligned
+// 4-byte loads never leave the allocation that holds byte p.
+__device__ __forceinline__ uint32_t fetch_byte(const uint8_t *base, uint32_t p, uint32_t &cache) {
+  uintptr_t addr = (uintptr_t)(base + p);
+  uint32_t sh = (uint32_t)(addr & 3u);
+  if (p == 0 || sh == 0) cache = __ldg(reinterpret_cast<const uint32_t *>(addr & ~(uintptr_t)3));
+  return (cache >> (8 * sh)) & 0xFFu;
+}
+
 template <int W>
 __global__ void scan_kernel(ScanView sv, const uint8_t *bases, const uint64_t *seq_off,
                             uint64_t n_seqs, uint64_t *mins, uint8_t *ambig) {
@@ -107,124 +134,6 @@ __global__ void scan_kernel(ScanView sv, const uint8_t *bases, const uint64_t *s
     bool amb = (int32_t)p - last_amb <= amb_span;
     ambig[j] = amb ? 1 : 0;
     mins[j] = amb ? ~0ull : (win.min(sv.w) ^ sv.toggle);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Classification kernels
-// ---------------------------------------------------------------------------
-
-constexpr int kKCap = 32;     // keys per lane per segment
-constexpr int kGCap = 48;     // groups per lane per segment
-constexpr int kMCap = 16;     // taxon map slots per lane
-constexpr int kWarpsPerBlock = 2;
-using FastStore = SmemStore<kKCap, kGCap, kMCap>;
-
-template <int W>
-__device__ __forceinline__ bool lane_fetch(Lane<W> &s, const ClassifyArgs &a, bool persistent,
-                                           bool &exhausted, uint64_t first) {
-  // Returns true when the lane holds a fragment afterwards.
-  const unsigned lane = threadIdx.x & 31;
-  if (!persistent) {
-    if (s.frag == ~0ull && !exhausted) {
-      exhausted = true;
-      if (first < a.n_frags) {
-        lane_begin(s, a, first);
-        return true;
-      }
-    }
-    return s.frag != ~0ull;
-  }
-  bool need = (s.frag == ~0ull) && !exhausted;
-  unsigned m = __ballot_sync(0xffffffffu, need);
-  if (m) {
-    int leader = __ffs(m) - 1;
-    unsigned long long base = 0;
-    if ((int)lane == leader) base = atomicAdd(a.next_frag, (unsigned long long)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (need) {
-      uint64_t f = base + __popc(m & ((1u << lane) - 1));
-      if (f < a.n_frags) lane_begin(s, a, f);
-      else exhausted = true;
-    }
-  }
-  return s.frag != ~0ull;
-}
-
-template <int W, bool PERSISTENT>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-classify_kernel(ClassifyArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  unsigned char *base = smem + (size_t)warp * FastStore::bytes_per_warp();
-  FastStore st;
-  st.keys = reinterpret_cast<uint64_t *>(base);
-  st.mkey = reinterpret_cast<uint32_t *>(base + 32 * kKCap * 8);
-  st.mcnt = st.mkey + 32 * kMCap;
-  st.groups = reinterpret_cast<uint16_t *>(base + 32 * (kKCap * 8 + kMCap * 8));
-  st.lane = lane;
-  for (int i = 0; i < kMCap; i++) st.map_key(i) = 0;
-
-  Lane<W> s;
-  s.frag = ~0ull;
-  bool exhausted = false;
-  const uint64_t first = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  while (true) {
-    bool have = lane_fetch(s, a, PERSISTENT, exhausted, first);
-    if (!__any_sync(0xffffffffu, have)) break;
-    if (have) {
-      int ng = 0, nk = 0;
-      scan_segment(s, st, a, ng, nk);
-      probe_segment(st, a, nk, s.frag, s.key_ordinal);
-      s.key_ordinal += nk;
-      bool ok = replay_segment(s, st, a, ng);
-      if (!ok) {
-        // taxon map overflow: hand the fragment to the slow path
-        unsigned long long at = atomicAdd(a.defer_count, 1ull);
-        if (at < a.defer_cap) a.defer_list[at] = s.frag;
-        else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
-        for (int i = 0; i < kMCap; i++) st.map_key(i) = 0;
-        s.frag = ~0ull;
-      } else if (s.quick_stop || s.scan_done) {
-        finish_fragment(s, st, a);
-        s.frag = ~0ull;
-      }
-    }
-  }
-}
-
-// Slow path: fragments whose taxon map overflowed.  One thread per
-// fragment, all per-lane buffers in global scratch with a map large enough
-// for every token of the longest fragment.
-constexpr int kSlowKCap = 256, kSlowGCap = 320;
-using SlowStore = GlobalStore<kSlowKCap, kSlowGCap>;
-
-template <int W>
-__global__ void classify_slow_kernel(ClassifyArgs a, int mcap) {
-  const uint64_t n_list = min((uint64_t)*a.defer_count, a.defer_cap);
-  uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (tid >= n_list) return;
-  uint64_t *region = a.scratch + tid * a.scratch_stride;
-  SlowStore st;
-  st.keys = region;
-  st.groups = reinterpret_cast<uint16_t *>(region + kSlowKCap);
-  st.mkey = reinterpret_cast<uint32_t *>(region + kSlowKCap + (kSlowGCap * 2 + 7) / 8);
-  st.mcnt = st.mkey + mcap;
-  st.mcap = mcap;
-  for (int i = 0; i < mcap; i++) st.map_key(i) = 0;
-  for (uint64_t li = tid; li < n_list; li += (uint64_t)gridDim.x * blockDim.x) {
-    Lane<W> s;
-    lane_begin(s, a, a.frag_list[li]);
-    while (true) {
-      int ng = 0, nk = 0;
-      scan_segment(s, st, a, ng, nk);
-      probe_segment(st, a, nk, s.frag, s.key_ordinal | 0x80000000u);
-      s.key_ordinal += nk;
-      replay_segment(s, st, a, ng);   // cannot overflow: map sized for all tokens
-      if (s.quick_stop || s.scan_done) break;
-    }
-    finish_fragment(s, st, a);
   }
 }
 
@@ -311,7 +220,33 @@ struct ClassifyScratch {
 };
 static ClassifyScratch g_scratch[64];
 
-template <int W>
+static cudaError_t dispatch_fast(const ClassifyArgs &a, int persistent, int sms, cudaStream_t st) {
+  const bool q = a.quals != nullptr && a.cls.min_quality > 0;
+  if (a.scan.revcom_version == 0)
+    return q ? launch_fast<0, true, false>(a, persistent, sms, st)
+             : launch_fast<0, false, false>(a, persistent, sms, st);
+  switch (a.scan.w) {
+    case 5: return q ? launch_fast<5, true, true>(a, persistent, sms, st)
+                     : launch_fast<5, false, true>(a, persistent, sms, st);
+    case 1: return q ? launch_fast<1, true, true>(a, persistent, sms, st)
+                     : launch_fast<1, false, true>(a, persistent, sms, st);
+    case 7: return q ? launch_fast<7, true, true>(a, persistent, sms, st)
+                     : launch_fast<7, false, true>(a, persistent, sms, st);
+    default: return q ? launch_fast<0, true, true>(a, persistent, sms, st)
+                      : launch_fast<0, false, true>(a, persistent, sms, st);
+  }
+}
+
+static cudaError_t dispatch_slow(const ClassifyArgs &a, int mcap, unsigned blocks, unsigned threads,
+                                 cudaStream_t st) {
+  const bool q = a.quals != nullptr && a.cls.min_quality > 0;
+  if (a.scan.revcom_version == 0)
+    return q ? launch_slow<true, false>(a, mcap, blocks, threads, st)
+             : launch_slow<false, false>(a, mcap, blocks, threads, st);
+  return q ? launch_slow<true, true>(a, mcap, blocks, threads, st)
+           : launch_slow<false, true>(a, mcap, blocks, threads, st);
+}
+
 static k2g_status run_classify(const k2g_db *db, ClassifyArgs &a, int mode, uint64_t max_len,
                                cudaStream_t st) {
   const int dev = db->device;
@@ -321,6 +256,8 @@ static k2g_status run_classify(const k2g_db *db, ClassifyArgs &a, int mode, uint
   uint64_t want_defer = std::max<uint64_t>(1024, a.n_frags);
   if (sc.defer_cap < want_defer) {
     if (sc.defer_list) cudaFree(sc.defer_list);
+    sc.defer_list = nullptr;
+    sc.defer_cap = 0;
     K2G_CUDA_TRY(cudaMalloc(&sc.defer_list, want_defer * sizeof(uint64_t)));
     sc.defer_cap = want_defer;
   }
@@ -330,25 +267,7 @@ static k2g_status run_classify(const k2g_db *db, ClassifyArgs &a, int mode, uint
   a.defer_list = sc.defer_list;
   a.defer_cap = sc.defer_cap;
   a.frag_list = nullptr;
-
-  const size_t smem = (size_t)kWarpsPerBlock * FastStore::bytes_per_warp();
-  static bool attr_set[2] = {false, false};
-  auto kern = mode == K2G_MODE_PERSISTENT ? classify_kernel<W, true> : classify_kernel<W, false>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  (void)attr_set;
-  unsigned blocks;
-  if (mode == K2G_MODE_PERSISTENT) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpsPerBlock * 32, smem);
-    if (per_sm < 1) per_sm = 1;
-    uint64_t want = (uint64_t)per_sm * sm_count(dev);
-    uint64_t need = (a.n_frags + kWarpsPerBlock * 32 - 1) / (kWarpsPerBlock * 32);
-    blocks = (unsigned)std::max<uint64_t>(1, std::min(want, need));
-  } else {
-    blocks = (unsigned)std::max<uint64_t>(1, (a.n_frags + kWarpsPerBlock * 32 - 1) / (kWarpsPerBlock * 32));
-  }
-  kern<<<blocks, kWarpsPerBlock * 32, smem, st>>>(a);
-  K2G_CUDA_TRY(cudaGetLastError());
+  K2G_CUDA_TRY(dispatch_fast(a, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), st));
 
   // Slow path for fragments whose taxon map overflowed.  The fragment count
   // stays on the device, so no host synchronisation is needed here.
@@ -372,8 +291,7 @@ static k2g_status run_classify(const k2g_db *db, ClassifyArgs &a, int mode, uint
   a.scratch = sc.slow;
   a.scratch_stride = stride;
   a.frag_list = sc.defer_list;
-  classify_slow_kernel<W><<<(unsigned)(nthreads / threads), threads, 0, st>>>(a, mcap);
-  K2G_CUDA_TRY(cudaGetLastError());
+  K2G_CUDA_TRY(dispatch_slow(a, mcap, (unsigned)(nthreads / threads), threads, st));
   return K2G_OK;
 }
 
@@ -446,6 +364,8 @@ extern "C" k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
   if (out->d_hit_keys && (!out->d_hit_taxa || !out->d_hit_order || !out->d_hits_used))
     return fail(K2G_ERR_ARG, "incomplete hit event buffers");
   if (reads->max_seq_len >= (1ull << 31)) return fail(K2G_ERR_ARG, "sequence too long");
+  if (((uintptr_t)reads->d_bases & 15u) || ((uintptr_t)reads->d_quals & 15u))
+    return fail(K2G_ERR_ARG, "d_bases and d_quals must be 16-byte aligned");
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   ClassifyArgs a{};
   a.table = db->table_view();
@@ -475,12 +395,7 @@ extern "C" k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
   a.hits_used = reinterpret_cast<unsigned long long *>(out->d_hits_used);
   a.status = out->d_status;
   cudaStream_t st = (cudaStream_t)stream;
-  switch (a.scan.w) {
-    case 1: return run_classify<1>(db, a, mode, reads->max_seq_len, st);
-    case 5: return run_classify<5>(db, a, mode, reads->max_seq_len, st);
-    case 7: return run_classify<7>(db, a, mode, reads->max_seq_len, st);
-    default: return run_classify<0>(db, a, mode, reads->max_seq_len, st);
-  }
+  return run_classify(db, a, mode, reads->max_seq_len, st);
 }
 
 extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
