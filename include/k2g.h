@@ -122,7 +122,8 @@ typedef struct {
 
 typedef struct {
   const char *d_bases;        /* concatenated sequences, ASCII              */
-  const char *d_quals;        /* NULL, or qualities in the same layout      */
+  const char *d_quals;        /* NULL, or qualities in the same layout, at
+                                 the same address alignment modulo 16      */
   const uint64_t *d_seq_off;  /* n_seqs + 1 offsets                         */
   uint64_t n_frags;           /* n_seqs = n_frags * (paired ? 2 : 1)        */
   uint64_t max_seq_len;       /* longest sequence (sizes scratch)           */

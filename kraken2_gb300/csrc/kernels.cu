@@ -364,8 +364,10 @@ extern "C" k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
   if (out->d_hit_keys && (!out->d_hit_taxa || !out->d_hit_order || !out->d_hits_used))
     return fail(K2G_ERR_ARG, "incomplete hit event buffers");
   if (reads->max_seq_len >= (1ull << 31)) return fail(K2G_ERR_ARG, "sequence too long");
-  if (((uintptr_t)reads->d_bases & 15u) || ((uintptr_t)reads->d_quals & 15u))
-    return fail(K2G_ERR_ARG, "d_bases and d_quals must be 16-byte aligned");
+  // Bases are read as the 16-byte aligned chunks that contain them (such a
+  // chunk never leaves the allocation); qualities must share that alignment.
+  if (reads->d_quals && (((uintptr_t)reads->d_bases - (uintptr_t)reads->d_quals) & 15u))
+    return fail(K2G_ERR_ARG, "d_bases and d_quals must have the same alignment modulo 16");
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   ClassifyArgs a{};
   a.table = db->table_view();
