@@ -391,19 +391,19 @@ __device__ __forceinline__ void probe_segment(Store &st, const ClassifyArgs &a, 
   const TableView &t = a.table;
   for (int j0 = 0; j0 < nk; j0 += B) {
     uint64_t hc[B], idx[B];
-    uint32_t cell[B];
+    Sector sec[B];
 #pragma unroll
     for (int b = 0; b < B; b++) {
       if (j0 + b < nk) {
         hc[b] = murmur3(st.key(j0 + b));
         idx[b] = fast_mod(hc[b], t.div);
-        cell[b] = load_cell(t.cells + idx[b]);
+        sec[b] = load_sector(t.cells, idx[b] & ~7ull);
       }
     }
 #pragma unroll
     for (int b = 0; b < B; b++) {
       if (j0 + b < nk) {
-        uint32_t v = probe_from(t, hc[b], idx[b], cell[b]);
+        uint32_t v = probe_sectors(t, hc[b], idx[b], sec[b]);
         if (a.hit_keys && v) emit_hit(a, frag, key_ordinal + j0 + b, st.key(j0 + b), v);
         st.val(j0 + b) = v;
       }

@@ -43,6 +43,66 @@ __device__ __forceinline__ uint32_t probe_from(const TableView &t, uint64_t hc, 
   }
 }
 
+// One aligned 32-byte sector (8 cells) of the table.  The table allocation
+// is padded to whole sectors, so the load never leaves it.
+struct Sector {
+  uint4 lo, hi;
+};
+
+__device__ __forceinline__ Sector load_sector(const uint32_t *cells, uint64_t base) {
+  const uint4 *p = reinterpret_cast<const uint4 *>(cells + base);
+  Sector s;
+  s.lo = __ldg(p);
+  s.hi = __ldg(p + 1);
+  return s;
+}
+
+// Get() resolved a sector at a time.  Starting at cell `idx` of the sector
+// loaded in `sec` (base = idx & ~7), the first cell that is empty or holds
+// the compacted key ends the walk (src/compact_hash.h:362-373); cells past
+// the capacity are not part of the table and the walk wraps to cell 0.  The
+// result is identical to the cell-by-cell walk of probe_from.
+__device__ __forceinline__ uint32_t probe_sectors(const TableView &t, uint64_t hc, uint64_t idx,
+                                                  Sector sec) {
+  const uint32_t ck = (uint32_t)(hc >> t.key_shift);
+  uint64_t base = idx & ~7ull;
+  uint32_t off = (uint32_t)(idx & 7u);
+  uint64_t walked = 0;
+  while (true) {
+    const uint32_t c[8] = {sec.lo.x, sec.lo.y, sec.lo.z, sec.lo.w,
+                           sec.hi.x, sec.hi.y, sec.hi.z, sec.hi.w};
+    const uint64_t left = t.capacity - base;             // real cells from base on
+    const uint32_t real = left >= 8 ? 0xFFu : ((1u << (uint32_t)left) - 1u);
+    uint32_t stop = 0, match = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const bool empty = (c[i] & t.value_mask) == 0;
+      const bool hit = !empty && (c[i] >> t.value_bits) == ck;
+      stop |= (uint32_t)(empty || hit) << i;
+      match |= (uint32_t)hit << i;
+    }
+    const uint32_t window = real & (0xFFu << off);
+    stop &= window;
+    const uint32_t span = __popc(window);
+    if (stop) {
+      const int i = __ffs(stop) - 1;
+      // the full-table guard of Get(): a walk over all cells finds nothing
+      if (walked + (uint32_t)(i - (int)off) >= t.capacity) return 0;
+      if (!((match >> i) & 1u)) return 0;
+      uint32_t v = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) v = (j == i) ? c[j] : v;
+      return v & t.value_mask;
+    }
+    walked += span;
+    if (walked >= t.capacity) return 0;
+    base += 8;
+    if (base >= t.capacity) base = 0;
+    off = 0;
+    sec = load_sector(t.cells, base);
+  }
+}
+
 __device__ __forceinline__ uint32_t table_get(const TableView &t, uint64_t key) {
   uint64_t hc = murmur3(key);
   uint64_t idx = fast_mod(hc, t.div);

@@ -64,20 +64,20 @@ __global__ void lookup_kernel(TableView t, const uint64_t *keys, uint32_t *vals,
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += stride * B) {
     uint64_t hc[B], idx[B];
-    uint32_t cell[B];
+    Sector sec[B];
 #pragma unroll
     for (int b = 0; b < B; b++) {
       uint64_t i = i0 + b * stride;
       if (i < n) {
         hc[b] = murmur3(keys[i]);
         idx[b] = fast_mod(hc[b], t.div);
-        cell[b] = load_cell(t.cells + idx[b]);
+        sec[b] = load_sector(t.cells, idx[b] & ~7ull);
       }
     }
 #pragma unroll
     for (int b = 0; b < B; b++) {
       uint64_t i = i0 + b * stride;
-      if (i < n) vals[i] = probe_from(t, hc[b], idx[b], cell[b]);
+      if (i < n) vals[i] = probe_sectors(t, hc[b], idx[b], sec[b]);
     }
   }
 }
