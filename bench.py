@@ -289,8 +289,9 @@ class DeviceRunner:
 
     def classify(self, b0, n, events=None):
         wl, k2g, cfg = self.wl, self.wl.k2g, self.wl.cfg
-        reads = k2g.Reads(wl.reads.data_ptr() + b0 * cfg.read_len, None, self.off.data_ptr(), n,
-                          cfg.read_len, None, b0)
+        reads = k2g.Reads(d_bases=wl.reads.data_ptr() + b0 * cfg.read_len, d_quals=None,
+                          d_seq_off=self.off.data_ptr(), n_frags=n, max_seq_len=cfg.read_len,
+                          total_bases=n * cfg.read_len, d_frag_block=None, frag_base=b0)
         res = k2g.Results(self.call.data_ptr(), self.hg.data_ptr(), self.hoff.data_ptr(),
                           self.hlen.data_ptr(), self.runs.data_ptr(), self.runs_cap,
                           self.tr.data_ptr(), None, None, None, 0, None, self.status.data_ptr())
@@ -453,7 +454,8 @@ def run_ours(args, log):
     rank, world, local, pg = dist_setup(args.gpus)
     cfg = Config(args.scale)
     wl = Workload(cfg, local, log=log if rank == 0 else (lambda *_: None))
-    mode = wl.k2g.MODE_PLAIN if args.mode == "plain" else wl.k2g.MODE_PERSISTENT
+    mode = {"plain": wl.k2g.MODE_PLAIN, "persistent": wl.k2g.MODE_PERSISTENT,
+            "pipelined": wl.k2g.MODE_PIPELINED}[args.mode]
     runner = DeviceRunner(wl, mode)
     if args.profile:
         # for ncu: setup, then exactly two classification steps
@@ -639,7 +641,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="persistent", choices=["persistent", "plain"])
+    ap.add_argument("--mode", default="pipelined", choices=["pipelined", "persistent", "plain"])
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the full-size workload (tests and probes only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

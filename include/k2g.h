@@ -127,6 +127,8 @@ typedef struct {
   const uint64_t *d_seq_off;  /* n_seqs + 1 offsets                         */
   uint64_t n_frags;           /* n_seqs = n_frags * (paired ? 2 : 1)        */
   uint64_t max_seq_len;       /* longest sequence (sizes scratch)           */
+  uint64_t total_bases;       /* d_seq_off[n_seqs] - d_seq_off[0], or 0 to
+                                 have it read from the device (synchronous) */
   const uint32_t *d_frag_block; /* reader block of each fragment (HLL), or NULL */
   uint64_t frag_base;         /* ordinal of fragment 0 in the whole run     */
 } k2g_reads;
@@ -154,8 +156,10 @@ typedef struct {
 } k2g_results;
 
 typedef enum {
-  K2G_MODE_PLAIN = 0,         /* one launch per batch, fixed fragment map   */
-  K2G_MODE_PERSISTENT = 1     /* persistent work-stealing kernel (default)  */
+  K2G_MODE_PLAIN = 0,         /* fused kernel, one thread per fragment      */
+  K2G_MODE_PERSISTENT = 1,    /* fused kernel, work-stealing lanes          */
+  K2G_MODE_PIPELINED = 2      /* scan / probe / resolve stages over
+                                 overlapping sub-batches (fastest)          */
 } k2g_mode;
 
 /* Classifies a batch of fragments held in device memory. */

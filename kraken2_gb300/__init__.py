@@ -25,6 +25,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_IO", 3: "ERR_FORMAT", 4: "ERR_CUD
                 9: "ERR_BUDGET"}
 MODE_PLAIN = 0
 MODE_PERSISTENT = 1
+MODE_PIPELINED = 2
 CODE_MATE_BORDER = 0xFFFFFFFF
 CODE_AMBIGUOUS = 0xFFFFFFFD
 
@@ -60,7 +61,7 @@ class ClassifyParams(C.Structure):
 
 class Reads(C.Structure):
     _fields_ = [("d_bases", C.c_void_p), ("d_quals", C.c_void_p), ("d_seq_off", C.c_void_p),
-                ("n_frags", C.c_uint64), ("max_seq_len", C.c_uint64),
+                ("n_frags", C.c_uint64), ("max_seq_len", C.c_uint64), ("total_bases", C.c_uint64),
                 ("d_frag_block", C.c_void_p), ("frag_base", C.c_uint64)]
 
 

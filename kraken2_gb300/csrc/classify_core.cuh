@@ -69,6 +69,7 @@ struct ClassifyArgs {
   const uint64_t *seq_off;
   uint64_t n_frags;
   uint64_t frag_base;
+  uint64_t frag_off;               // index of fragment 0 of this view in the caller's batch
   // outputs
   uint32_t *call;
   uint32_t *hit_groups;
@@ -228,7 +229,7 @@ __device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, ui
   s.key_ordinal = 0;
   s.distinct = 0;
   s.quick_stop = false;
-  s.run_base = o0 + 2 * f;
+  s.run_base = o0 + 2 * (f + a.frag_off);
 }
 
 // ---- scan phase ----------------------------------------------------------
@@ -446,9 +447,8 @@ __device__ __forceinline__ uint32_t map_get(Store &st, uint32_t taxon) {
   }
 }
 
-template <int W>
-__device__ __forceinline__ void emit_run(Lane<W> &s, const ClassifyArgs &a, uint32_t code,
-                                         uint32_t n) {
+template <class L>
+__device__ __forceinline__ void emit_run(L &s, const ClassifyArgs &a, uint32_t code, uint32_t n) {
   if (s.run_cnt && s.run_code == code) {
     s.run_cnt += n;
     return;
@@ -508,8 +508,8 @@ __device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const Clas
 }
 
 // ---- resolve and write -------------------------------------------------
-template <int W, class Store>
-__device__ __forceinline__ void finish_fragment(Lane<W> &s, Store &st, const ClassifyArgs &a) {
+template <class L, class Store>
+__device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyArgs &a) {
   const uint32_t *parent = a.parent;
   uint32_t total = s.total_tokens;
   if (a.cls.paired) total -= 1;

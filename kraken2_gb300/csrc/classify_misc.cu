@@ -1,6 +1,7 @@
 // Instantiations of the classify kernels for other windows (k == l, k - l = 6,
 // runtime window), the legacy reverse complement, and the slow path.
 #include "classify_kernels.cuh"
+#include "pipeline.cuh"
 
 namespace k2g {
 template cudaError_t launch_fast<1, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
@@ -15,4 +16,12 @@ template cudaError_t launch_slow<false, true>(const ClassifyArgs &, int, unsigne
 template cudaError_t launch_slow<true, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 template cudaError_t launch_slow<false, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 template cudaError_t launch_slow<true, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
+template cudaError_t launch_pipe_scan<1, false, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<1, true, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<7, false, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<7, true, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<0, false, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<0, true, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<0, false, false>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_scan<0, true, false>(const PipeArgs &, cudaStream_t);
 }  // namespace k2g

@@ -243,6 +243,7 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
     rd.d_seq_off = s.off;
     rd.n_frags = nf;
     rd.max_seq_len = max_len;
+    rd.total_bases = nb;
     rd.frag_base = f0;
     k2g_results rs{};
     rs.d_call = s.call;
@@ -252,7 +253,7 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
     rs.runs_cap = sparse_cap;
     rs.d_taxon_reads = reinterpret_cast<uint64_t *>(d_taxon_reads);
     rs.d_status = s.status;
-    status = k2g_classify(db, &rd, params, &rs, K2G_MODE_PERSISTENT, s.st);
+    status = k2g_classify(db, &rd, params, &rs, K2G_MODE_PIPELINED, s.st);
     if (status != K2G_OK) { cleanup(); return status; }
     status = compact_runs(s.sparse, s.off, per, s.hlen, nf, s.excl, s.sums, s.total, s.dense, s.st);
     if (status != K2G_OK) { cleanup(); return status; }

@@ -8,6 +8,7 @@
 
 #include "classify_kernels.cuh"
 #include "k2g_internal.h"
+#include "pipeline.cuh"
 
 namespace k2g {
 // compiled in classify_w5.cu / classify_misc.cu
@@ -25,6 +26,16 @@ extern template cudaError_t launch_slow<false, true>(const ClassifyArgs &, int, 
 extern template cudaError_t launch_slow<true, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 extern template cudaError_t launch_slow<false, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 extern template cudaError_t launch_slow<true, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<5, false, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<5, true, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<1, false, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<1, true, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<7, false, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<7, true, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<0, false, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<0, true, true>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<0, false, false>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_scan<0, true, false>(const PipeArgs &, cudaStream_t);
 }  // namespace k2g
 
 namespace k2g {
@@ -209,16 +220,85 @@ static void launch_scan(const ScanView &sv, const uint8_t *bases, const uint64_t
   scan_kernel<W><<<(unsigned)blocks, 128, 0, st>>>(sv, bases, off, n, mins, amb);
 }
 
-struct ClassifyScratch {
-  std::mutex mu;
-  int device = -1;
+// Each classification sub-batch runs on one of two internal execution
+// contexts: a stream plus every piece of device scratch the kernels of one
+// sub-batch use (work counter, deferred-fragment list, slow-path scratch,
+// pipeline buffers).  Consecutive sub-batches alternate contexts, so the
+// stages of one overlap those of the other, and scratch is never shared by
+// work that can run concurrently.  The caller's stream is joined through
+// events, so calls stay asynchronous and capturable.
+struct ExecCtx {
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
   unsigned long long *counters = nullptr;   // [0] next_frag, [1] defer_count
   uint64_t *defer_list = nullptr;
   uint64_t defer_cap = 0;
   uint64_t *slow = nullptr;
   size_t slow_bytes = 0;
+  uint16_t *gstream = nullptr;
+  uint32_t *gtax = nullptr;
+  uint64_t *rkey = nullptr;
+  uint32_t *rslot = nullptr;
+  uint64_t cap_slots = 0;
+  uint32_t *gcount = nullptr;
+  uint32_t *bcount = nullptr;
+  uint64_t cap_frags = 0;
 };
-static ClassifyScratch g_scratch[64];
+
+struct DeviceState {
+  std::mutex mu;
+  bool init = false;
+  cudaEvent_t start = nullptr;
+  ExecCtx ctx[2];
+  int next = 0;           // context of the next sub-batch (round robin across calls)
+};
+static DeviceState g_state[64];
+
+template <class T>
+static cudaError_t grow(T *&p, uint64_t &cap, uint64_t want) {
+  if (cap >= want) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+  if (e == cudaSuccess) cap = want;
+  return e;
+}
+
+static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t slow_bytes,
+                              bool pipeline) {
+  if (!c.st) {
+    K2G_CUDA_TRY(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+    K2G_CUDA_TRY(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    K2G_CUDA_TRY(cudaMalloc(&c.counters, 2 * sizeof(unsigned long long)));
+  }
+  K2G_CUDA_TRY(grow(c.defer_list, c.defer_cap, std::max<uint64_t>(1024, frags)));
+  if (c.slow_bytes < slow_bytes) {
+    if (c.slow) cudaFree(c.slow);
+    c.slow = nullptr;
+    c.slow_bytes = 0;
+    K2G_CUDA_TRY(cudaMalloc(&c.slow, slow_bytes));
+    c.slow_bytes = slow_bytes;
+  }
+  if (pipeline) {
+    uint64_t cs = c.cap_slots;
+    K2G_CUDA_TRY(grow(c.gstream, cs, slots));
+    cs = c.cap_slots;
+    K2G_CUDA_TRY(grow(c.gtax, cs, slots));
+    cs = c.cap_slots;
+    K2G_CUDA_TRY(grow(c.rkey, cs, slots));
+    cs = c.cap_slots;
+    K2G_CUDA_TRY(grow(c.rslot, cs, slots));
+    c.cap_slots = std::max(c.cap_slots, slots);
+    uint64_t cf = c.cap_frags;
+    K2G_CUDA_TRY(grow(c.gcount, cf, frags));
+    cf = c.cap_frags;
+    uint64_t blocks = (frags + kPipeBlock - 1) / kPipeBlock;
+    K2G_CUDA_TRY(grow(c.bcount, cf, std::max(frags, blocks)));
+    c.cap_frags = std::max(c.cap_frags, frags);
+  }
+  return K2G_OK;
+}
 
 static cudaError_t dispatch_fast(const ClassifyArgs &a, int persistent, int sms, cudaStream_t st) {
   const bool q = a.quals != nullptr && a.cls.min_quality > 0;
@@ -237,6 +317,19 @@ static cudaError_t dispatch_fast(const ClassifyArgs &a, int persistent, int sms,
   }
 }
 
+static cudaError_t dispatch_pipe_scan(const PipeArgs &p, cudaStream_t st) {
+  const ClassifyArgs &a = p.a;
+  const bool q = a.quals != nullptr && a.cls.min_quality > 0;
+  if (a.scan.revcom_version == 0)
+    return q ? launch_pipe_scan<0, true, false>(p, st) : launch_pipe_scan<0, false, false>(p, st);
+  switch (a.scan.w) {
+    case 5: return q ? launch_pipe_scan<5, true, true>(p, st) : launch_pipe_scan<5, false, true>(p, st);
+    case 1: return q ? launch_pipe_scan<1, true, true>(p, st) : launch_pipe_scan<1, false, true>(p, st);
+    case 7: return q ? launch_pipe_scan<7, true, true>(p, st) : launch_pipe_scan<7, false, true>(p, st);
+    default: return q ? launch_pipe_scan<0, true, true>(p, st) : launch_pipe_scan<0, false, true>(p, st);
+  }
+}
+
 static cudaError_t dispatch_slow(const ClassifyArgs &a, int mcap, unsigned blocks, unsigned threads,
                                  cudaStream_t st) {
   const bool q = a.quals != nullptr && a.cls.min_quality > 0;
@@ -247,51 +340,108 @@ static cudaError_t dispatch_slow(const ClassifyArgs &a, int mcap, unsigned block
            : launch_slow<false, true>(a, mcap, blocks, threads, st);
 }
 
-static k2g_status run_classify(const k2g_db *db, ClassifyArgs &a, int mode, uint64_t max_len,
-                               cudaStream_t st) {
-  const int dev = db->device;
-  ClassifyScratch &sc = g_scratch[dev & 63];
-  std::lock_guard<std::mutex> lock(sc.mu);
-  if (!sc.counters) K2G_CUDA_TRY(cudaMalloc(&sc.counters, 2 * sizeof(unsigned long long)));
-  uint64_t want_defer = std::max<uint64_t>(1024, a.n_frags);
-  if (sc.defer_cap < want_defer) {
-    if (sc.defer_list) cudaFree(sc.defer_list);
-    sc.defer_list = nullptr;
-    sc.defer_cap = 0;
-    K2G_CUDA_TRY(cudaMalloc(&sc.defer_list, want_defer * sizeof(uint64_t)));
-    sc.defer_cap = want_defer;
-  }
-  K2G_CUDA_TRY(cudaMemsetAsync(sc.counters, 0, 2 * sizeof(unsigned long long), st));
-  a.next_frag = sc.counters;
-  a.defer_count = sc.counters + 1;
-  a.defer_list = sc.defer_list;
-  a.defer_cap = sc.defer_cap;
-  a.frag_list = nullptr;
-  K2G_CUDA_TRY(dispatch_fast(a, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), st));
+// Slow-path geometry for fragments up to max_len bases per mate.
+struct SlowPlan {
+  int mcap;
+  size_t stride;        // 64-bit words per thread
+  uint64_t threads;     // total threads
+  size_t bytes;
+};
 
-  // Slow path for fragments whose taxon map overflowed.  The fragment count
-  // stays on the device, so no host synchronisation is needed here.
-  const uint64_t per = a.cls.paired ? 2 : 1;
-  uint64_t tokens = per * std::max<uint64_t>(max_len, 1) + 2;
-  int mcap = 64;
-  while ((uint64_t)mcap < 2 * tokens + 2) mcap <<= 1;
-  const int threads = 128;
-  size_t stride = kSlowKCap + (kSlowGCap * 2 + 7) / 8 + (size_t)mcap;   // 64-bit words
-  uint64_t nthreads = (1ull << 30) / (stride * 8);
-  nthreads = std::max<uint64_t>(threads, std::min<uint64_t>(nthreads, 8192));
-  nthreads = nthreads / threads * threads;
-  size_t bytes = nthreads * stride * 8;
-  if (sc.slow_bytes < bytes) {
-    if (sc.slow) cudaFree(sc.slow);
-    sc.slow = nullptr;
-    sc.slow_bytes = 0;
-    K2G_CUDA_TRY(cudaMalloc(&sc.slow, bytes));
-    sc.slow_bytes = bytes;
+static SlowPlan slow_plan(uint64_t max_len, bool paired) {
+  SlowPlan p;
+  const uint64_t per = paired ? 2 : 1;
+  const uint64_t tokens = per * std::max<uint64_t>(max_len, 1) + 2;
+  p.mcap = 64;
+  while ((uint64_t)p.mcap < 2 * tokens + 2) p.mcap <<= 1;
+  p.stride = kSlowKCap + (kSlowGCap * 2 + 7) / 8 + (size_t)p.mcap;
+  uint64_t n = (1ull << 30) / (p.stride * 8);
+  n = std::max<uint64_t>(128, std::min<uint64_t>(n, 8192));
+  p.threads = n / 128 * 128;
+  p.bytes = p.threads * p.stride * 8;
+  return p;
+}
+
+// Fragments per sub-batch and slot capacity for a batch of n fragments
+// holding total_bases bases.
+static void sub_batch_plan(uint64_t n, uint64_t total_bases, int per, uint64_t max_len,
+                           uint64_t &sb_frags, uint64_t &cap_slots) {
+  const uint64_t target_bases = 256ull << 20;
+  const double avg = n ? (double)total_bases / (double)n : 1.0;   // bases per fragment
+  sb_frags = (uint64_t)std::max(1.0, target_bases / std::max(avg, 1.0));
+  sb_frags = std::min<uint64_t>(sb_frags, 2ull << 20);
+  sb_frags = std::max<uint64_t>(kPipeBlock, sb_frags / kPipeBlock * kPipeBlock);
+  sb_frags = std::min<uint64_t>(sb_frags, n);
+  // Twice the average sub-batch, and room for at least a block of the
+  // longest fragments; fragments beyond the capacity take the slow path.
+  cap_slots = (uint64_t)(2.0 * avg * sb_frags) + 2 * sb_frags +
+              (uint64_t)kPipeBlock * (per * max_len + 2) + 64;
+}
+
+static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mode,
+                               uint64_t max_len, uint64_t total_bases, cudaStream_t caller) {
+  const int dev = db->device;
+  DeviceState &ds = g_state[dev & 63];
+  std::lock_guard<std::mutex> lock(ds.mu);
+  if (!ds.init) {
+    K2G_CUDA_TRY(cudaEventCreateWithFlags(&ds.start, cudaEventDisableTiming));
+    ds.init = true;
   }
-  a.scratch = sc.slow;
-  a.scratch_stride = stride;
-  a.frag_list = sc.defer_list;
-  K2G_CUDA_TRY(dispatch_slow(a, mcap, (unsigned)(nthreads / threads), threads, st));
+  const int per = a0.cls.paired ? 2 : 1;
+  const bool pipeline = mode == K2G_MODE_PIPELINED;
+  uint64_t sb_frags = a0.n_frags, cap_slots = 0;
+  if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, sb_frags, cap_slots);
+  const SlowPlan sp = slow_plan(max_len, a0.cls.paired != 0);
+  for (auto &c : ds.ctx) {
+    k2g_status s = ctx_reserve(c, sb_frags, cap_slots, sp.bytes, pipeline);
+    if (s != K2G_OK) return s;
+  }
+  K2G_CUDA_TRY(cudaEventRecord(ds.start, caller));
+  for (auto &c : ds.ctx) K2G_CUDA_TRY(cudaStreamWaitEvent(c.st, ds.start, 0));
+  int &k = ds.next;
+  for (uint64_t f0 = 0; f0 < a0.n_frags; f0 += sb_frags, k ^= 1) {
+    ExecCtx &c = ds.ctx[k];
+    const uint64_t n = std::min(sb_frags, a0.n_frags - f0);
+    ClassifyArgs a = a0;
+    a.seq_off = a0.seq_off + f0 * per;
+    a.n_frags = n;
+    a.frag_base = a0.frag_base + f0;
+    a.frag_off = a0.frag_off + f0;
+    a.call = a0.call + f0;
+    if (a0.hit_groups) a.hit_groups = a0.hit_groups + f0;
+    if (a0.hitlist_off) a.hitlist_off = a0.hitlist_off + f0;
+    if (a0.hitlist_len) a.hitlist_len = a0.hitlist_len + f0;
+    a.next_frag = c.counters;
+    a.defer_count = c.counters + 1;
+    a.defer_list = c.defer_list;
+    a.defer_cap = c.defer_cap;
+    a.frag_list = nullptr;
+    a.scratch = c.slow;
+    a.scratch_stride = sp.stride;
+    K2G_CUDA_TRY(cudaMemsetAsync(c.counters, 0, 2 * sizeof(unsigned long long), c.st));
+    if (pipeline) {
+      PipeArgs p;
+      p.a = a;
+      p.gstream = c.gstream;
+      p.gtax = c.gtax;
+      p.gcount = c.gcount;
+      p.rkey = c.rkey;
+      p.rslot = c.rslot;
+      p.bcount = c.bcount;
+      p.cap_slots = c.cap_slots;
+      K2G_CUDA_TRY(dispatch_pipe_scan(p, c.st));
+      K2G_CUDA_TRY(launch_pipe_probe(p, c.st));
+      K2G_CUDA_TRY(launch_pipe_resolve(p, c.st));
+    } else {
+      K2G_CUDA_TRY(dispatch_fast(a, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), c.st));
+    }
+    a.frag_list = c.defer_list;
+    K2G_CUDA_TRY(dispatch_slow(a, sp.mcap, (unsigned)(sp.threads / 128), 128, c.st));
+  }
+  for (auto &c : ds.ctx) {
+    K2G_CUDA_TRY(cudaEventRecord(c.done, c.st));
+    K2G_CUDA_TRY(cudaStreamWaitEvent(caller, c.done, 0));
+  }
   return K2G_OK;
 }
 
@@ -397,7 +547,17 @@ extern "C" k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
   a.hits_used = reinterpret_cast<unsigned long long *>(out->d_hits_used);
   a.status = out->d_status;
   cudaStream_t st = (cudaStream_t)stream;
-  return run_classify(db, a, mode, reads->max_seq_len, st);
+  uint64_t total = reads->total_bases;
+  if (!total) {
+    // not given: read d_seq_off[0] and d_seq_off[n_seqs] (synchronous)
+    const uint64_t n_seqs = reads->n_frags * (params->paired ? 2 : 1);
+    uint64_t ends[2];
+    K2G_CUDA_TRY(cudaMemcpyAsync(&ends[0], reads->d_seq_off, 8, cudaMemcpyDeviceToHost, st));
+    K2G_CUDA_TRY(cudaMemcpyAsync(&ends[1], reads->d_seq_off + n_seqs, 8, cudaMemcpyDeviceToHost, st));
+    K2G_CUDA_TRY(cudaStreamSynchronize(st));
+    total = ends[1] - ends[0];
+  }
+  return run_classify(db, a, mode, reads->max_seq_len, total, st);
 }
 
 extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,

@@ -1,0 +1,377 @@
+// Pipelined classification: scan -> probe -> resolve as three kernels.
+//
+// The fused kernel keeps every per-read buffer of a warp in shared memory,
+// which caps it at 12 warps per SM; at that occupancy the scan arithmetic and
+// the random table loads do not overlap (measured ~1 instruction per cycle
+// per SM).  Here each stage is its own kernel at high occupancy, and the
+// stages of consecutive sub-batches run on different streams:
+//
+//   scan     one thread per fragment: minimizers and token groups
+//            (src/classify.cc:797-838).  Groups go to a per-fragment slice of
+//            `gstream`; every LOOKUP key becomes a record (key, group slot)
+//            appended to its block's record range.
+//   probe    one thread per record: CompactHashTable::Get
+//            (src/compact_hash.h:355-374), the value stored at the record's
+//            group slot in `gtax`.
+//   resolve  one thread per fragment: replay of the groups with their taxa
+//            (src/classify.cc:847-906), ResolveTree (:710-762), hit-list runs
+//            (:950-991) and the outputs.
+//
+// Fragment f's groups occupy slots [gbase(f), gbase(f) + gcount[f]) with
+// gbase(f) = seq_off[f * per] - seq_off[0] + 2 f; a block's records start at
+// the gbase of its first fragment, since a fragment has no more LOOKUP
+// tokens than groups.
+#pragma once
+
+#include "classify_core.cuh"
+
+namespace k2g {
+
+constexpr int kPipeBlock = 128;     // fragments per scan / resolve block
+constexpr int kStage = 16;          // staged keys per lane (one chunk)
+
+struct PipeArgs {
+  ClassifyArgs a;
+  uint16_t *gstream;
+  uint32_t *gtax;
+  uint32_t *gcount;
+  uint64_t *rkey;
+  uint32_t *rslot;
+  uint32_t *bcount;
+  uint64_t cap_slots;     // capacity of gstream / gtax / records
+};
+
+__device__ __forceinline__ uint64_t pipe_gbase(const PipeArgs &p, uint64_t f) {
+  const int per = p.a.cls.paired ? 2 : 1;
+  return p.a.seq_off[f * per] - p.a.seq_off[0] + 2 * f;
+}
+
+// Scan state of one fragment (registers).
+template <int W>
+struct ScanLane {
+  const uint8_t *ap, *aq;
+  uint32_t head, nchunks, ci, len;
+  const uint8_t *seq2, *qual2;
+  uint32_t len2, mate;
+  uint4 c0, c1, q0, q1;
+  uint64_t fwd, rc;
+  int32_t run, last_amb;
+  Window<W> win;
+  uint64_t last_min;
+  uint32_t gkind, glen;
+  uint32_t ng;            // groups written
+  uint64_t gbase;
+  bool done;
+};
+
+template <int W>
+__device__ __forceinline__ void scanlane_mate(ScanLane<W> &s, const uint8_t *seq, const uint8_t *qual,
+                                              uint32_t len) {
+  const uint32_t head = (uint32_t)((uintptr_t)seq & 15u);
+  s.head = head;
+  s.ap = seq - head;
+  s.aq = qual ? qual - head : nullptr;
+  s.len = len;
+  s.nchunks = (head + len + 15) / 16;
+  s.ci = 0;
+  s.c0 = load_chunk(s.ap, 0, s.nchunks);
+  s.c1 = load_chunk(s.ap, 1, s.nchunks);
+  if (qual) {
+    s.q0 = load_chunk(s.aq, 0, s.nchunks);
+    s.q1 = load_chunk(s.aq, 1, s.nchunks);
+  }
+  s.fwd = s.rc = 0;
+  s.run = 0;
+  s.last_amb = -1;
+  s.win.reset();
+  s.last_min = ~0ull;
+}
+
+// One base; groups go straight to the global stream, keys to the lane's
+// staging slots (kept branch-free so the warp stays in step).
+template <int W, bool RC1>
+__device__ __forceinline__ void pipe_scan_base(ScanLane<W> &s, const PipeArgs &pa, const ScanConst &c,
+                                               int32_t p, uint32_t valid, uint32_t code,
+                                               uint64_t *skey, uint32_t *sslot, int &nst) {
+  s.fwd = ((s.fwd << 2) | code) & c.lmer_mask;
+  s.rc = (s.rc >> 2) | ((uint64_t)(code ^ 3u) << c.top_shift);
+  s.run = valid ? s.run + 1 : 0;
+  s.last_amb = valid ? s.last_amb : p;
+  const uint64_t rcv = RC1 ? s.rc : revcomp_v0(s.fwd, c.lmer_mask);
+  uint64_t cand = ((s.fwd < rcv ? s.fwd : rcv) & c.smask) ^ c.toggle;
+  cand = (s.run >= c.l) ? cand : ~0ull;
+  s.win.push(cand);
+  const bool emit = (p >= c.k - 1) && (p < (int32_t)s.len);
+  const bool amb = (p - s.last_amb) <= c.amb_span;
+  const uint64_t m = s.win.min(c.w) ^ c.toggle;
+  const bool nonamb = emit && !amb;
+  const bool is_new = nonamb && (m != s.last_min);
+  s.last_min = nonamb ? m : s.last_min;
+  bool skip = false;
+  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  const bool is_key = is_new && !skip;
+  const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
+  const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
+                                       : (tkind == G_CONT && s.gkind != G_AMBIG && s.gkind != G_NONE);
+  const bool newg = emit && !cont;
+  const bool close = newg && (s.gkind != G_NONE);
+  if (close) pa.gstream[s.gbase + s.ng] = make_group(s.gkind, s.glen);
+  s.ng += close ? 1u : 0u;
+  s.glen = emit ? (newg ? 1u : s.glen + 1u) : s.glen;
+  s.gkind = newg ? tkind : s.gkind;
+  if (is_key) {
+    skey[nst * kPipeBlock] = m;
+    sslot[nst * kPipeBlock] = (uint32_t)s.ng;   // the slot this KEY group will close into
+  }
+  nst += is_key ? 1 : 0;
+}
+
+template <int W, bool QUAL, bool RC1>
+__global__ void __launch_bounds__(kPipeBlock)
+pipe_scan_kernel(PipeArgs pa) {
+  __shared__ uint64_t s_key[kStage * kPipeBlock];
+  __shared__ uint32_t s_slot[kStage * kPipeBlock];
+  __shared__ uint32_t s_count;
+  const ClassifyArgs &a = pa.a;
+  const uint64_t f0 = (uint64_t)blockIdx.x * kPipeBlock;
+  const uint64_t f = f0 + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) s_count = 0;
+  __syncthreads();
+  const uint64_t rbase = pipe_gbase(pa, f0);
+  uint64_t *skey = s_key + threadIdx.x;
+  uint32_t *sslot = s_slot + threadIdx.x;
+  const ScanConst c = scan_const(a);
+
+  ScanLane<W> s;
+  s.done = f >= a.n_frags;
+  if (!s.done) {
+    const int per = a.cls.paired ? 2 : 1;
+    const uint64_t o0 = a.seq_off[f * per], o1 = a.seq_off[f * per + 1];
+    if (per == 2) {
+      const uint64_t o2 = a.seq_off[f * per + 2];
+      s.seq2 = a.bases + o1;
+      s.qual2 = (QUAL && a.quals) ? a.quals + o1 : nullptr;
+      s.len2 = (uint32_t)(o2 - o1);
+    }
+    s.mate = 0;
+    scanlane_mate(s, a.bases + o0, (QUAL && a.quals) ? a.quals + o0 : nullptr, (uint32_t)(o1 - o0));
+    s.gkind = G_NONE;
+    s.glen = 0;
+    s.ng = 0;
+    s.gbase = o0 - a.seq_off[0] + 2 * f;
+    // a fragment that does not fit the slot capacity goes to the slow path
+    const uint64_t need = (per == 2 ? (uint64_t)(a.seq_off[f * per + 2] - o0) : (uint64_t)(o1 - o0)) + 2;
+    if (s.gbase + need > pa.cap_slots) {
+      unsigned long long at = atomicAdd(a.defer_count, 1ull);
+      if (at < a.defer_cap) a.defer_list[at] = f;
+      else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
+      pa.gcount[f] = 0xFFFFFFFFu;
+      s.done = true;
+    }
+  }
+  while (__any_sync(0xffffffffu, !s.done)) {
+    int nst = 0;
+    if (!s.done) {
+      if (s.ci >= s.nchunks) {
+        if (s.gkind != G_NONE) pa.gstream[s.gbase + s.ng++] = make_group(s.gkind, s.glen);
+        s.gkind = G_NONE;
+        if (a.cls.paired && s.mate == 0) {
+          pa.gstream[s.gbase + s.ng++] = make_group(G_BORDER, 1);
+          s.mate = 1;
+          scanlane_mate(s, s.seq2, QUAL ? s.qual2 : nullptr, s.len2);
+        } else {
+          pa.gcount[f] = s.ng;
+          s.done = true;
+        }
+      } else {
+        const uint4 cur = s.c0;
+        s.c0 = s.c1;
+        s.c1 = load_chunk(s.ap, s.ci + 2, s.nchunks);
+        uint4 qc = make_uint4(0, 0, 0, 0);
+        if (QUAL) {
+          qc = s.q0;
+          s.q0 = s.q1;
+          s.q1 = load_chunk(s.aq, s.ci + 2, s.nchunks);
+        }
+        const int32_t pbase = (int32_t)(16 * s.ci) - (int32_t)s.head;
+#pragma unroll 1
+        for (int wi = 0; wi < 4; wi++) {
+          const uint32_t wd = wi == 0 ? cur.x : (wi == 1 ? cur.y : (wi == 2 ? cur.z : cur.w));
+          const uint32_t lower = wd | 0x20202020u;
+          uint32_t ok = __vcmpeq4(lower, 0x61616161u) | __vcmpeq4(lower, 0x63636363u) |
+                        __vcmpeq4(lower, 0x67676767u) | __vcmpeq4(lower, 0x74747474u);
+          if (QUAL) {
+            const uint32_t qw = wi == 0 ? qc.x : (wi == 1 ? qc.y : (wi == 2 ? qc.z : qc.w));
+            ok &= ~__vcmplts4(qw, c.qthr4);
+            if (c.qall) ok = 0;
+          }
+          const int32_t before = -(pbase + 4 * wi);
+          if (before > 0) ok = before >= 4 ? 0u : (ok & (0xFFFFFFFFu << (8 * before)));
+          const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
+#pragma unroll
+          for (int b = 0; b < 4; b++) {
+            pipe_scan_base<W, RC1>(s, pa, c, pbase + 4 * wi + b, (ok >> (8 * b)) & 1u,
+                                   (codes >> (8 * b)) & 3u, skey, sslot, nst);
+          }
+        }
+        s.ci++;
+      }
+    }
+    // append this chunk's staged keys to the block's record range
+    unsigned incl = (unsigned)nst;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned wbase = 0;
+    if (lane == 31 && total) wbase = atomicAdd(&s_count, total);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    const uint64_t at = rbase + wbase + incl - (unsigned)nst;
+    for (int j = 0; j < nst; j++) {
+      pa.rkey[at + j] = skey[j * kPipeBlock];
+      pa.rslot[at + j] = (uint32_t)(s.gbase - rbase) + sslot[j * kPipeBlock];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) pa.bcount[blockIdx.x] = s_count;
+}
+
+}  // namespace k2g
+
+namespace k2g {
+
+// Probe: every record of a scan block, several table loads in flight per
+// thread, result stored at the record's group slot.
+__global__ void __launch_bounds__(kPipeBlock)
+pipe_probe_kernel(PipeArgs pa) {
+  constexpr int B = 4;
+  const uint64_t f0 = (uint64_t)blockIdx.x * kPipeBlock;
+  const uint64_t rbase = pipe_gbase(pa, f0);
+  const uint32_t cnt = pa.bcount[blockIdx.x];
+  const TableView &t = pa.a.table;
+  for (uint32_t i0 = threadIdx.x; i0 < cnt; i0 += B * kPipeBlock) {
+    uint64_t hc[B], idx[B];
+    Sector sec[B];
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+      const uint32_t i = i0 + b * kPipeBlock;
+      if (i < cnt) {
+        hc[b] = murmur3(pa.rkey[rbase + i]);
+        idx[b] = fast_mod(hc[b], t.div);
+        sec[b] = load_sector(t.cells, idx[b] & ~7ull);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+      const uint32_t i = i0 + b * kPipeBlock;
+      if (i < cnt) pa.gtax[rbase + pa.rslot[rbase + i]] = probe_sectors(t, hc[b], idx[b], sec[b]);
+    }
+  }
+}
+
+// Taxon map of one resolve thread in shared memory, interleaved by thread.
+struct ResolveMap {
+  static constexpr int kMapResolve = 16;
+  uint32_t *mkey, *mcnt;
+  int tid;
+  __device__ __forceinline__ uint32_t &map_key(int s) { return mkey[s * kPipeBlock + tid]; }
+  __device__ __forceinline__ uint32_t &map_cnt(int s) { return mcnt[s * kPipeBlock + tid]; }
+  __host__ __device__ static constexpr int map_cap() { return kMapResolve; }
+};
+
+struct ResolveLane {
+  uint64_t frag;
+  uint32_t cur_taxon;
+  uint32_t run_code, run_cnt, n_runs;
+  uint32_t hit_groups;
+  uint32_t total_tokens;
+  uint32_t distinct;
+  bool quick_stop;
+  uint64_t run_base;
+};
+
+// Resolve: replay the token groups with their taxa (src/classify.cc:847-888),
+// then ResolveTree and the outputs (finish_fragment).  A fragment whose
+// taxon map overflows is handed to the slow path.
+__global__ void __launch_bounds__(kPipeBlock)
+pipe_resolve_kernel(PipeArgs pa) {
+  __shared__ uint32_t s_mkey[ResolveMap::kMapResolve * kPipeBlock];
+  __shared__ uint32_t s_mcnt[ResolveMap::kMapResolve * kPipeBlock];
+  const ClassifyArgs &a = pa.a;
+  const uint64_t f = (uint64_t)blockIdx.x * kPipeBlock + threadIdx.x;
+  if (f >= a.n_frags) return;
+  ResolveMap st{s_mkey, s_mcnt, (int)threadIdx.x};
+  for (int i = 0; i < ResolveMap::kMapResolve; i++) st.map_key(i) = 0;
+  ResolveLane s;
+  s.frag = f;
+  s.cur_taxon = 0;
+  s.run_code = s.run_cnt = s.n_runs = 0;
+  s.hit_groups = 0;
+  s.total_tokens = 0;
+  s.distinct = 0;
+  s.quick_stop = false;
+  const int per = a.cls.paired ? 2 : 1;
+  s.run_base = a.seq_off[f * per] + 2 * (f + a.frag_off);
+  const uint64_t gb = pipe_gbase(pa, f);
+  const uint32_t ng = pa.gcount[f];
+  if (ng == 0xFFFFFFFFu) return;   // deferred by the scan
+  for (uint32_t g = 0; g < ng; g++) {
+    const uint32_t grp = pa.gstream[gb + g];
+    const uint32_t kind = grp >> kGroupLenBits, len = grp & kGroupMaxLen;
+    uint32_t taxon;
+    if (kind == G_AMBIG) {
+      emit_run(s, a, K2G_CODE_AMBIGUOUS, len);
+      s.total_tokens += len;
+      continue;
+    }
+    if (kind == G_BORDER) {
+      emit_run(s, a, K2G_CODE_MATE_BORDER, 1);
+      s.total_tokens += 1;
+      continue;
+    }
+    if (kind == G_KEY) {
+      taxon = pa.gtax[gb + g];
+      s.cur_taxon = taxon;
+      if (taxon) {
+        s.hit_groups++;
+        if (a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
+          s.quick_stop = true;
+          break;
+        }
+      }
+    } else if (kind == G_SKIP) {
+      taxon = 0;
+      s.cur_taxon = 0;
+    } else {
+      taxon = s.cur_taxon;
+    }
+    if (taxon && !map_add(st, s.distinct, taxon, len)) {
+      unsigned long long at = atomicAdd(a.defer_count, 1ull);
+      if (at < a.defer_cap) a.defer_list[at] = f;
+      else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
+      return;
+    }
+    emit_run(s, a, taxon, len);
+    s.total_tokens += len;
+  }
+  finish_fragment(s, st, a);
+}
+
+}  // namespace k2g
+
+namespace k2g {
+
+template <int W, bool QUAL, bool RC1>
+cudaError_t launch_pipe_scan(const PipeArgs &pa, cudaStream_t st) {
+  const unsigned blocks = (unsigned)((pa.a.n_frags + kPipeBlock - 1) / kPipeBlock);
+  pipe_scan_kernel<W, QUAL, RC1><<<blocks, kPipeBlock, 0, st>>>(pa);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pipe_probe(const PipeArgs &pa, cudaStream_t st);
+cudaError_t launch_pipe_resolve(const PipeArgs &pa, cudaStream_t st);
+
+}  // namespace k2g

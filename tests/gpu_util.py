@@ -63,7 +63,7 @@ class DeviceResult:
         return out
 
 
-def classify_batch(db: k2g.Database, b: Batch, params: dict, mode=k2g.MODE_PERSISTENT,
+def classify_batch(db: k2g.Database, b: Batch, params: dict, mode=k2g.MODE_PIPELINED,
                    node_count: int | None = None) -> DeviceResult:
     t = torch()
     d_bases = bytes_dev(b.bases)
@@ -79,8 +79,12 @@ def classify_batch(db: k2g.Database, b: Batch, params: dict, mode=k2g.MODE_PERSI
     nc = node_count or db.info().node_count
     tr = zeros(nc, t.int64)
     status = zeros(1, t.int32)
-    reads = k2g.Reads(d_bases.data_ptr(), d_quals.data_ptr() if d_quals is not None else None,
-                      d_off.data_ptr(), n, int(np.max(np.diff(b.seq_off))) if n else 0, None, 0)
+    reads = k2g.Reads(d_bases=d_bases.data_ptr(),
+                      d_quals=d_quals.data_ptr() if d_quals is not None else None,
+                      d_seq_off=d_off.data_ptr(), n_frags=n,
+                      max_seq_len=int(np.max(np.diff(b.seq_off))) if n else 0,
+                      total_bases=int(b.seq_off[-1] - b.seq_off[0]), d_frag_block=None,
+                      frag_base=0)
     res = k2g.Results(call.data_ptr(), hg.data_ptr(), hoff.data_ptr(), hlen.data_ptr(),
                       runs.data_ptr(), runs_cap, tr.data_ptr(), None, None, None, 0, None,
                       status.data_ptr())

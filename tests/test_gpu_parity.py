@@ -101,7 +101,8 @@ def test_scan_golden_vectors():
 RUNS = sorted(manifest()["runs"].items())
 
 
-@pytest.mark.parametrize("mode", [k2g.MODE_PERSISTENT, k2g.MODE_PLAIN], ids=["persistent", "plain"])
+@pytest.mark.parametrize("mode", [k2g.MODE_PIPELINED, k2g.MODE_PERSISTENT, k2g.MODE_PLAIN],
+                         ids=["pipelined", "persistent", "plain"])
 @pytest.mark.parametrize("tag,run", RUNS, ids=[t for t, _ in RUNS])
 def test_classify_golden(tag, run, mode):
     params, flags = parse_args(run["args"])
