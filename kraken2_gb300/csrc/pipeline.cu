@@ -1,4 +1,5 @@
 // Probe and resolve stage launchers of the pipelined classification.
+#define K2G_PIPELINE_STAGE_KERNELS
 #include "classify_kernels.cuh"
 #include "pipeline.cuh"
 

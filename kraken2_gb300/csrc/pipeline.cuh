@@ -243,6 +243,7 @@ pipe_scan_kernel(PipeArgs pa) {
 
 namespace k2g {
 
+#ifdef K2G_PIPELINE_STAGE_KERNELS
 // Probe: every record of a scan block, several table loads in flight per
 // thread, result stored at the record's group slot.
 __global__ void __launch_bounds__(kPipeBlock)
@@ -359,6 +360,8 @@ pipe_resolve_kernel(PipeArgs pa) {
   }
   finish_fragment(s, st, a);
 }
+
+#endif  // K2G_PIPELINE_STAGE_KERNELS
 
 }  // namespace k2g
 
