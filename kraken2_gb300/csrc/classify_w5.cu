@@ -6,6 +6,6 @@
 namespace k2g {
 template cudaError_t launch_fast<5, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
 template cudaError_t launch_fast<5, true, true>(const ClassifyArgs &, int, int, cudaStream_t);
-template cudaError_t launch_pipe_scan<5, false, true>(const PipeArgs &, cudaStream_t);
-template cudaError_t launch_pipe_scan<5, true, true>(const PipeArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<5, false, true>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<5, true, true>(const StepArgs &, cudaStream_t);
 }  // namespace k2g

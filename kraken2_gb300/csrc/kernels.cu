@@ -26,16 +26,16 @@ extern template cudaError_t launch_slow<false, true>(const ClassifyArgs &, int, 
 extern template cudaError_t launch_slow<true, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 extern template cudaError_t launch_slow<false, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 extern template cudaError_t launch_slow<true, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<5, false, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<5, true, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<1, false, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<1, true, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<7, false, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<7, true, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<0, false, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<0, true, true>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<0, false, false>(const PipeArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_scan<0, true, false>(const PipeArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<5, false, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<5, true, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<1, false, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<1, true, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<7, false, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<7, true, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, false, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, true, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, false, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, true, false>(const StepArgs &, cudaStream_t);
 }  // namespace k2g
 
 namespace k2g {
@@ -220,13 +220,12 @@ static void launch_scan(const ScanView &sv, const uint8_t *bases, const uint64_t
   scan_kernel<W><<<(unsigned)blocks, 128, 0, st>>>(sv, bases, off, n, mins, amb);
 }
 
-// Each classification sub-batch runs on one of two internal execution
-// contexts: a stream plus every piece of device scratch the kernels of one
-// sub-batch use (work counter, deferred-fragment list, slow-path scratch,
-// pipeline buffers).  Consecutive sub-batches alternate contexts, so the
-// stages of one overlap those of the other, and scratch is never shared by
-// work that can run concurrently.  The caller's stream is joined through
-// events, so calls stay asynchronous and capturable.
+// Classification runs on one internal stream per device, joined to the
+// caller's stream through events (calls stay asynchronous and capturable,
+// and concurrent callers never share scratch in flight).  Each sub-batch in
+// flight owns an execution context: every piece of device scratch its
+// kernels use (work counter, deferred-fragment list, slow-path scratch,
+// pipeline buffers).  The pipelined mode keeps three sub-batches in flight.
 struct ExecCtx {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
@@ -248,9 +247,9 @@ struct ExecCtx {
 struct DeviceState {
   std::mutex mu;
   bool init = false;
-  cudaEvent_t start = nullptr;
-  ExecCtx ctx[2];
-  int next = 0;           // context of the next sub-batch (round robin across calls)
+  cudaStream_t st = nullptr;      // all classification work of the device
+  cudaEvent_t start = nullptr, done = nullptr;
+  ExecCtx ctx[3];
 };
 static DeviceState g_state[64];
 
@@ -267,11 +266,7 @@ static cudaError_t grow(T *&p, uint64_t &cap, uint64_t want) {
 
 static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t slow_bytes,
                               bool pipeline) {
-  if (!c.st) {
-    K2G_CUDA_TRY(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
-    K2G_CUDA_TRY(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
-    K2G_CUDA_TRY(cudaMalloc(&c.counters, 2 * sizeof(unsigned long long)));
-  }
+  if (!c.counters) K2G_CUDA_TRY(cudaMalloc(&c.counters, 2 * sizeof(unsigned long long)));
   K2G_CUDA_TRY(grow(c.defer_list, c.defer_cap, std::max<uint64_t>(1024, frags)));
   if (c.slow_bytes < slow_bytes) {
     if (c.slow) cudaFree(c.slow);
@@ -280,7 +275,7 @@ static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t
     K2G_CUDA_TRY(cudaMalloc(&c.slow, slow_bytes));
     c.slow_bytes = slow_bytes;
   }
-  if (pipeline) {
+  if (pipeline && c.cap_slots < slots) {
     uint64_t cs = c.cap_slots;
     K2G_CUDA_TRY(grow(c.gstream, cs, slots));
     cs = c.cap_slots;
@@ -289,13 +284,14 @@ static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t
     K2G_CUDA_TRY(grow(c.rkey, cs, slots));
     cs = c.cap_slots;
     K2G_CUDA_TRY(grow(c.rslot, cs, slots));
-    c.cap_slots = std::max(c.cap_slots, slots);
+    c.cap_slots = slots;
+  }
+  if (pipeline && c.cap_frags < frags) {
     uint64_t cf = c.cap_frags;
     K2G_CUDA_TRY(grow(c.gcount, cf, frags));
     cf = c.cap_frags;
-    uint64_t blocks = (frags + kPipeBlock - 1) / kPipeBlock;
-    K2G_CUDA_TRY(grow(c.bcount, cf, std::max(frags, blocks)));
-    c.cap_frags = std::max(c.cap_frags, frags);
+    K2G_CUDA_TRY(grow(c.bcount, cf, frags));
+    c.cap_frags = frags;
   }
   return K2G_OK;
 }
@@ -317,16 +313,16 @@ static cudaError_t dispatch_fast(const ClassifyArgs &a, int persistent, int sms,
   }
 }
 
-static cudaError_t dispatch_pipe_scan(const PipeArgs &p, cudaStream_t st) {
-  const ClassifyArgs &a = p.a;
+static cudaError_t dispatch_pipe_step(const StepArgs &sa, cudaStream_t st) {
+  const ClassifyArgs &a = sa.scan.a;
   const bool q = a.quals != nullptr && a.cls.min_quality > 0;
   if (a.scan.revcom_version == 0)
-    return q ? launch_pipe_scan<0, true, false>(p, st) : launch_pipe_scan<0, false, false>(p, st);
+    return q ? launch_pipe_step<0, true, false>(sa, st) : launch_pipe_step<0, false, false>(sa, st);
   switch (a.scan.w) {
-    case 5: return q ? launch_pipe_scan<5, true, true>(p, st) : launch_pipe_scan<5, false, true>(p, st);
-    case 1: return q ? launch_pipe_scan<1, true, true>(p, st) : launch_pipe_scan<1, false, true>(p, st);
-    case 7: return q ? launch_pipe_scan<7, true, true>(p, st) : launch_pipe_scan<7, false, true>(p, st);
-    default: return q ? launch_pipe_scan<0, true, true>(p, st) : launch_pipe_scan<0, false, true>(p, st);
+    case 5: return q ? launch_pipe_step<5, true, true>(sa, st) : launch_pipe_step<5, false, true>(sa, st);
+    case 1: return q ? launch_pipe_step<1, true, true>(sa, st) : launch_pipe_step<1, false, true>(sa, st);
+    case 7: return q ? launch_pipe_step<7, true, true>(sa, st) : launch_pipe_step<7, false, true>(sa, st);
+    default: return q ? launch_pipe_step<0, true, true>(sa, st) : launch_pipe_step<0, false, true>(sa, st);
   }
 }
 
@@ -366,7 +362,7 @@ static SlowPlan slow_plan(uint64_t max_len, bool paired) {
 // holding total_bases bases.
 static void sub_batch_plan(uint64_t n, uint64_t total_bases, int per, uint64_t max_len,
                            uint64_t &sb_frags, uint64_t &cap_slots) {
-  const uint64_t target_bases = 256ull << 20;
+  const uint64_t target_bases = 64ull << 20;
   const double avg = n ? (double)total_bases / (double)n : 1.0;   // bases per fragment
   sb_frags = (uint64_t)std::max(1.0, target_bases / std::max(avg, 1.0));
   sb_frags = std::min<uint64_t>(sb_frags, 2ull << 20);
@@ -378,70 +374,109 @@ static void sub_batch_plan(uint64_t n, uint64_t total_bases, int per, uint64_t m
               (uint64_t)kPipeBlock * (per * max_len + 2) + 64;
 }
 
+// The view of sub-batch [f0, f0 + n) of a batch, bound to context c.
+static ClassifyArgs sub_view(const ClassifyArgs &a0, uint64_t f0, uint64_t n, const ExecCtx &c,
+                             const SlowPlan &sp) {
+  const int per = a0.cls.paired ? 2 : 1;
+  ClassifyArgs a = a0;
+  a.seq_off = a0.seq_off + f0 * per;
+  a.n_frags = n;
+  a.frag_base = a0.frag_base + f0;
+  a.frag_off = a0.frag_off + f0;
+  a.call = a0.call + f0;
+  if (a0.hit_groups) a.hit_groups = a0.hit_groups + f0;
+  if (a0.hitlist_off) a.hitlist_off = a0.hitlist_off + f0;
+  if (a0.hitlist_len) a.hitlist_len = a0.hitlist_len + f0;
+  a.next_frag = c.counters;
+  a.defer_count = c.counters + 1;
+  a.defer_list = c.defer_list;
+  a.defer_cap = c.defer_cap;
+  a.frag_list = c.defer_list;
+  a.scratch = c.slow;
+  a.scratch_stride = sp.stride;
+  return a;
+}
+
+static PipeArgs pipe_view(const ClassifyArgs &a, const ExecCtx &c) {
+  PipeArgs p;
+  p.a = a;
+  p.gstream = c.gstream;
+  p.gtax = c.gtax;
+  p.gcount = c.gcount;
+  p.rkey = c.rkey;
+  p.rslot = c.rslot;
+  p.bcount = c.bcount;
+  p.cap_slots = c.cap_slots;
+  return p;
+}
+
 static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mode,
                                uint64_t max_len, uint64_t total_bases, cudaStream_t caller) {
   const int dev = db->device;
   DeviceState &ds = g_state[dev & 63];
   std::lock_guard<std::mutex> lock(ds.mu);
   if (!ds.init) {
+    K2G_CUDA_TRY(cudaStreamCreateWithFlags(&ds.st, cudaStreamNonBlocking));
     K2G_CUDA_TRY(cudaEventCreateWithFlags(&ds.start, cudaEventDisableTiming));
+    K2G_CUDA_TRY(cudaEventCreateWithFlags(&ds.done, cudaEventDisableTiming));
     ds.init = true;
   }
   const int per = a0.cls.paired ? 2 : 1;
   const bool pipeline = mode == K2G_MODE_PIPELINED;
-  uint64_t sb_frags = a0.n_frags, cap_slots = 0;
-  if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, sb_frags, cap_slots);
+  uint64_t sb = a0.n_frags, cap_slots = 0;
+  if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, sb, cap_slots);
   const SlowPlan sp = slow_plan(max_len, a0.cls.paired != 0);
-  for (auto &c : ds.ctx) {
-    k2g_status s = ctx_reserve(c, sb_frags, cap_slots, sp.bytes, pipeline);
+  const int nctx = pipeline ? 3 : 1;
+  for (int i = 0; i < nctx; i++) {
+    k2g_status s = ctx_reserve(ds.ctx[i], sb, cap_slots, sp.bytes, pipeline);
     if (s != K2G_OK) return s;
   }
+  cudaStream_t st = ds.st;
   K2G_CUDA_TRY(cudaEventRecord(ds.start, caller));
-  for (auto &c : ds.ctx) K2G_CUDA_TRY(cudaStreamWaitEvent(c.st, ds.start, 0));
-  int &k = ds.next;
-  for (uint64_t f0 = 0; f0 < a0.n_frags; f0 += sb_frags, k ^= 1) {
-    ExecCtx &c = ds.ctx[k];
-    const uint64_t n = std::min(sb_frags, a0.n_frags - f0);
-    ClassifyArgs a = a0;
-    a.seq_off = a0.seq_off + f0 * per;
-    a.n_frags = n;
-    a.frag_base = a0.frag_base + f0;
-    a.frag_off = a0.frag_off + f0;
-    a.call = a0.call + f0;
-    if (a0.hit_groups) a.hit_groups = a0.hit_groups + f0;
-    if (a0.hitlist_off) a.hitlist_off = a0.hitlist_off + f0;
-    if (a0.hitlist_len) a.hitlist_len = a0.hitlist_len + f0;
-    a.next_frag = c.counters;
-    a.defer_count = c.counters + 1;
-    a.defer_list = c.defer_list;
-    a.defer_cap = c.defer_cap;
-    a.frag_list = nullptr;
-    a.scratch = c.slow;
-    a.scratch_stride = sp.stride;
-    K2G_CUDA_TRY(cudaMemsetAsync(c.counters, 0, 2 * sizeof(unsigned long long), c.st));
-    if (pipeline) {
-      PipeArgs p;
-      p.a = a;
-      p.gstream = c.gstream;
-      p.gtax = c.gtax;
-      p.gcount = c.gcount;
-      p.rkey = c.rkey;
-      p.rslot = c.rslot;
-      p.bcount = c.bcount;
-      p.cap_slots = c.cap_slots;
-      K2G_CUDA_TRY(dispatch_pipe_scan(p, c.st));
-      K2G_CUDA_TRY(launch_pipe_probe(p, c.st));
-      K2G_CUDA_TRY(launch_pipe_resolve(p, c.st));
-    } else {
-      K2G_CUDA_TRY(dispatch_fast(a, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), c.st));
+  K2G_CUDA_TRY(cudaStreamWaitEvent(st, ds.start, 0));
+  const uint64_t S = (a0.n_frags + sb - 1) / sb;
+  auto slow = [&](uint64_t i) -> cudaError_t {
+    const ExecCtx &c = ds.ctx[pipeline ? i % 3 : 0];
+    const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+    return dispatch_slow(sub_view(a0, f0, n, c, sp), sp.mcap, (unsigned)(sp.threads / 128), 128, st);
+  };
+  if (pipeline) {
+    // beat t: scan t, probe t-1, resolve t-2
+    for (uint64_t t = 0; t < S + 2; t++) {
+      StepArgs sa{};
+      PipeArgs none{};
+      none.a = a0;
+      none.a.n_frags = 0;
+      sa.scan = sa.probe = sa.resolve = none;
+      auto bind = [&](uint64_t i, PipeArgs &p, uint32_t &nb) {
+        const ExecCtx &c = ds.ctx[i % 3];
+        const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+        p = pipe_view(sub_view(a0, f0, n, c, sp), c);
+        nb = (uint32_t)((n + kPipeBlock - 1) / kPipeBlock);
+      };
+      if (t < S) {
+        K2G_CUDA_TRY(cudaMemsetAsync(ds.ctx[t % 3].counters, 0, 2 * sizeof(unsigned long long), st));
+        bind(t, sa.scan, sa.n_scan);
+      }
+      if (t >= 1 && t - 1 < S) bind(t - 1, sa.probe, sa.n_probe);
+      if (t >= 2 && t - 2 < S) bind(t - 2, sa.resolve, sa.n_resolve);
+      if (!sa.n_scan) sa.scan = sa.probe.a.n_frags ? sa.probe : sa.resolve;   // scan config for dispatch
+      if (!sa.n_scan) sa.scan.a.n_frags = 0;
+      K2G_CUDA_TRY(dispatch_pipe_step(sa, st));
+      if (t >= 2 && t - 2 < S) K2G_CUDA_TRY(slow(t - 2));
     }
-    a.frag_list = c.defer_list;
-    K2G_CUDA_TRY(dispatch_slow(a, sp.mcap, (unsigned)(sp.threads / 128), 128, c.st));
+  } else {
+    for (uint64_t i = 0; i < S; i++) {
+      const ExecCtx &c = ds.ctx[0];
+      const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+      K2G_CUDA_TRY(cudaMemsetAsync(c.counters, 0, 2 * sizeof(unsigned long long), st));
+      K2G_CUDA_TRY(dispatch_fast(sub_view(a0, f0, n, c, sp), mode == K2G_MODE_PERSISTENT ? 1 : 0,
+                                 sm_count(dev), st));
+      K2G_CUDA_TRY(slow(i));
+    }
   }
-  for (auto &c : ds.ctx) {
-    K2G_CUDA_TRY(cudaEventRecord(c.done, c.st));
-    K2G_CUDA_TRY(cudaStreamWaitEvent(caller, c.done, 0));
-  }
+  K2G_CUDA_TRY(cudaEventRecord(ds.done, st));
+  K2G_CUDA_TRY(cudaStreamWaitEvent(caller, ds.done, 0));
   return K2G_OK;
 }
 

@@ -126,14 +126,15 @@ __device__ __forceinline__ void pipe_scan_base(ScanLane<W> &s, const PipeArgs &p
   nst += is_key ? 1 : 0;
 }
 
+constexpr size_t kScanSmem = (size_t)kStage * kPipeBlock * 12 + 16;
+
 template <int W, bool QUAL, bool RC1>
-__global__ void __launch_bounds__(kPipeBlock)
-pipe_scan_kernel(PipeArgs pa) {
-  __shared__ uint64_t s_key[kStage * kPipeBlock];
-  __shared__ uint32_t s_slot[kStage * kPipeBlock];
-  __shared__ uint32_t s_count;
+__device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk, unsigned char *smem) {
+  uint64_t *s_key = reinterpret_cast<uint64_t *>(smem);
+  uint32_t *s_slot = reinterpret_cast<uint32_t *>(smem + (size_t)kStage * kPipeBlock * 8);
+  uint32_t &s_count = *reinterpret_cast<uint32_t *>(smem + (size_t)kStage * kPipeBlock * 12);
   const ClassifyArgs &a = pa.a;
-  const uint64_t f0 = (uint64_t)blockIdx.x * kPipeBlock;
+  const uint64_t f0 = (uint64_t)blk * kPipeBlock;
   const uint64_t f = f0 + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) s_count = 0;
@@ -236,22 +237,20 @@ pipe_scan_kernel(PipeArgs pa) {
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) pa.bcount[blockIdx.x] = s_count;
+  if (threadIdx.x == 0) pa.bcount[blk] = s_count;
 }
 
 }  // namespace k2g
 
 namespace k2g {
 
-#ifdef K2G_PIPELINE_STAGE_KERNELS
 // Probe: every record of a scan block, several table loads in flight per
 // thread, result stored at the record's group slot.
-__global__ void __launch_bounds__(kPipeBlock)
-pipe_probe_kernel(PipeArgs pa) {
+__device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk) {
   constexpr int B = 4;
-  const uint64_t f0 = (uint64_t)blockIdx.x * kPipeBlock;
+  const uint64_t f0 = (uint64_t)blk * kPipeBlock;
   const uint64_t rbase = pipe_gbase(pa, f0);
-  const uint32_t cnt = pa.bcount[blockIdx.x];
+  const uint32_t cnt = pa.bcount[blk];
   const TableView &t = pa.a.table;
   for (uint32_t i0 = threadIdx.x; i0 < cnt; i0 += B * kPipeBlock) {
     uint64_t hc[B], idx[B];
@@ -297,12 +296,12 @@ struct ResolveLane {
 // Resolve: replay the token groups with their taxa (src/classify.cc:847-888),
 // then ResolveTree and the outputs (finish_fragment).  A fragment whose
 // taxon map overflows is handed to the slow path.
-__global__ void __launch_bounds__(kPipeBlock)
-pipe_resolve_kernel(PipeArgs pa) {
-  __shared__ uint32_t s_mkey[ResolveMap::kMapResolve * kPipeBlock];
-  __shared__ uint32_t s_mcnt[ResolveMap::kMapResolve * kPipeBlock];
+__device__ __forceinline__ void pipe_resolve_body(const PipeArgs &pa, uint32_t blk,
+                                                  unsigned char *smem) {
+  uint32_t *s_mkey = reinterpret_cast<uint32_t *>(smem);
+  uint32_t *s_mcnt = s_mkey + ResolveMap::kMapResolve * kPipeBlock;
   const ClassifyArgs &a = pa.a;
-  const uint64_t f = (uint64_t)blockIdx.x * kPipeBlock + threadIdx.x;
+  const uint64_t f = (uint64_t)blk * kPipeBlock + threadIdx.x;
   if (f >= a.n_frags) return;
   ResolveMap st{s_mkey, s_mcnt, (int)threadIdx.x};
   for (int i = 0; i < ResolveMap::kMapResolve; i++) st.map_key(i) = 0;
@@ -361,20 +360,42 @@ pipe_resolve_kernel(PipeArgs pa) {
   finish_fragment(s, st, a);
 }
 
-#endif  // K2G_PIPELINE_STAGE_KERNELS
 
 }  // namespace k2g
 
 namespace k2g {
 
+// One beat of the pipeline: the blocks of one launch are interleaved by
+// role -- scan of sub-batch t, probe of t-1, resolve of t-2 -- so every SM
+// runs memory-bound probe blocks next to compute-bound scan and resolve
+// blocks.  Stages of the same sub-batch are ordered by the launches.
+struct StepArgs {
+  PipeArgs scan, probe, resolve;
+  uint32_t n_scan, n_probe, n_resolve;   // blocks per role
+};
+
 template <int W, bool QUAL, bool RC1>
-cudaError_t launch_pipe_scan(const PipeArgs &pa, cudaStream_t st) {
-  const unsigned blocks = (unsigned)((pa.a.n_frags + kPipeBlock - 1) / kPipeBlock);
-  pipe_scan_kernel<W, QUAL, RC1><<<blocks, kPipeBlock, 0, st>>>(pa);
-  return cudaGetLastError();
+__global__ void __launch_bounds__(kPipeBlock, 6)
+pipe_step_kernel(StepArgs sa) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t role = blockIdx.x % 3, blk = blockIdx.x / 3;
+  if (role == 0) {
+    if (blk < sa.n_scan) pipe_scan_body<W, QUAL, RC1>(sa.scan, blk, smem);
+  } else if (role == 1) {
+    if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk);
+  } else {
+    if (blk < sa.n_resolve) pipe_resolve_body(sa.resolve, blk, smem);
+  }
 }
 
-cudaError_t launch_pipe_probe(const PipeArgs &pa, cudaStream_t st);
-cudaError_t launch_pipe_resolve(const PipeArgs &pa, cudaStream_t st);
+template <int W, bool QUAL, bool RC1>
+cudaError_t launch_pipe_step(const StepArgs &sa, cudaStream_t st) {
+  const uint32_t most = max(sa.n_scan, max(sa.n_probe, sa.n_resolve));
+  if (!most) return cudaSuccess;
+  const size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
+                          ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
+  pipe_step_kernel<W, QUAL, RC1><<<3 * most, kPipeBlock, smem, st>>>(sa);
+  return cudaGetLastError();
+}
 
 }  // namespace k2g
