@@ -300,7 +300,6 @@ class DeviceRunner:
         wl.db.classify(reads, self.params, res, mode=self.mode, stream=wl.stream.cuda_stream)
         if events is not None:
             events[1].record(wl.stream)
-        self.launches += 2   # classify kernel + slow-path kernel
 
     def step(self, timed_calls=None):
         for b0, n in self.batches():
@@ -449,6 +448,39 @@ def barrier(pg):
     torch.cuda.synchronize()
 
 
+def random_sector_rate(wl, n_loads: int = 1 << 31) -> float:
+    """Random 32-byte loads/s over the resident table (k2g_sector_gather):
+    the ceiling for a lookup stream, measured on the same memory."""
+    torch = wl.torch
+    sink = torch.zeros(1, dtype=torch.int32, device=wl.dev)
+    st = wl.stream.cuda_stream
+    wl.db.sector_gather(n_loads // 8, sink.data_ptr(), st)
+    threads = torch.cuda.get_device_properties(wl.dev).multi_processor_count * 16 * 256
+    per = -(-(-(-n_loads // threads)) // 4) * 4      # the kernel's rounding
+    issued = per * threads
+    best = 0.0
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(wl.stream)
+        wl.db.sector_gather(n_loads, sink.data_ptr(), st)
+        b.record(wl.stream)
+        b.synchronize()
+        best = max(best, issued / (a.elapsed_time(b) / 1e3))
+    return best
+
+
+def profiled_dram_bytes_per_read() -> float | None:
+    """DRAM bytes per read of the classification step kernel, from the
+    committed ncu summary (a 'dram_bytes_per_read = X' line)."""
+    path = os.path.join(ROOT, "profiles", "pipe_step_kernel_150bp.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_read ="):
+            return float(line.split("=")[1].split()[0])
+    return None
+
+
 def run_ours(args, log):
     import torch
     rank, world, local, pg = dist_setup(args.gpus)
@@ -469,14 +501,14 @@ def run_ours(args, log):
     barrier(pg)
     calls = []
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    runner.launches = 0
+    launches0 = wl.k2g.kernel_launches()
     with Clocks(local) as clk:
         start.record(wl.stream)
         for s in range(args.steps):
             runner.step(calls if s == args.steps - 1 else None)
         end.record(wl.stream)
         torch.cuda.synchronize()
-    launches = runner.launches
+    launches = wl.k2g.kernel_launches() - launches0
     ms_total = max_over_ranks(pg, start.elapsed_time(end))
     ms_step = ms_total / args.steps
     if int(runner.status.cpu()[0]):
@@ -520,15 +552,14 @@ def run_ours(args, log):
 
     # roofline of the dominant kernel (the classify launch of each batch)
     peak, peak_kind = hbm_peak()
+    rs_loads_s = random_sector_rate(wl)
     kern_reads = sum(n for n, _ in call_ms)
     kern_ms = sum(ms for _, ms in call_ms)
     achieved = bytes_per_read * kern_reads / (kern_ms / 1e3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "classify_traffic.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            tj = json.load(f)
-        traffic = tj.get("bytes_per_read", 0) * (kern_reads / max(len(call_ms), 1)) or None
+    dram_per_read = profiled_dram_bytes_per_read()
+    if dram_per_read:
+        traffic = round(dram_per_read * kern_reads / max(len(call_ms), 1))
 
     # CPU baseline: the oracle restatement with every host thread
     threads = os.cpu_count() or 1
@@ -582,6 +613,10 @@ def run_ours(args, log):
                      "sectors_per_read": round(sectors_per_read, 3),
                      "lookups_per_read": round(lookups_per_read, 3),
                      "hit_fraction_of_lookups": round(float(hit.mean()), 4),
+                     "random_sector_gbs": round(rs_loads_s * 32 / 1e9, 1),
+                     "frac_of_random_sector": round(achieved / (rs_loads_s * 32 / 1e9), 4),
+                     "sectors_per_s": round(sectors_per_read * kern_reads / (kern_ms / 1e3) / 1e9, 3),
+                     "random_sectors_per_s": round(rs_loads_s / 1e9, 3),
                      "kernel_ms_per_launch": round(kern_ms / max(len(call_ms), 1), 3),
                      "reads_per_launch": int(kern_reads / max(len(call_ms), 1))},
         "cpu_baseline": {"value": round(rate * 60 / 1e6, 3), "unit": "Mreads/min",

@@ -184,6 +184,18 @@ k2g_status k2g_classify_host(const k2g_db *db, const char *bases, const char *qu
 k2g_status k2g_host_alloc(void **ptr, size_t bytes);
 k2g_status k2g_host_free(void *ptr);
 
+/* ---- diagnostics (no counterpart in the reference) */
+
+/* Issues at least n_loads random 32-byte loads spread uniformly over the
+ * table's cells (each thread rounds its share up to a multiple of 4) and
+ * writes nothing unless a data-dependent sentinel matches (d_sink: 4 device
+ * bytes).  Timing it on `stream` gives the random-sector rate that bounds
+ * k2g_lookup / k2g_classify on this table. */
+k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint32_t *d_sink, void *stream);
+
+/* Number of kernels this library has launched in this process so far. */
+uint64_t k2g_kernel_launches(void);
+
 /* ---- build: CompareAndSet with LCA merge (src/compact_hash.h:417-462,
  * src/build_db.h:187-194, :217-326) */
 

@@ -33,7 +33,8 @@ CODE_AMBIGUOUS = 0xFFFFFFFD
 EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g_db_close",
            "k2g_db_info_get", "k2g_db_write_hash", "k2g_db_download", "k2g_lookup",
            "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
-           "k2g_host_alloc", "k2g_host_free", "k2g_build_insert"]
+           "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_sector_gather",
+           "k2g_kernel_launches"]
 
 
 class K2GError(RuntimeError):
@@ -88,6 +89,8 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.k2g_last_error.restype = C.c_char_p
         L.k2g_version.restype = C.c_char_p
+        L.k2g_kernel_launches.restype = C.c_uint64
+        L.k2g_kernel_launches.argtypes = []
         vp, u64, i32 = C.c_void_p, C.c_uint64, C.c_int
         sig = {
             "k2g_db_open": [C.c_char_p, C.c_char_p, C.c_char_p, i32, C.POINTER(vp)],
@@ -107,6 +110,7 @@ def lib():
             "k2g_host_alloc": [C.POINTER(vp), C.c_size_t],
             "k2g_host_free": [vp],
             "k2g_build_insert": [vp, vp, vp, u64, i32, vp],
+            "k2g_sector_gather": [vp, u64, vp, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -123,6 +127,11 @@ def check(status: int):
 
 def version() -> str:
     return lib().k2g_version().decode()
+
+
+def kernel_launches() -> int:
+    """Kernels launched by libk2g in this process so far."""
+    return int(lib().k2g_kernel_launches())
 
 
 class Database:
@@ -185,6 +194,10 @@ class Database:
         vals = np.zeros(len(keys), np.uint32)
         check(lib().k2g_lookup_host(self.h, keys.ctypes.data, vals.ctypes.data, len(keys)))
         return vals
+
+    def sector_gather(self, n_loads: int, d_sink: int, stream: int = 0):
+        """Random 32-byte loads over the table (random-access ceiling probe)."""
+        check(lib().k2g_sector_gather(self.h, n_loads, d_sink, stream))
 
     def scan(self, d_bases: int, d_seq_off: int, n_seqs: int, d_mins: int, d_ambig: int,
              stream: int = 0):

@@ -149,6 +149,7 @@ cudaError_t launch_fast(const ClassifyArgs &a, int persistent, int sms, cudaStre
   }
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, (unsigned)per_block, smem, st>>>(a, persistent);
+  note_launches();
   return cudaGetLastError();
 }
 
@@ -156,6 +157,7 @@ template <bool QUAL, bool RC1>
 cudaError_t launch_slow(const ClassifyArgs &a, int mcap, unsigned blocks, unsigned threads,
                         cudaStream_t st) {
   classify_slow_kernel<QUAL, RC1><<<blocks, threads, 0, st>>>(a, mcap);
+  note_launches();
   return cudaGetLastError();
 }
 

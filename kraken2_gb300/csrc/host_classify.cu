@@ -90,6 +90,7 @@ k2g_status compact_runs(const uint64_t *d_sparse, const uint64_t *d_seq_off, int
   uint64_t nb = (n + kScanBlock - 1) / kScanBlock;
   scan_blocks_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(d_len, d_excl, d_sums, n);
   scan_sums_kernel<<<1, kScanBlock, 0, st>>>(d_sums, nb, d_total);
+  note_launches(3);
   gather_runs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_sparse, d_seq_off, per, d_len,
                                                                  d_excl, d_sums, n, d_dense);
   K2G_CUDA_TRY(cudaGetLastError());
@@ -235,6 +236,7 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
     if (quals) SLOT_TRY(cudaMemcpyAsync(s.quals, quals + b0, nb, cudaMemcpyHostToDevice, s.st));
     SLOT_TRY(cudaMemcpyAsync(s.off, seq_off + f0 * per, (nf * per + 1) * 8,
                              cudaMemcpyHostToDevice, s.st));
+    note_launches();
     rebase_kernel<<<(unsigned)((nf * per + 1 + 255) / 256), 256, 0, s.st>>>(s.off, nf * per + 1, b0);
     SLOT_TRY(cudaMemsetAsync(s.status, 0, 4, s.st));
     k2g_reads rd{};

@@ -82,6 +82,8 @@ namespace k2g {
 // Thread-local error message plumbing.
 k2g_status fail(k2g_status s, const std::string &msg);
 k2g_status cuda_fail(int err, const char *what);
+// Counts each kernel launch issued by the library (k2g_kernel_launches).
+void note_launches(uint64_t n = 1);
 }  // namespace k2g
 
 #define K2G_CUDA_TRY(call)                                        \

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -60,6 +61,7 @@ k2g_status max_table_value(const k2g_db *db, uint32_t *out) {
   K2G_CUDA_TRY(cudaMemset(d, 0, 4));
   max_value_kernel<<<1216, 256>>>(db->d_cells, db->capacity,
                                   (uint32_t)((1ull << db->value_bits) - 1), d);
+  note_launches();
   cudaError_t e = cudaMemcpy(out, d, 4, cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_fail(e, "max_value_kernel");
@@ -204,6 +206,9 @@ __global__ void insert_kernel(TableView t, uint32_t *cells, const uint32_t *pare
 // Launch helpers
 // ---------------------------------------------------------------------------
 
+static std::atomic<uint64_t> g_launches{0};
+void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 static int sm_count(int device) {
   static int cached[64] = {0};
   if (device < 64 && cached[device]) return cached[device];
@@ -218,6 +223,7 @@ static void launch_scan(const ScanView &sv, const uint8_t *bases, const uint64_t
                         uint64_t n, uint64_t *mins, uint8_t *amb, cudaStream_t st) {
   uint64_t blocks = (n + 127) / 128;
   scan_kernel<W><<<(unsigned)blocks, 128, 0, st>>>(sv, bases, off, n, mins, amb);
+  note_launches();
 }
 
 // Classification runs on one internal stream per device, joined to the
@@ -493,8 +499,34 @@ extern "C" k2g_status k2g_lookup(const k2g_db *db, const uint64_t *d_keys, uint3
   uint64_t blocks = std::min<uint64_t>((n + 1023) / 1024, (uint64_t)sm_count(db->device) * 16);
   lookup_kernel<<<(unsigned)std::max<uint64_t>(1, blocks), 256, 0, st>>>(db->table_view(), d_keys,
                                                                           d_vals, n);
+  note_launches();
   K2G_CUDA_TRY(cudaGetLastError());
   return K2G_OK;
+}
+
+// Random 32-byte sector gathers over the table's own cells: the access
+// pattern of a lookup without its hashing and compare, timed by callers to
+// get the random-access ceiling that lookups are measured against.  Each
+// thread keeps kGatherDepth independent loads in flight.
+constexpr int kGatherDepth = 4;
+
+__global__ void sector_gather_kernel(const uint4 *cells, uint64_t n_sectors, uint64_t per_thread,
+                                     uint64_t seed, uint32_t *sink) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  uint32_t acc = 0;
+  for (uint64_t it = 0; it < per_thread; it += kGatherDepth) {
+    uint4 v[kGatherDepth][2];
+#pragma unroll
+    for (int u = 0; u < kGatherDepth; u++) {
+      const uint64_t h = murmur3((tid << 24) ^ (it + u) ^ seed);
+      const uint4 *p = cells + 2 * __umul64hi(h, n_sectors);
+      v[u][0] = __ldg(p);
+      v[u][1] = __ldg(p + 1);
+    }
+#pragma unroll
+    for (int u = 0; u < kGatherDepth; u++) acc ^= v[u][0].x ^ v[u][1].w;
+  }
+  if (acc == 0x5eed5eedu) *sink = acc;   // keeps the loads live
 }
 
 extern "C" k2g_status k2g_lookup_host(const k2g_db *db, const uint64_t *keys, uint32_t *vals,
@@ -516,6 +548,24 @@ extern "C" k2g_status k2g_lookup_host(const k2g_db *db, const uint64_t *keys, ui
   if (e != cudaSuccess) return cuda_fail(e, "k2g_lookup_host");
   return s;
 }
+
+extern "C" k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint32_t *d_sink,
+                                        void *stream) {
+  if (!db || !d_sink) return fail(K2G_ERR_ARG, "null argument");
+  const uint64_t n_sectors = db->capacity / 8;   // whole 32-byte sectors of cells
+  if (!n_loads || !n_sectors) return K2G_OK;
+  K2G_CUDA_TRY(cudaSetDevice(db->device));
+  const uint64_t threads = (uint64_t)sm_count(db->device) * 16 * 256;
+  uint64_t per = (n_loads + threads - 1) / threads;
+  per = (per + kGatherDepth - 1) / kGatherDepth * kGatherDepth;
+  sector_gather_kernel<<<(unsigned)(threads / 256), 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const uint4 *>(db->d_cells), n_sectors, per, 0x9E3779B97F4A7C15ull, d_sink);
+  note_launches();
+  K2G_CUDA_TRY(cudaGetLastError());
+  return K2G_OK;
+}
+
+extern "C" uint64_t k2g_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 extern "C" k2g_status k2g_scan(const k2g_db *db, const char *d_bases, const uint64_t *d_seq_off,
                                uint64_t n_seqs, uint64_t *d_mins, uint8_t *d_ambig,
@@ -610,6 +660,7 @@ extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const
   insert_kernel<<<(unsigned)std::max<uint64_t>(1, blocks), 256, 0, st>>>(
       t, db->d_cells, db->d_parent, db->node_count, d_keys, d_taxids, n,
       reinterpret_cast<unsigned long long *>(db->d_size), d_status);
+  note_launches();
   uint32_t status = 0;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status, d_status, 4, cudaMemcpyDeviceToHost, st);

@@ -395,6 +395,7 @@ cudaError_t launch_pipe_step(const StepArgs &sa, cudaStream_t st) {
   const size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
                           ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
   pipe_step_kernel<W, QUAL, RC1><<<3 * most, kPipeBlock, smem, st>>>(sa);
+  note_launches();
   return cudaGetLastError();
 }
 

@@ -18,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "k2g.h")
 
 def declared_symbols():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:k2g_status|const char \*)\s*(k2g_\w+)\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:k2g_status|const char \*|uint64_t)\s*(k2g_\w+)\(", text, re.M)))
 
 
 def test_header_matches_binding():
