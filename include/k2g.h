@@ -167,6 +167,25 @@ k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
                         const k2g_classify_params *params, k2g_results *out,
                         int mode, void *stream);
 
+/* Limits of k2g_classify_static. */
+#define K2G_STATIC_MAX_FRAGS 262144u   /* fragments per call               */
+#define K2G_STATIC_MAX_LEN 512u        /* bases per sequence (mate)        */
+
+/* Classification that allocates no device memory (no counterpart in the
+ * reference).  Same inputs, outputs and results as k2g_classify in
+ * K2G_MODE_PLAIN, run on `stream` itself.  Its scratch is a fixed module
+ * array (about 11.2 MB, one per device) instead of library-allocated
+ * buffers.  For callers that must not allocate while classifying.  Rejects
+ * (K2G_ERR_ARG) more than K2G_STATIC_MAX_FRAGS fragments or max_seq_len
+ * above K2G_STATIC_MAX_LEN.
+ * The first call on a device resolves the scratch address and may load the
+ * module, so make it before any stream capture.  All calls on one device
+ * share the scratch: calls that overlap in time race, so order them on one
+ * stream or with events. */
+k2g_status k2g_classify_static(const k2g_db *db, const k2g_reads *reads,
+                               const k2g_classify_params *params, k2g_results *out,
+                               void *stream);
+
 /* Host-buffer classification: copies the reads in, classifies, and copies
  * the per-fragment results back, overlapping transfers with compute over
  * internal chunks (pinned buffers from k2g_host_alloc make the copies

@@ -34,7 +34,7 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_db_info_get", "k2g_db_write_hash", "k2g_db_download", "k2g_lookup",
            "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
            "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_sector_gather",
-           "k2g_kernel_launches"]
+           "k2g_kernel_launches", "k2g_classify_static"]
 
 
 class K2GError(RuntimeError):
@@ -111,6 +111,8 @@ def lib():
             "k2g_host_free": [vp],
             "k2g_build_insert": [vp, vp, vp, u64, i32, vp],
             "k2g_sector_gather": [vp, u64, vp, vp],
+            "k2g_classify_static": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams),
+                                    C.POINTER(Results), vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -207,6 +209,12 @@ class Database:
                  mode: int = MODE_PERSISTENT, stream: int = 0):
         check(lib().k2g_classify(self.h, C.byref(reads), C.byref(params), C.byref(results),
                                  mode, stream))
+
+    def classify_static(self, reads: Reads, params: ClassifyParams, results: Results,
+                        stream: int = 0):
+        """k2g_classify_static: plain classification with no device allocation."""
+        check(lib().k2g_classify_static(self.h, C.byref(reads), C.byref(params),
+                                        C.byref(results), stream))
 
     def build_insert(self, d_keys: int, d_taxids: int, n: int, ordered: bool = False,
                      stream: int = 0):

@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC]
 HOST_FLAGS = "-fPIC,-O3,-ffp-contract=off,-Wall"
 
-CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc.cu"]
+CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc.cu",
+              "classify_static.cu"]
 CC_SOURCES = ["db.cc"]
 
 
