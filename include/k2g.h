@@ -42,6 +42,15 @@ typedef enum {
   K2G_ERR_BUDGET = 9        /* request exceeds the serving HBM budget       */
 } k2g_status;
 
+/* Hit-event markers (records whose taxon is 0; the key holds the kind).
+ * RESET: drop the fragment's events whose ordinal lacks K2G_HIT_SLOW (a
+ * first attempt was abandoned and redone).  STOP: drop the fragment's events
+ * whose ordinal (without K2G_HIT_SLOW) is above the marker's -- the search
+ * ended there (quick mode). */
+#define K2G_HIT_MARK_RESET 1u
+#define K2G_HIT_MARK_STOP 2u
+#define K2G_HIT_SLOW 0x80000000u
+
 /* Codes of the per-k-mer hit list besides taxon ids (src/classify.cc:33-35). */
 #define K2G_CODE_MATE_BORDER 0xFFFFFFFFu
 #define K2G_CODE_AMBIGUOUS   0xFFFFFFFDu
@@ -145,8 +154,11 @@ typedef struct {
   uint64_t *d_runs;
   uint64_t runs_cap;
   uint64_t *d_taxon_reads;    /* [node_count] += calls per taxon, or NULL   */
-  /* add_kmer events for HyperLogLog++ (-K), or NULL: one record per LOOKUP
-   * token whose taxon is nonzero (src/classify.cc:869-873). */
+  /* add_kmer events for the taxon counters of -R/-K, or NULL: one record
+   * per LOOKUP token whose taxon is nonzero (src/classify.cc:869-873), in
+   * no particular order; d_hit_order gives (fragment, token ordinal).
+   * Records with taxon 0 are markers for that fragment (see
+   * K2G_HIT_MARK_*); k2g_counters_add applies them. */
   uint64_t *d_hit_keys;       /* the minimizer                              */
   uint32_t *d_hit_taxa;       /* its taxon                                  */
   uint64_t *d_hit_order;      /* (frag_base + fragment) << 32 | key ordinal */
@@ -185,6 +197,31 @@ k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
 k2g_status k2g_classify_static(const k2g_db *db, const k2g_reads *reads,
                                const k2g_classify_params *params, k2g_results *out,
                                void *stream);
+
+/* ---- taxon counters of --report-minimizer-data (-K): minimizer hits and
+ * HyperLogLog++ distinct-minimizer estimates per clade (src/classify.cc:554,
+ * :640-645, :869-873; src/reports.cc:32-45; src/hyperloglogplus.cc:117-190,
+ * :472-651, :709-739). */
+typedef struct k2g_counters k2g_counters;
+
+k2g_status k2g_counters_create(const k2g_db *db, k2g_counters **out);
+k2g_status k2g_counters_destroy(k2g_counters *c);
+
+/* Folds the add_kmer events of one k2g_classify call (res: d_hit_keys,
+ * d_hit_taxa, d_hit_order, d_hits_used, hits_cap) into the counters.
+ * reads->d_frag_block gives the reader block of each fragment
+ * (non-decreasing); a block must not continue into the next call, because
+ * each block's sketches decide their own sparse/dense switch.  Synchronises
+ * `stream`. */
+k2g_status k2g_counters_add(k2g_counters *c, const k2g_reads *reads, const k2g_results *res,
+                            void *stream);
+
+/* Per taxonomy node (node_count entries, host memory): taxon_kmers (may be
+ * NULL) = add_kmer calls of the taxon, clade_kmers = of its subtree (the
+ * report's minimizer column), clade_distinct = the HyperLogLog++ estimate of
+ * distinct minimizers of the subtree (the distinct-minimizer column). */
+k2g_status k2g_counters_finish(k2g_counters *c, uint64_t *taxon_kmers, uint64_t *clade_kmers,
+                               uint64_t *clade_distinct, void *stream);
 
 /* Host-buffer classification: copies the reads in, classifies, and copies
  * the per-fragment results back, overlapping transfers with compute over

@@ -28,13 +28,17 @@ MODE_PERSISTENT = 1
 MODE_PIPELINED = 2
 CODE_MATE_BORDER = 0xFFFFFFFF
 CODE_AMBIGUOUS = 0xFFFFFFFD
+HIT_MARK_RESET = 1          # K2G_HIT_MARK_RESET
+HIT_MARK_STOP = 2           # K2G_HIT_MARK_STOP
+HIT_SLOW = 0x80000000       # K2G_HIT_SLOW
 
 # Every symbol include/k2g.h declares.
 EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g_db_close",
            "k2g_db_info_get", "k2g_db_write_hash", "k2g_db_download", "k2g_lookup",
            "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
            "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_sector_gather",
-           "k2g_kernel_launches", "k2g_classify_static"]
+           "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
+           "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish"]
 
 
 class K2GError(RuntimeError):
@@ -113,6 +117,10 @@ def lib():
             "k2g_sector_gather": [vp, u64, vp, vp],
             "k2g_classify_static": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams),
                                     C.POINTER(Results), vp],
+            "k2g_counters_create": [vp, C.POINTER(vp)],
+            "k2g_counters_destroy": [vp],
+            "k2g_counters_add": [vp, C.POINTER(Reads), C.POINTER(Results), vp],
+            "k2g_counters_finish": [vp, vp, vp, vp, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -219,3 +227,34 @@ class Database:
     def build_insert(self, d_keys: int, d_taxids: int, n: int, ordered: bool = False,
                      stream: int = 0):
         check(lib().k2g_build_insert(self.h, d_keys, d_taxids, n, int(ordered), stream))
+
+
+class Counters:
+    """Taxon counters of -R/-K on the device (k2g_counters)."""
+
+    def __init__(self, db: "Database"):
+        self.db = db
+        self.h = C.c_void_p()
+        check(lib().k2g_counters_create(db.h, C.byref(self.h)))
+
+    def add(self, reads: Reads, results: Results, stream: int = 0):
+        check(lib().k2g_counters_add(self.h, C.byref(reads), C.byref(results), stream))
+
+    def finish(self, stream: int = 0):
+        """-> (taxon_kmers, clade_kmers, clade_distinct), uint64 per node."""
+        n = self.db.info().node_count
+        tk, ck, cd = (np.zeros(n, np.uint64) for _ in range(3))
+        check(lib().k2g_counters_finish(self.h, tk.ctypes.data, ck.ctypes.data, cd.ctypes.data,
+                                        stream))
+        return tk, ck, cd
+
+    def close(self):
+        if self.h:
+            lib().k2g_counters_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

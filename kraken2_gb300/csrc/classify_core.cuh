@@ -166,6 +166,7 @@ struct Lane {
   uint32_t hit_groups;
   uint32_t total_tokens;
   uint32_t key_ordinal;
+  uint32_t stop_ordinal;   // key ordinal of the lookup that ended a quick search
   uint32_t distinct;
   bool quick_stop;
   uint64_t run_base;
@@ -227,6 +228,7 @@ __device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, ui
   s.hit_groups = 0;
   s.total_tokens = 0;
   s.key_ordinal = 0;
+  s.stop_ordinal = 0;
   s.distinct = 0;
   s.quick_stop = false;
   s.run_base = o0 + 2 * (f + a.frag_off);
@@ -490,6 +492,7 @@ __device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const Clas
         s.hit_groups++;
         if (a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
           s.quick_stop = true;
+          s.stop_ordinal = s.key_ordinal + ki;
           return true;
         }
       }

@@ -78,8 +78,8 @@ classify_kernel(ClassifyArgs a, int persistent) {
       int ng = 0, nk = 0;
       scan_segment<W, QUAL, RC1>(s, st, a, ng, nk);
       probe_segment(st, a, nk, s.frag, s.key_ordinal);
-      s.key_ordinal += nk;
       bool ok = replay_segment(s, st, a, ng);
+      s.key_ordinal += nk;
       if (!ok) {
         // taxon map overflow: hand the fragment to the slow path
         unsigned long long at = atomicAdd(a.defer_count, 1ull);
@@ -89,6 +89,9 @@ classify_kernel(ClassifyArgs a, int persistent) {
         s.frag = ~0ull;
       } else if (s.quick_stop || s.scan_done) {
         finish_fragment(s, st, a);
+        // probe_segment emitted every hit of the last segment; the marker
+        // drops those after the lookup that ended the quick search
+        if (a.hit_keys && s.quick_stop) emit_hit(a, s.frag, s.stop_ordinal, K2G_HIT_MARK_STOP, 0);
         s.frag = ~0ull;
       }
     }
@@ -114,15 +117,19 @@ __global__ void classify_slow_kernel(ClassifyArgs a, int mcap) {
   for (uint64_t li = tid; li < n_list; li += (uint64_t)gridDim.x * blockDim.x) {
     Lane<0> s;
     lane_begin(s, a, a.frag_list[li]);
+    // events of an earlier, abandoned attempt at this fragment are void
+    if (a.hit_keys) emit_hit(a, s.frag, K2G_HIT_SLOW, K2G_HIT_MARK_RESET, 0);
     while (true) {
       int ng = 0, nk = 0;
       scan_segment<0, QUAL, RC1>(s, st, a, ng, nk);
-      probe_segment(st, a, nk, s.frag, s.key_ordinal | 0x80000000u);
-      s.key_ordinal += nk;
+      probe_segment(st, a, nk, s.frag, s.key_ordinal | K2G_HIT_SLOW);
       replay_segment(s, st, a, ng);   // cannot overflow: map sized for all tokens
+      s.key_ordinal += nk;
       if (s.quick_stop || s.scan_done) break;
     }
     finish_fragment(s, st, a);
+    if (a.hit_keys && s.quick_stop)
+      emit_hit(a, s.frag, s.stop_ordinal | K2G_HIT_SLOW, K2G_HIT_MARK_STOP, 0);
   }
 }
 

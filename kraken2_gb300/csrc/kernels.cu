@@ -248,6 +248,8 @@ struct ExecCtx {
   uint32_t *gcount = nullptr;
   uint32_t *bcount = nullptr;
   uint64_t cap_frags = 0;
+  uint64_t *gkey = nullptr;       // only when hit events are requested
+  uint64_t cap_gkey = 0;
 };
 
 struct DeviceState {
@@ -271,7 +273,7 @@ static cudaError_t grow(T *&p, uint64_t &cap, uint64_t want) {
 }
 
 static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t slow_bytes,
-                              bool pipeline) {
+                              bool pipeline, bool keys) {
   if (!c.counters) K2G_CUDA_TRY(cudaMalloc(&c.counters, 2 * sizeof(unsigned long long)));
   K2G_CUDA_TRY(grow(c.defer_list, c.defer_cap, std::max<uint64_t>(1024, frags)));
   if (c.slow_bytes < slow_bytes) {
@@ -292,6 +294,7 @@ static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t
     K2G_CUDA_TRY(grow(c.rslot, cs, slots));
     c.cap_slots = slots;
   }
+  if (pipeline && keys) K2G_CUDA_TRY(grow(c.gkey, c.cap_gkey, slots));
   if (pipeline && c.cap_frags < frags) {
     uint64_t cf = c.cap_frags;
     K2G_CUDA_TRY(grow(c.gcount, cf, frags));
@@ -412,6 +415,7 @@ static PipeArgs pipe_view(const ClassifyArgs &a, const ExecCtx &c) {
   p.rkey = c.rkey;
   p.rslot = c.rslot;
   p.bcount = c.bcount;
+  p.gkey = a.hit_keys ? c.gkey : nullptr;
   p.cap_slots = c.cap_slots;
   return p;
 }
@@ -434,7 +438,7 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
   const SlowPlan sp = slow_plan(max_len, a0.cls.paired != 0);
   const int nctx = pipeline ? 3 : 1;
   for (int i = 0; i < nctx; i++) {
-    k2g_status s = ctx_reserve(ds.ctx[i], sb, cap_slots, sp.bytes, pipeline);
+    k2g_status s = ctx_reserve(ds.ctx[i], sb, cap_slots, sp.bytes, pipeline, a0.hit_keys != nullptr);
     if (s != K2G_OK) return s;
   }
   cudaStream_t st = ds.st;

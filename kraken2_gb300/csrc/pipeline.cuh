@@ -38,6 +38,7 @@ struct PipeArgs {
   uint64_t *rkey;
   uint32_t *rslot;
   uint32_t *bcount;
+  uint64_t *gkey;         // key of each lookup group, or null (only with hit events)
   uint64_t cap_slots;     // capacity of gstream / gtax / records
 };
 
@@ -267,7 +268,11 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
 #pragma unroll
     for (int b = 0; b < B; b++) {
       const uint32_t i = i0 + b * kPipeBlock;
-      if (i < cnt) pa.gtax[rbase + pa.rslot[rbase + i]] = probe_sectors(t, hc[b], idx[b], sec[b]);
+      if (i < cnt) {
+        const uint32_t slot = pa.rslot[rbase + i];
+        pa.gtax[rbase + slot] = probe_sectors(t, hc[b], idx[b], sec[b]);
+        if (pa.gkey) pa.gkey[rbase + slot] = pa.rkey[rbase + i];
+      }
     }
   }
 }
@@ -293,6 +298,46 @@ struct ResolveLane {
   uint64_t run_base;
 };
 
+// add_kmer events of the fragments this warp completed (src/classify.cc:
+// 869-873): every lookup group with a nonzero taxon, in token order, up to
+// and including the group that ended a quick-mode search -- n_ev of them,
+// which is the fragment's hit-group count.  One atomic per warp reserves the
+// warp's range; all 32 lanes take part (n_ev = 0 for idle lanes).
+__device__ __forceinline__ void pipe_emit_hits(const PipeArgs &pa, uint64_t f, uint64_t gb,
+                                               uint32_t ng, uint32_t n_ev) {
+  const ClassifyArgs &a = pa.a;
+  const unsigned lane = threadIdx.x & 31;
+  uint32_t incl = n_ev;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (unsigned)o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned long long base = 0;
+  if (lane == 31 && total) base = atomicAdd(a.hits_used, (unsigned long long)total);
+  base = __shfl_sync(0xffffffffu, base, 31) + (incl - n_ev);
+  if (!n_ev) return;
+  if (base + n_ev > a.hits_cap) {
+    atomicOr(a.status, STATUS_HITS_OVERFLOW);
+    return;
+  }
+  const uint64_t order0 = (a.frag_base + f) << 32;
+  uint32_t k = 0, ordinal = 0;
+  for (uint32_t g = 0; g < ng && k < n_ev; g++) {
+    const uint32_t kind = pa.gstream[gb + g] >> kGroupLenBits;
+    if (kind != G_KEY) continue;
+    const uint32_t taxon = pa.gtax[gb + g];
+    if (taxon) {
+      a.hit_keys[base + k] = pa.gkey[gb + g];
+      a.hit_taxa[base + k] = taxon;
+      a.hit_order[base + k] = order0 | ordinal;
+      k++;
+    }
+    ordinal++;
+  }
+}
+
 // Resolve: replay the token groups with their taxa (src/classify.cc:847-888),
 // then ResolveTree and the outputs (finish_fragment).  A fragment whose
 // taxon map overflows is handed to the slow path.
@@ -302,64 +347,71 @@ __device__ __forceinline__ void pipe_resolve_body(const PipeArgs &pa, uint32_t b
   uint32_t *s_mcnt = s_mkey + ResolveMap::kMapResolve * kPipeBlock;
   const ClassifyArgs &a = pa.a;
   const uint64_t f = (uint64_t)blk * kPipeBlock + threadIdx.x;
-  if (f >= a.n_frags) return;
-  ResolveMap st{s_mkey, s_mcnt, (int)threadIdx.x};
-  for (int i = 0; i < ResolveMap::kMapResolve; i++) st.map_key(i) = 0;
-  ResolveLane s;
-  s.frag = f;
-  s.cur_taxon = 0;
-  s.run_code = s.run_cnt = s.n_runs = 0;
-  s.hit_groups = 0;
-  s.total_tokens = 0;
-  s.distinct = 0;
-  s.quick_stop = false;
-  const int per = a.cls.paired ? 2 : 1;
-  s.run_base = a.seq_off[f * per] + 2 * (f + a.frag_off);
-  const uint64_t gb = pipe_gbase(pa, f);
-  const uint32_t ng = pa.gcount[f];
-  if (ng == 0xFFFFFFFFu) return;   // deferred by the scan
-  for (uint32_t g = 0; g < ng; g++) {
-    const uint32_t grp = pa.gstream[gb + g];
-    const uint32_t kind = grp >> kGroupLenBits, len = grp & kGroupMaxLen;
-    uint32_t taxon;
-    if (kind == G_AMBIG) {
-      emit_run(s, a, K2G_CODE_AMBIGUOUS, len);
-      s.total_tokens += len;
-      continue;
-    }
-    if (kind == G_BORDER) {
-      emit_run(s, a, K2G_CODE_MATE_BORDER, 1);
-      s.total_tokens += 1;
-      continue;
-    }
-    if (kind == G_KEY) {
-      taxon = pa.gtax[gb + g];
-      s.cur_taxon = taxon;
-      if (taxon) {
-        s.hit_groups++;
-        if (a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
-          s.quick_stop = true;
-          break;
-        }
+  uint64_t gb = 0;
+  uint32_t ng = 0, n_ev = 0;
+  if (f < a.n_frags) {
+    ResolveMap st{s_mkey, s_mcnt, (int)threadIdx.x};
+    for (int i = 0; i < ResolveMap::kMapResolve; i++) st.map_key(i) = 0;
+    ResolveLane s;
+    s.frag = f;
+    s.cur_taxon = 0;
+    s.run_code = s.run_cnt = s.n_runs = 0;
+    s.hit_groups = 0;
+    s.total_tokens = 0;
+    s.distinct = 0;
+    s.quick_stop = false;
+    const int per = a.cls.paired ? 2 : 1;
+    s.run_base = a.seq_off[f * per] + 2 * (f + a.frag_off);
+    gb = pipe_gbase(pa, f);
+    ng = pa.gcount[f];
+    bool done = ng != 0xFFFFFFFFu;   // else deferred by the scan
+    for (uint32_t g = 0; done && g < ng; g++) {
+      const uint32_t grp = pa.gstream[gb + g];
+      const uint32_t kind = grp >> kGroupLenBits, len = grp & kGroupMaxLen;
+      uint32_t taxon;
+      if (kind == G_AMBIG) {
+        emit_run(s, a, K2G_CODE_AMBIGUOUS, len);
+        s.total_tokens += len;
+        continue;
       }
-    } else if (kind == G_SKIP) {
-      taxon = 0;
-      s.cur_taxon = 0;
-    } else {
-      taxon = s.cur_taxon;
+      if (kind == G_BORDER) {
+        emit_run(s, a, K2G_CODE_MATE_BORDER, 1);
+        s.total_tokens += 1;
+        continue;
+      }
+      if (kind == G_KEY) {
+        taxon = pa.gtax[gb + g];
+        s.cur_taxon = taxon;
+        if (taxon) {
+          s.hit_groups++;
+          if (a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
+            s.quick_stop = true;
+            break;
+          }
+        }
+      } else if (kind == G_SKIP) {
+        taxon = 0;
+        s.cur_taxon = 0;
+      } else {
+        taxon = s.cur_taxon;
+      }
+      if (taxon && !map_add(st, s.distinct, taxon, len)) {
+        unsigned long long at = atomicAdd(a.defer_count, 1ull);
+        if (at < a.defer_cap) a.defer_list[at] = f;
+        else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
+        done = false;
+      }
+      if (!done) break;
+      emit_run(s, a, taxon, len);
+      s.total_tokens += len;
     }
-    if (taxon && !map_add(st, s.distinct, taxon, len)) {
-      unsigned long long at = atomicAdd(a.defer_count, 1ull);
-      if (at < a.defer_cap) a.defer_list[at] = f;
-      else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
-      return;
+    if (done) {
+      finish_fragment(s, st, a);
+      n_ev = s.hit_groups;
     }
-    emit_run(s, a, taxon, len);
-    s.total_tokens += len;
   }
-  finish_fragment(s, st, a);
+  if (a.hit_keys) pipe_emit_hits(pa, f, gb, ng, n_ev);
 }
-
 
 }  // namespace k2g
 
