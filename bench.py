@@ -313,6 +313,64 @@ class DeviceRunner:
                 self.wl.stream.synchronize()
 
 
+class KmerRunner:
+    """Classification with add_kmer events folded into the -K taxon counters
+    (k2g_counters), batch by batch, then the clade estimates.  Reader blocks
+    are those of a 150 bp single-end FASTQ read in 3 MiB blocks; batches hold
+    whole blocks."""
+
+    def __init__(self, wl: Workload, mode: int, n_reads: int | None = None,
+                 blocks_per_batch: int = 476):
+        torch, cfg, k2g = wl.torch, wl.cfg, wl.k2g
+        self.wl, self.mode = wl, mode
+        self.n_reads = n_reads or cfg.n_reads
+        self.block = -(-(3 * 1024 * 1024) // cfg.read_len)
+        self.batch = min(self.n_reads, self.block * blocks_per_batch)
+        B, L, dev = self.batch, cfg.read_len, wl.dev
+        self.off = torch.arange(B + 1, dtype=torch.int64, device=dev) * L
+        self.call = torch.empty(B, dtype=torch.int32, device=dev)
+        self.hg = torch.empty(B, dtype=torch.int32, device=dev)
+        self.hoff = torch.empty(B, dtype=torch.int64, device=dev)
+        self.hlen = torch.empty(B, dtype=torch.int32, device=dev)
+        self.runs_cap = B * (L + 2) + 8
+        self.runs = torch.empty(self.runs_cap, dtype=torch.int64, device=dev)
+        self.tr = torch.zeros(cfg.nodes, dtype=torch.int64, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.hits_cap = 64 * B
+        self.hk = torch.empty(self.hits_cap, dtype=torch.int64, device=dev)
+        self.ht = torch.empty(self.hits_cap, dtype=torch.int32, device=dev)
+        self.ho = torch.empty(self.hits_cap, dtype=torch.int64, device=dev)
+        self.hu = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.blk = (torch.arange(self.n_reads, dtype=torch.int64, device=dev)
+                    // self.block).to(torch.int32)
+        self.params = k2g.ClassifyParams(cfg.confidence, cfg.min_hit_groups, 0, 0, 0)
+
+    def run(self):
+        """One pass over the reads -> (taxon_reads, clade_kmers, clade_distinct)."""
+        wl, k2g, cfg = self.wl, self.wl.k2g, self.wl.cfg
+        st = wl.stream.cuda_stream
+        counters = k2g.Counters(wl.db)
+        self.tr.zero_()
+        for b0 in range(0, self.n_reads, self.batch):
+            n = min(self.batch, self.n_reads - b0)
+            self.hu.zero_()
+            reads = k2g.Reads(d_bases=wl.reads.data_ptr() + b0 * cfg.read_len, d_quals=None,
+                              d_seq_off=self.off.data_ptr(), n_frags=n, max_seq_len=cfg.read_len,
+                              total_bases=n * cfg.read_len,
+                              d_frag_block=self.blk.data_ptr() + 4 * b0, frag_base=b0)
+            res = k2g.Results(self.call.data_ptr(), self.hg.data_ptr(), self.hoff.data_ptr(),
+                              self.hlen.data_ptr(), self.runs.data_ptr(), self.runs_cap,
+                              self.tr.data_ptr(), self.hk.data_ptr(), self.ht.data_ptr(),
+                              self.ho.data_ptr(), self.hits_cap, self.hu.data_ptr(),
+                              self.status.data_ptr())
+            wl.torch.cuda.current_stream().synchronize()
+            wl.db.classify(reads, self.params, res, mode=self.mode, stream=st)
+            counters.add(reads, res, st)
+        _, clade_kmers, distinct = counters.finish(st)
+        counters.close()
+        return self.tr.cpu().numpy().view(np.uint64).copy(), clade_kmers, distinct
+
+
 def murmur3_np(keys: np.ndarray) -> np.ndarray:
     """MurmurHash3 finalizer (src/kv_store.h:59-67), vectorised."""
     k = keys.astype(np.uint64).copy()
@@ -386,6 +444,25 @@ def cpu_classify(wl: Workload, cells: np.ndarray, n_reads: int, threads: int):
                                            min_hit_groups=cfg.min_hit_groups)
     dt = time.perf_counter() - t0
     return dt, calls, hg, nr, runs, base
+
+
+def kmer_parity(wl: Workload, cells: np.ndarray, mode: int, n_blocks: int = 5) -> dict:
+    """-K counters of the GPU against the oracle on the first reader blocks."""
+    import oracle
+    cfg = wl.cfg
+    kr = KmerRunner(wl, mode, n_reads=min(cfg.n_reads, n_blocks * -(-(3 << 20) // cfg.read_len)))
+    n = kr.n_reads
+    tr, ck, cd = kr.run()
+    L = cfg.read_len
+    bases = wl.reads[:n * L].cpu().numpy().tobytes()
+    off = np.arange(n + 1, dtype=np.uint64) * L
+    o = oracle.Oracle(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, wl.parent,
+                      oracle.index_opts(cfg.k, cfg.l, spaced_mask(SEED_TEMPLATE), TOGGLE))
+    _, otr, ock, ocd = o.taxon_counters(bases, None, off, n, kr.blk[:n].cpu().numpy().view(np.uint32),
+                                         kmer_data=True, confidence=cfg.confidence,
+                                         min_hit_groups=cfg.min_hit_groups)
+    bad = int((ck != ock).sum() + (cd != ocd).sum() + (tr != otr).sum())
+    return {"reads": n, "taxa": int((ock > 0).sum()), "mismatches_vs_oracle": bad}
 
 
 def e2e_run(wl: Workload, n_reads: int, steps: int):
@@ -536,10 +613,29 @@ def run_ours(args, log):
         torch.cuda.synchronize()
         plain = cfg.n_reads / (ps.elapsed_time(pe) / 1e3)
 
+    # --report-minimizer-data (-K): the same reads with add_kmer events and the
+    # HyperLogLog++ taxon counters, one full pass timed end to end on the host
+    kmer = None
+    if not args.skip_kmer:
+        kr = KmerRunner(wl, mode)
+        kr.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kr.run()
+        torch.cuda.synchronize()
+        kdt = time.perf_counter() - t0
+        kmer = {"mreads_min": round(cfg.n_reads / kdt * 60 / 1e6, 3), "s_per_pass": round(kdt, 3),
+                "reads": cfg.n_reads, "blocks_per_batch": kr.batch // kr.block,
+                "reads_per_block": kr.block}
+        del kr
+        log(f"-K pass {kdt:.2f}s")
+
     # host copy of the table: algorithmic bytes, parity sample, CPU baseline
     t0 = time.time()
     cells, _ = wl.db.download()
     log(f"table download {time.time() - t0:.1f}s")
+    if kmer is not None:
+        kmer["parity"] = kmer_parity(wl, cells, mode)
     n_sample = min(cfg.n_reads, 50_000)
     keys = sample_lookup_keys(wl, n_sample)
     sectors, hit = probe_sectors(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, keys)
@@ -629,6 +725,7 @@ def run_ours(args, log):
         "plain_vs_batched": ({"plain_mreads_min": round(plain * 60 / 1e6, 3),
                               "plain_form": "one synchronous launch per 3 MiB reader block",
                               "batched_over_plain": round(reads_s / plain, 3)} if plain else None),
+        "minimizer_data": kmer,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -681,6 +778,8 @@ def main():
                     help="fraction of the full-size workload (tests and probes only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-kmer", action="store_true",
+                    help="skip the -K (minimizer data) measurement")
     ap.add_argument("--profile", action="store_true",
                     help="setup plus two classification steps only (for ncu captures)")
     args = ap.parse_args()

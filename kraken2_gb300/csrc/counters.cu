@@ -125,14 +125,18 @@ __global__ void count_kernel(EventView ev, uint32_t *seg, const uint32_t *pre, i
     const uint64_t j = i0 + lane;
     bool keep = false;
     uint64_t key = 0;
+    int64_t si = -1;
     if (j < ev.n) {
-      const int64_t si = seg_index(ev, j);
+      si = seg_index(ev, j);
       if (si >= 0) {
         keep = true;
-        atomicAdd(&seg[si], 1u);
         key = ((uint64_t)hll_encode(hll_hash(ev.keys[j])) << tbits) | pre[ev.taxa[j]];
       }
     }
+    // one atomic per distinct (taxon, block) in the warp: a read's hits
+    // mostly fall on one taxon, and a warp holds a few reads' events
+    const unsigned same = __match_any_sync(0xffffffffu, (unsigned long long)si);
+    if (si >= 0 && (__ffs(same) - 1) == (int)lane) atomicAdd(&seg[si], (unsigned)__popc(same));
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     unsigned long long base = 0;
     if (lane == 0 && m) base = atomicAdd(acc_used, (unsigned long long)__popc(m));
@@ -289,8 +293,8 @@ struct CladeView {
   const uint32_t *parent;
   const uint32_t *slot;      // taxon -> register block of a dense clade, or ~0
   uint32_t *regs;            // [dense clades][4096]
-  uint32_t *hist;            // [node][kHist] rank counts of sparse clades
-  uint32_t *size;            // [node] distinct encodings of sparse clades
+  uint32_t *hist;            // [node][kHist] rank counts of sparse clades (their
+                             // sum is the number of distinct encodings)
 };
 
 // Keys are (encoding << tbits | preorder), sorted and unique.  Within one
@@ -313,7 +317,6 @@ __global__ void clade_walk_kernel(const uint64_t *k, uint64_t n, int tbits, Clad
         atomicMax(&cv.regs[(uint64_t)sl * (1u << kHllP) + idx], r);
       } else {
         atomicAdd(&cv.hist[(uint64_t)a * kHist + (r < kHist ? r : kHist - 1)], 1u);
-        atomicAdd(&cv.size[a], 1u);
       }
     }
   }
@@ -353,6 +356,7 @@ struct k2g_counters {
   uint8_t *d_dense = nullptr;          // some block's sketch of the taxon went dense
   unsigned long long *d_ctr = nullptr; // [0] accumulator fill, [1] big segments, [2] big events
   uint64_t *d_acc = nullptr, acc_cap = 0, acc_used = 0, acc_compact = 0;
+  uint64_t acc_budget = 0;             // keys held before a compaction is forced
   uint64_t *d_alt = nullptr, alt_cap = 0;
   uint8_t *d_reset = nullptr;
   uint32_t *d_stop = nullptr;
@@ -460,6 +464,7 @@ k2g_status sort_unique(k2g_counters *c, uint64_t *&keys, uint64_t &keys_cap, uin
 }
 
 k2g_status compact_acc(k2g_counters *c, cudaStream_t st) {
+  if (c->acc_used == c->acc_compact) return K2G_OK;   // already sorted and unique
   uint64_t n = 0;
   k2g_status s = sort_unique(c, c->d_acc, c->acc_cap, c->d_alt, c->alt_cap, c->acc_used,
                              32 + c->tbits, st, &n);
@@ -574,6 +579,11 @@ extern "C" k2g_status k2g_counters_create(const k2g_db *db, k2g_counters **out) 
       (e = cudaMemset(c->d_ctr, 0, 4 * sizeof(unsigned long long))) != cudaSuccess)
     return bad(cuda_fail(e, "counter set-up"));
   (void)dummy;
+  // a quarter of the free memory for the accumulator and its sort buffer
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 1ull << 32;
+  c->acc_budget = std::max<uint64_t>(free_b / 4 / 16, 1ull << 24);
+  c->acc_budget = std::min<uint64_t>(c->acc_budget, (1ull << 32) - (1ull << 30));
   *out = c;
   return K2G_OK;
 }
@@ -671,8 +681,9 @@ extern "C" k2g_status k2g_counters_add(k2g_counters *c, const k2g_reads *reads,
     note_launches(2);
     K2G_CUDA_TRY(cudaGetLastError());
   }
-  // keep the accumulator near its distinct size
-  if (c->acc_used > std::max<uint64_t>(2 * c->acc_compact, 1ull << 26)) {
+  // Sorting once at the end costs least; compact earlier only when the
+  // accumulator (and the sort's second buffer) would outgrow its budget.
+  if (c->acc_used > c->acc_budget) {
     k2g_status s = compact_acc(c, st);
     if (s != K2G_OK) return s;
   }
@@ -711,25 +722,23 @@ extern "C" k2g_status k2g_counters_finish(k2g_counters *c, uint64_t *taxon_kmers
       clade_of_slot.push_back((uint32_t)t);
     }
   const uint64_t nd = clade_of_slot.size();
-  uint32_t *d_slot = nullptr, *d_cos = nullptr, *d_regs = nullptr, *d_hist = nullptr, *d_size = nullptr;
+  uint32_t *d_slot = nullptr, *d_cos = nullptr, *d_regs = nullptr, *d_hist = nullptr;
   auto release = [&]() {
-    for (void *p : {(void *)d_slot, (void *)d_cos, (void *)d_regs, (void *)d_hist, (void *)d_size})
+    for (void *p : {(void *)d_slot, (void *)d_cos, (void *)d_regs, (void *)d_hist})
       if (p) cudaFree(p);
   };
-  std::vector<uint32_t> hist(n * kHist), size(n);
+  std::vector<uint32_t> hist(n * kHist);
   cudaError_t e = cudaSuccess;
   do {
     if ((e = cudaMalloc(&d_slot, n * 4)) != cudaSuccess) break;
     if ((e = cudaMalloc(&d_cos, std::max<uint64_t>(nd, 1) * 4)) != cudaSuccess) break;
     if ((e = cudaMalloc(&d_regs, std::max<uint64_t>(nd, 1) * (4ull << kHllP))) != cudaSuccess) break;
     if ((e = cudaMalloc(&d_hist, n * kHist * 4)) != cudaSuccess) break;
-    if ((e = cudaMalloc(&d_size, n * 4)) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(d_slot, slot.data(), n * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
     if (nd && (e = cudaMemcpyAsync(d_cos, clade_of_slot.data(), nd * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(d_regs, 0, std::max<uint64_t>(nd, 1) * (4ull << kHllP), st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(d_hist, 0, n * kHist * 4, st)) != cudaSuccess) break;
-    if ((e = cudaMemsetAsync(d_size, 0, n * 4, st)) != cudaSuccess) break;
-    CladeView cv{c->d_node_of, c->d_pre, c->d_end, c->db->d_parent, d_slot, d_regs, d_hist, d_size};
+    CladeView cv{c->d_node_of, c->d_pre, c->d_end, c->db->d_parent, d_slot, d_regs, d_hist};
     if (c->acc_used) {
       clade_walk_kernel<<<grid_for(c->device, c->acc_used), 256, 0, st>>>(c->d_acc, c->acc_used,
                                                                           c->tbits, cv);
@@ -741,7 +750,6 @@ extern "C" k2g_status k2g_counters_finish(k2g_counters *c, uint64_t *taxon_kmers
     }
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     if ((e = cudaMemcpyAsync(hist.data(), d_hist, n * kHist * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
-    if ((e = cudaMemcpyAsync(size.data(), d_size, n * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
     e = cudaStreamSynchronize(st);
   } while (false);
   release();
@@ -755,7 +763,9 @@ extern "C" k2g_status k2g_counters_finish(k2g_counters *c, uint64_t *taxon_kmers
     if (dense_clade[a]) {
       clade_distinct[a] = ertl_estimate(C, 64 - kHllP, 1ull << kHllP, clade_kmers[a]);
     } else {
-      C[0] = (1ull << kHllPP) - size[a];
+      uint64_t size = 0;
+      for (int i = 1; i < kHist; i++) size += C[i];
+      C[0] = (1ull << kHllPP) - size;
       clade_distinct[a] = ertl_estimate(C, 64 - kHllPP, 1ull << kHllPP, clade_kmers[a]);
     }
   }
