@@ -236,6 +236,18 @@ k2g_status k2g_classify_host(const k2g_db *db, const char *bases, const char *qu
                              uint32_t *hit_groups, uint32_t *hitlist_len, uint64_t *runs,
                              uint64_t *n_runs, uint64_t *taxon_reads);
 
+/* k2g_classify_host for a caller that reads in reader blocks: frag_block
+ * (host, one per fragment, non-decreasing) gives each fragment's block, and
+ * when counters is non-NULL every fragment's add_kmer events are folded into
+ * it (k2g_counters_add; internal chunks end at block boundaries).  counters
+ * may be NULL; frag_block may be NULL only when counters is. */
+k2g_status k2g_classify_host_blocks(const k2g_db *db, const char *bases, const char *quals,
+                                    const uint64_t *seq_off, uint64_t n_frags,
+                                    const uint32_t *frag_block, k2g_counters *counters,
+                                    const k2g_classify_params *params, uint32_t *call,
+                                    uint32_t *hit_groups, uint32_t *hitlist_len,
+                                    uint64_t *runs, uint64_t *n_runs, uint64_t *taxon_reads);
+
 /* Pinned host memory helpers for callers that stage their own buffers. */
 k2g_status k2g_host_alloc(void **ptr, size_t bytes);
 k2g_status k2g_host_free(void *ptr);

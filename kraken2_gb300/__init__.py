@@ -38,7 +38,8 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
            "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_sector_gather",
            "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
-           "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish"]
+           "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
+           "k2g_classify_host_blocks"]
 
 
 class K2GError(RuntimeError):
@@ -121,6 +122,8 @@ def lib():
             "k2g_counters_destroy": [vp],
             "k2g_counters_add": [vp, C.POINTER(Reads), C.POINTER(Results), vp],
             "k2g_counters_finish": [vp, vp, vp, vp, vp],
+            "k2g_classify_host_blocks": [vp, vp, vp, vp, u64, vp, vp, C.POINTER(ClassifyParams),
+                                         vp, vp, vp, vp, C.POINTER(u64), vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

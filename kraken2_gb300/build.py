@@ -16,6 +16,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
+HOST = os.path.join(HERE, "host")
 OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
@@ -26,6 +27,8 @@ HOST_FLAGS = "-fPIC,-O3,-ffp-contract=off,-Wall"
 CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc.cu",
               "classify_static.cu", "counters.cu"]
 CC_SOURCES = ["db.cc"]
+# the classify drop-in (host C++ over the C ABI)
+HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "report.cc"]
 
 
 def nvcc() -> str:
@@ -51,11 +54,26 @@ def _newer(target, deps):
 
 def _deps():
     out = []
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, HOST):
         for f in os.listdir(d):
             if f.endswith((".h", ".cuh", ".cu", ".cc")):
                 out.append(os.path.join(d, f))
     return out
+
+
+def classify_path() -> str:
+    return os.path.join(OUT, "classify")
+
+
+def _build_classify(lib: str):
+    """g++ for the drop-in; it finds libk2g.so next to itself ($ORIGIN)."""
+    gxx = shutil.which("g++") or "g++"
+    exe = classify_path()
+    tmp = exe + ".tmp"
+    _run([gxx, "-O2", "-std=c++17", "-Wall", "-I", INCLUDE,
+          *[os.path.join(HOST, s) for s in HOST_SOURCES],
+          "-L", OUT, "-lk2g", "-Wl,-rpath,$ORIGIN", "-o", tmp])
+    os.replace(tmp, exe)
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
@@ -63,7 +81,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     lib = os.path.join(OUT, "libk2g.so")
     deps = _deps()
+    if not force and _newer(lib, deps + [__file__]) and _newer(classify_path(), deps + [lib]):
+        return lib
     if not force and _newer(lib, deps + [__file__]):
+        _build_classify(lib)
         return lib
     nv = nvcc()
     jobs = []
@@ -86,6 +107,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     tmp = lib + ".tmp"
     _run([nv, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static", "-lpthread"])
     os.replace(tmp, lib)
+    _build_classify(lib)
     return lib
 
 

@@ -112,6 +112,9 @@ struct Slot {
   uint64_t *sparse = nullptr, *dense = nullptr, *excl = nullptr, *sums = nullptr;
   uint64_t *total = nullptr;       // device
   uint64_t *h_total = nullptr;     // pinned
+  // add_kmer events (only with counters)
+  uint64_t *hit_keys = nullptr, *hit_order = nullptr, *hits_used = nullptr;
+  uint32_t *hit_taxa = nullptr, *blocks = nullptr;
   // chunk bookkeeping for the deferred runs copy
   bool pending = false;
   uint64_t f0 = 0, nf = 0;
@@ -120,7 +123,8 @@ struct Slot {
 void free_slot(Slot &s) {
   if (s.st) cudaStreamSynchronize(s.st);
   void *dev[] = {s.bases, s.quals, s.off, s.call, s.hg, s.hlen, s.status, s.sparse,
-                 s.dense, s.excl, s.sums, s.total};
+                 s.dense, s.excl, s.sums, s.total, s.hit_keys, s.hit_order, s.hits_used,
+                 s.hit_taxa, s.blocks};
   for (void *p : dev)
     if (p) cudaFree(p);
   if (s.h_total) cudaFreeHost(s.h_total);
@@ -130,13 +134,17 @@ void free_slot(Slot &s) {
 
 }  // namespace
 
-extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, const char *quals,
-                                        const uint64_t *seq_off, uint64_t n_frags,
-                                        const k2g_classify_params *params, uint32_t *call,
-                                        uint32_t *hit_groups, uint32_t *hitlist_len,
-                                        uint64_t *runs, uint64_t *n_runs,
-                                        uint64_t *taxon_reads) {
+// Host-buffer classification over double-buffered chunks.  With counters,
+// chunks end at reader-block boundaries (frag_block) and each chunk's
+// add_kmer events are folded in after it is classified.
+static k2g_status host_classify(const k2g_db *db, const char *bases, const char *quals,
+                                const uint64_t *seq_off, uint64_t n_frags,
+                                const uint32_t *frag_block, k2g_counters *counters,
+                                const k2g_classify_params *params, uint32_t *call,
+                                uint32_t *hit_groups, uint32_t *hitlist_len, uint64_t *runs,
+                                uint64_t *n_runs, uint64_t *taxon_reads) {
   if (!db || !bases || !seq_off || !params || !call) return fail(K2G_ERR_ARG, "null argument");
+  if (counters && !frag_block) return fail(K2G_ERR_ARG, "counters need frag_block");
   if (runs && !n_runs) return fail(K2G_ERR_ARG, "runs given without n_runs capacity");
   const uint64_t runs_cap = runs ? *n_runs : 0;
   if (n_runs) *n_runs = 0;
@@ -145,8 +153,8 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
   const int per = params->paired ? 2 : 1;
   const uint64_t n_seqs = n_frags * per;
 
-  // chunk plan: ~256 MB of bases or 2M fragments per chunk
-  const uint64_t max_bases = 256ull << 20, max_frags = 2ull << 20;
+  // chunk plan: ~256 MB of bases (64 MB with hit events) or 2M fragments
+  const uint64_t max_bases = counters ? 64ull << 20 : 256ull << 20, max_frags = 2ull << 20;
   std::vector<uint64_t> cuts{0};
   {
     uint64_t f = 0;
@@ -155,6 +163,17 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
       uint64_t b0 = seq_off[f * per];
       while (g < n_frags && g - f < max_frags && seq_off[(g + 1) * per] - b0 <= max_bases) g++;
       if (g == f) g = f + 1;   // a single oversized fragment forms its own chunk
+      if (counters && g < n_frags) {
+        // end the chunk at the last block boundary; a block larger than a
+        // chunk forms its own chunk
+        uint64_t h = g;
+        while (h > f && frag_block[h] == frag_block[h - 1]) h--;
+        if (h == f) {
+          h = g;
+          while (h < n_frags && frag_block[h] == frag_block[h - 1]) h++;
+        }
+        g = h;
+      }
       cuts.push_back(g);
       f = g;
     }
@@ -187,6 +206,7 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
     }                                                       \
   } while (0)
   const uint64_t sparse_cap = chunk_bases + 2 * chunk_frags + 8;
+  const uint64_t hits_cap = counters ? chunk_bases + 4 * chunk_frags + 16 : 0;
   for (auto &s : slots) {
     SLOT_TRY(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
     SLOT_TRY(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
@@ -203,6 +223,13 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
     SLOT_TRY(cudaMalloc(&s.sums, ((chunk_frags + kScanBlock - 1) / kScanBlock + 1) * 8));
     SLOT_TRY(cudaMalloc(&s.total, 8));
     SLOT_TRY(cudaHostAlloc(&s.h_total, 8, cudaHostAllocDefault));
+    if (counters) {
+      SLOT_TRY(cudaMalloc(&s.hit_keys, hits_cap * 8));
+      SLOT_TRY(cudaMalloc(&s.hit_taxa, hits_cap * 4));
+      SLOT_TRY(cudaMalloc(&s.hit_order, hits_cap * 8));
+      SLOT_TRY(cudaMalloc(&s.hits_used, 8));
+      SLOT_TRY(cudaMalloc(&s.blocks, chunk_frags * 4));
+    }
   }
 
   uint64_t runs_written = 0;
@@ -255,8 +282,22 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
     rs.runs_cap = sparse_cap;
     rs.d_taxon_reads = reinterpret_cast<uint64_t *>(d_taxon_reads);
     rs.d_status = s.status;
+    if (counters) {
+      SLOT_TRY(cudaMemcpyAsync(s.blocks, frag_block + f0, nf * 4, cudaMemcpyHostToDevice, s.st));
+      SLOT_TRY(cudaMemsetAsync(s.hits_used, 0, 8, s.st));
+      rd.d_frag_block = s.blocks;
+      rs.d_hit_keys = s.hit_keys;
+      rs.d_hit_taxa = s.hit_taxa;
+      rs.d_hit_order = s.hit_order;
+      rs.hits_cap = hits_cap;
+      rs.d_hits_used = s.hits_used;
+    }
     status = k2g_classify(db, &rd, params, &rs, K2G_MODE_PIPELINED, s.st);
     if (status != K2G_OK) { cleanup(); return status; }
+    if (counters) {
+      status = k2g_counters_add(counters, &rd, &rs, s.st);
+      if (status != K2G_OK) { cleanup(); return status; }
+    }
     status = compact_runs(s.sparse, s.off, per, s.hlen, nf, s.excl, s.sums, s.total, s.dense, s.st);
     if (status != K2G_OK) { cleanup(); return status; }
     SLOT_TRY(cudaMemcpyAsync(s.h_total, s.total, 8, cudaMemcpyDeviceToHost, s.st));
@@ -288,4 +329,26 @@ extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, con
   cleanup();
   return K2G_OK;
 #undef SLOT_TRY
+}
+
+extern "C" k2g_status k2g_classify_host(const k2g_db *db, const char *bases, const char *quals,
+                                        const uint64_t *seq_off, uint64_t n_frags,
+                                        const k2g_classify_params *params, uint32_t *call,
+                                        uint32_t *hit_groups, uint32_t *hitlist_len,
+                                        uint64_t *runs, uint64_t *n_runs,
+                                        uint64_t *taxon_reads) {
+  return host_classify(db, bases, quals, seq_off, n_frags, nullptr, nullptr, params, call,
+                       hit_groups, hitlist_len, runs, n_runs, taxon_reads);
+}
+
+extern "C" k2g_status k2g_classify_host_blocks(const k2g_db *db, const char *bases,
+                                               const char *quals, const uint64_t *seq_off,
+                                               uint64_t n_frags, const uint32_t *frag_block,
+                                               k2g_counters *counters,
+                                               const k2g_classify_params *params, uint32_t *call,
+                                               uint32_t *hit_groups, uint32_t *hitlist_len,
+                                               uint64_t *runs, uint64_t *n_runs,
+                                               uint64_t *taxon_reads) {
+  return host_classify(db, bases, quals, seq_off, n_frags, frag_block, counters, params, call,
+                       hit_groups, hitlist_len, runs, n_runs, taxon_reads);
 }
