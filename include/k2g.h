@@ -267,11 +267,14 @@ uint64_t k2g_kernel_launches(void);
 /* ---- build: CompareAndSet with LCA merge (src/compact_hash.h:417-462,
  * src/build_db.h:187-194, :217-326) */
 
-/* Inserts (key, taxid) pairs with SetMinimizerLCA semantics.  ordered != 0
- * reproduces sequential insertion in list order (safe-prefix rounds of
- * src/build_db.h:286-321); ordered == 0 is the fast unordered insert of
- * ProcessSequenceFast (src/build_db.h:196-214), whose key->taxid map can
- * differ only when compacted keys collide along a probe path. */
+/* Inserts (key, taxid) pairs with SetMinimizerLCA semantics; pairs with
+ * taxid 0 are skipped.  ordered != 0 leaves exactly the table that
+ * sequential insertion in list order leaves (the order the reference's
+ * deterministic build fixes with its safe-prefix rounds,
+ * src/build_db.h:217-326); it needs a device copy of the table while it
+ * runs.  ordered == 0 is the fast unordered insert (ProcessSequenceFast,
+ * src/build_db.h:196-214), whose key->taxid map can differ only where
+ * compacted keys collide along a probe path.  Synchronises `stream`. */
 k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
                             uint64_t n, int ordered, void *stream);
 

@@ -1,6 +1,8 @@
 // Internal definitions shared by the host code and the CUDA kernels of libk2g.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -84,6 +86,9 @@ k2g_status fail(k2g_status s, const std::string &msg);
 k2g_status cuda_fail(int err, const char *what);
 // Counts each kernel launch issued by the library (k2g_kernel_launches).
 void note_launches(uint64_t n = 1);
+// One round (< 2^30 pairs) of the order-exact build insert (build_ordered.cu).
+k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
+                                uint64_t n, cudaStream_t st);
 }  // namespace k2g
 
 #define K2G_CUDA_TRY(call)                                        \

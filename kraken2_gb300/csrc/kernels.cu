@@ -653,9 +653,17 @@ extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const
                                        uint64_t n, int ordered, void *stream) {
   if (!db || (n && (!d_keys || !d_taxids))) return fail(K2G_ERR_ARG, "null argument");
   if (!n) return K2G_OK;
-  if (ordered) return fail(K2G_ERR_UNSUPPORTED, "ordered insert not available yet");
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   cudaStream_t st = (cudaStream_t)stream;
+  if (ordered) {
+    // sequential insertion of the whole list = rounds of it in order
+    const uint64_t round = (1ull << 30) - 1;
+    for (uint64_t i = 0; i < n; i += round) {
+      k2g_status s = build_insert_ordered(db, d_keys + i, d_taxids + i, std::min(round, n - i), st);
+      if (s != K2G_OK) return s;
+    }
+    return K2G_OK;
+  }
   uint32_t *d_status = nullptr;
   K2G_CUDA_TRY(cudaMalloc(&d_status, 4));
   K2G_CUDA_TRY(cudaMemsetAsync(d_status, 0, 4, st));

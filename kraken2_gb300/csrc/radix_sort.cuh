@@ -14,6 +14,8 @@
 
 namespace k2g {
 namespace rsort {
+// internal linkage: every translation unit that sorts gets its own kernels
+namespace {
 
 constexpr int kThreads = 256;
 constexpr int kPerThread = 16;
@@ -200,5 +202,6 @@ inline cudaError_t sort_u64(uint64_t *keys, uint64_t *alt, uint64_t n, int nbits
   return cudaSuccess;
 }
 
+}  // namespace
 }  // namespace rsort
 }  // namespace k2g
