@@ -248,6 +248,30 @@ k2g_status k2g_classify_host_blocks(const k2g_db *db, const char *bases, const c
                                     uint32_t *hit_groups, uint32_t *hitlist_len,
                                     uint64_t *runs, uint64_t *n_runs, uint64_t *taxon_reads);
 
+/* ---- serving: a resident database answering classification requests
+ * (no counterpart in the reference, which classifies one invocation's files).
+ * A worker thread batches queued requests as device capacity frees up
+ * (continuous batching; large requests are split over batches).  Device
+ * memory for request data is bounded by hbm_budget_bytes (two batch slots);
+ * requests wait in the queue until a slot is free.  Results equal
+ * k2g_classify_host's for the same reads, whatever else is in flight. */
+typedef struct k2g_server k2g_server;
+
+k2g_status k2g_server_create(const k2g_db *db, const k2g_classify_params *params,
+                             uint64_t hbm_budget_bytes, k2g_server **out);
+/* Copies the request (host buffers, layout as k2g_classify_host; quals only
+ * used when params->min_quality > 0) and returns at once with a ticket. */
+k2g_status k2g_server_submit(k2g_server *s, const char *bases, const char *quals,
+                             const uint64_t *seq_off, uint64_t n_frags, uint64_t *ticket);
+/* Waits up to timeout_s (0: just looks) for the request; *done = 1 when finished. */
+k2g_status k2g_server_wait(k2g_server *s, uint64_t ticket, double timeout_s, int *done);
+/* Copies a finished request's results out (any may be NULL; *n_runs: in =
+ * capacity of runs, out = used) and releases it; latency_s = submit to done. */
+k2g_status k2g_server_fetch(k2g_server *s, uint64_t ticket, uint32_t *call, uint32_t *hit_groups,
+                            uint32_t *hitlist_len, uint64_t *runs, uint64_t *n_runs,
+                            double *latency_s);
+k2g_status k2g_server_destroy(k2g_server *s);
+
 /* Pinned host memory helpers for callers that stage their own buffers. */
 k2g_status k2g_host_alloc(void **ptr, size_t bytes);
 k2g_status k2g_host_free(void *ptr);

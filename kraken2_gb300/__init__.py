@@ -39,7 +39,8 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_sector_gather",
            "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
            "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
-           "k2g_classify_host_blocks"]
+           "k2g_classify_host_blocks", "k2g_server_create", "k2g_server_submit",
+           "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy"]
 
 
 class K2GError(RuntimeError):
@@ -124,6 +125,11 @@ def lib():
             "k2g_counters_finish": [vp, vp, vp, vp, vp],
             "k2g_classify_host_blocks": [vp, vp, vp, vp, u64, vp, vp, C.POINTER(ClassifyParams),
                                          vp, vp, vp, vp, C.POINTER(u64), vp],
+            "k2g_server_create": [vp, C.POINTER(ClassifyParams), u64, C.POINTER(vp)],
+            "k2g_server_submit": [vp, vp, vp, vp, u64, C.POINTER(u64)],
+            "k2g_server_wait": [vp, u64, C.c_double, C.POINTER(i32)],
+            "k2g_server_fetch": [vp, u64, vp, vp, vp, vp, C.POINTER(u64), C.POINTER(C.c_double)],
+            "k2g_server_destroy": [vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -254,6 +260,51 @@ class Counters:
     def close(self):
         if self.h:
             lib().k2g_counters_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A classification service over a resident database (k2g_server)."""
+
+    def __init__(self, db: "Database", params: ClassifyParams, hbm_budget_bytes: int):
+        self.db = db
+        self.paired = bool(params.paired)
+        self.h = C.c_void_p()
+        check(lib().k2g_server_create(db.h, C.byref(params), int(hbm_budget_bytes),
+                                      C.byref(self.h)))
+
+    def submit(self, bases: bytes, seq_off: np.ndarray, n_frags: int, quals: bytes | None = None) -> int:
+        off = np.ascontiguousarray(seq_off, dtype=np.uint64)
+        t = C.c_uint64(0)
+        check(lib().k2g_server_submit(self.h, bases, quals, off.ctypes.data, n_frags, C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> bool:
+        done = C.c_int(0)
+        check(lib().k2g_server_wait(self.h, ticket, timeout_s, C.byref(done)))
+        return bool(done.value)
+
+    def fetch(self, ticket: int, n_frags: int, runs_cap: int):
+        """-> (call, hit_groups, hitlist_len, runs, latency_s)"""
+        call = np.zeros(n_frags, np.uint32)
+        hg = np.zeros(n_frags, np.uint32)
+        hl = np.zeros(n_frags, np.uint32)
+        runs = np.zeros(max(runs_cap, 1), np.uint64)
+        nr = C.c_uint64(len(runs))
+        lat = C.c_double(0)
+        check(lib().k2g_server_fetch(self.h, ticket, call.ctypes.data, hg.ctypes.data,
+                                     hl.ctypes.data, runs.ctypes.data, C.byref(nr), C.byref(lat)))
+        return call, hg, hl, runs[:nr.value], lat.value
+
+    def close(self):
+        if self.h:
+            lib().k2g_server_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):
