@@ -465,6 +465,344 @@ def kmer_parity(wl: Workload, cells: np.ndarray, mode: int, n_blocks: int = 5) -
     return {"reads": n, "taxa": int((ock > 0).sum()), "mismatches_vs_oracle": bad}
 
 
+def serving_pool(wl: Workload, n_reads: int, seed: int = 9):
+    """Host reads of the uneven-length mix: 5 in 6 of 150 bp, 1 in 6 of
+    log-normal length (mean 5 kb, clipped to 150 bp - 50 kb); 70% are
+    substrings of the source genomes, 30% uniform random."""
+    torch = wl.torch
+    rng = np.random.default_rng(seed)
+    sigma = 0.8
+    long_ = rng.random(n_reads) < 1 / 6
+    ln = rng.lognormal(np.log(5000) - sigma * sigma / 2, sigma, n_reads)
+    lens = np.where(long_, np.clip(ln, 150, 50_000), 150).astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    src_n = wl.src.numel()
+    starts = rng.integers(0, src_n - 50_001, n_reads)
+    from_src = rng.random(n_reads) < 0.7
+    bases = np.empty(int(off[-1]), np.uint8)
+    lut = torch.tensor(list(b"ACGT"), dtype=torch.uint8, device=wl.dev)
+    g = torch.Generator(device=wl.dev).manual_seed(seed)
+    chunk = 50_000
+    for r0 in range(0, n_reads, chunk):
+        r1 = min(n_reads, r0 + chunk)
+        ln_t = torch.from_numpy(lens[r0:r1]).to(wl.dev)
+        st_t = torch.from_numpy(starts[r0:r1]).to(wl.dev)
+        tot = int(ln_t.sum())
+        first = torch.cumsum(ln_t, 0) - ln_t
+        within = torch.arange(tot, device=wl.dev) - torch.repeat_interleave(first, ln_t)
+        seq = wl.src[torch.repeat_interleave(st_t, ln_t) + within]
+        rnd = lut[torch.randint(0, 4, (tot,), generator=g, device=wl.dev, dtype=torch.uint8).long()]
+        keep = torch.repeat_interleave(torch.from_numpy(from_src[r0:r1]).to(wl.dev), ln_t)
+        seq = torch.where(keep, seq, rnd)
+        bases[int(off[r0]):int(off[r1])] = seq.cpu().numpy()
+    return bases, off
+
+
+def serving_run(wl: Workload, log, budget_gb: float = 8.0, n_pool: int = 1_500_000,
+                seconds: float = 12.0, seed: int = 11) -> dict:
+    """k2g_server on the resident table: a burst for capacity, then a Poisson
+    stream of requests (log-uniform 1k-1M reads) at 70% of it."""
+    import threading
+    k2g, cfg = wl.k2g, wl.cfg
+    n_pool = min(n_pool, max(cfg.n_reads, 2_000_000))
+    bases, off = serving_pool(wl, n_pool)
+    log(f"serving pool: {n_pool} reads, {len(bases) / 1e9:.2f} Gbases")
+    params = k2g.ClassifyParams(cfg.confidence, cfg.min_hit_groups, 0, 0, 0)
+    sv = k2g.Server(wl.db, params, int(budget_gb * 1e9))
+    rng = np.random.default_rng(seed)
+    max_req = min(1_000_000, n_pool)
+
+    def request():
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(max_req))))
+        a = int(rng.integers(0, n_pool - n + 1))
+        return a, a + n
+
+    def submit(a, z):
+        return sv.submit(bases, off[a:z + 1], z - a)
+
+    def collect(items, out):
+        for t, (a, z) in items:
+            sv.wait(t, 600)
+            nb = int(off[z] - off[a])
+            *_, lat = sv.fetch(t, z - a, nb + 2 * (z - a) + 8)
+            out.append((z - a, lat))
+
+    # capacity: a burst of requests submitted at once
+    burst = [request() for _ in range(24)]
+    t0 = time.perf_counter()
+    tk = [(submit(a, z), (a, z)) for a, z in burst]
+    res = []
+    collect(tk, res)
+    burst_s = time.perf_counter() - t0
+    cap_reads_s = sum(n for n, _ in res) / burst_s
+    mean_req = (max_req - 1000) / np.log(max_req / 1000)
+    rate = 0.7 * cap_reads_s / mean_req                   # requests per second
+    # Poisson arrivals at 70% of capacity
+    arrivals = []
+    t = 0.0
+    while t < seconds:
+        t += rng.exponential(1 / rate)
+        arrivals.append((t, request()))
+    lock = threading.Lock()
+    pending = []
+    done = []
+    finished = threading.Event()
+
+    def collector():
+        while True:
+            with lock:
+                item = pending.pop(0) if pending else None
+            if item is None:
+                if finished.is_set():
+                    with lock:
+                        if not pending:
+                            return
+                time.sleep(0.0005)
+                continue
+            collect([item], done)
+
+    th = threading.Thread(target=collector)
+    th.start()
+    t_start = time.perf_counter()
+    for when, (a, z) in arrivals:
+        d = t_start + when - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        tkt = submit(a, z)
+        with lock:
+            pending.append((tkt, (a, z)))
+    finished.set()
+    th.join()
+    wall = time.perf_counter() - t_start
+    sv.close()
+    lats = np.array([l for _, l in done])
+    reads = sum(n for n, _ in done)
+    return {"workload": "Poisson arrivals at 70% of burst capacity; requests log-uniform "
+                        "1k-1M reads; lengths 5/6 x 150 bp + 1/6 log-normal mean 5 kb",
+            "hbm_budget_gb": budget_gb, "requests": len(done), "offered_req_per_s": round(rate, 2),
+            "reads_per_s": round(reads / wall), "burst_capacity_reads_per_s": round(cap_reads_s),
+            "latency_ms": {"p50": round(float(np.percentile(lats, 50)) * 1e3, 2),
+                           "p99": round(float(np.percentile(lats, 99)) * 1e3, 2),
+                           "max": round(float(lats.max()) * 1e3, 2)}}
+
+
+def _substitute(torch, seq, rate, g, lut):
+    """Uniform substitutions at the given rate (in place on a uint8 tensor)."""
+    hit = torch.rand(seq.numel(), generator=g, device=seq.device) < rate
+    n = int(hit.sum())
+    seq[hit] = lut[torch.randint(0, 4, (n,), generator=g, device=seq.device).long()]
+
+
+def _time_classify(wl, reads, res, params, mode, st):
+    torch = wl.torch
+    wl.db.classify(reads, params, res, mode=mode, stream=st)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(wl.stream)
+    wl.db.classify(reads, params, res, mode=mode, stream=st)
+    b.record(wl.stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def _gpu_buffers(torch, n, runs_cap, nodes):
+    z = lambda m, dt: torch.zeros(max(int(m), 1), dtype=dt, device="cuda")  # noqa: E731
+    return dict(call=z(n, torch.int32), hg=z(n, torch.int32), hoff=z(n, torch.int64),
+                hlen=z(n, torch.int32), runs=z(runs_cap, torch.int64), tr=z(nodes, torch.int64),
+                status=z(1, torch.int32))
+
+
+def _results(k2g, b, runs_cap):
+    return k2g.Results(b["call"].data_ptr(), b["hg"].data_ptr(), b["hoff"].data_ptr(),
+                       b["hlen"].data_ptr(), b["runs"].data_ptr(), runs_cap, b["tr"].data_ptr(),
+                       None, None, None, 0, None, b["status"].data_ptr())
+
+
+def _oracle_calls(wl, cells, bases, off, n_frags, paired, params):
+    import oracle
+    cfg = wl.cfg
+    o = oracle.Oracle(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, wl.parent,
+                      oracle.index_opts(cfg.k, cfg.l, spaced_mask(SEED_TEMPLATE), TOGGLE))
+    calls, *_ = o.classify(bases, None, off, n_frags, threads=os.cpu_count() or 1,
+                           confidence=params.confidence, min_hit_groups=params.min_hit_groups,
+                           paired=paired)
+    return calls
+
+
+def paired_and_uneven_run(log) -> dict:
+    """Paired 2 x 150 bp reads and an uneven-length mix on a 2 GB table
+    (0.5e9 cells, load 0.7): the batched path against the plain GPU form,
+    with oracle parity on a sample."""
+    import torch
+    cfg = Config(0.05)
+    cfg.n_reads = 100_000
+    wl = Workload(cfg, 0, log=lambda *a: None)
+    k2g = wl.k2g
+    st = wl.stream.cuda_stream
+    g = torch.Generator(device=wl.dev).manual_seed(21)
+    lut = torch.tensor(list(b"ACGT"), dtype=torch.uint8, device=wl.dev)
+    cells, _ = wl.db.download()
+    out = {"table": "0.5e9 cells (2 GB) at load 0.7, 50000 taxa"}
+
+    # -- 10M pairs of 2 x 150 bp, fragment length ~N(300, 50), 1% substitutions
+    n_pairs, L = 10_000_000, 150
+    frag = torch.clamp(torch.normal(300.0, 50.0, (n_pairs,), generator=g, device=wl.dev), 150, 600).long()
+    start = torch.randint(0, wl.src.numel() - 700, (n_pairs,), generator=g, device=wl.dev)
+    ar = torch.arange(L, device=wl.dev)
+    bases = torch.empty(n_pairs * 2 * L + 16, dtype=torch.uint8, device=wl.dev)
+    step = 2_000_000
+    for p0 in range(0, n_pairs, step):
+        p1 = min(n_pairs, p0 + step)
+        m1 = wl.src[start[p0:p1, None] + ar[None, :]]
+        m2 = wl.src[(start[p0:p1] + frag[p0:p1] - L)[:, None] + ar[None, :]]
+        bases[p0 * 2 * L:p1 * 2 * L] = torch.stack([m1, m2], 1).reshape(-1)
+    _substitute(torch, bases[:n_pairs * 2 * L], 0.01, g, lut)
+    bases[n_pairs * 2 * L:] = 0
+    params = k2g.ClassifyParams(0.1, 2, 0, 1, 0)
+    batch = 2_500_000
+    off = torch.arange(2 * batch + 1, dtype=torch.int64, device=wl.dev) * L
+    runs_cap = batch * (2 * L + 2) + 8
+    buf = _gpu_buffers(torch, batch, runs_cap, cfg.nodes)
+    res = _results(k2g, buf, runs_cap)
+
+    def run_pairs(mode, per_launch, sync):
+        t0 = time.perf_counter()
+        for b0 in range(0, n_pairs, per_launch):
+            n = min(per_launch, n_pairs - b0)
+            rd = k2g.Reads(d_bases=bases.data_ptr() + b0 * 2 * L, d_quals=None,
+                           d_seq_off=off.data_ptr(), n_frags=n, max_seq_len=L,
+                           total_bases=n * 2 * L, d_frag_block=None, frag_base=b0)
+            wl.db.classify(rd, params, res, mode=mode, stream=st)
+            if sync:
+                wl.stream.synchronize()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    run_pairs(k2g.MODE_PIPELINED, batch, False)
+    t_batched = run_pairs(k2g.MODE_PIPELINED, batch, False)
+    t_plain = run_pairs(k2g.MODE_PLAIN, 10_000, True)     # one launch per 10,000-pair reader batch
+    ns = 20_000
+    run_pairs(k2g.MODE_PIPELINED, batch, False)          # leaves the last batch's calls
+    rd = k2g.Reads(d_bases=bases.data_ptr(), d_quals=None, d_seq_off=off.data_ptr(), n_frags=ns,
+                   max_seq_len=L, total_bases=ns * 2 * L, d_frag_block=None, frag_base=0)
+    wl.db.classify(rd, params, res, mode=k2g.MODE_PIPELINED, stream=st)
+    torch.cuda.synchronize()
+    gcalls = buf["call"][:ns].cpu().numpy().view(np.uint32).astype(np.uint64)
+    ocalls = _oracle_calls(wl, cells, bases[:ns * 2 * L].cpu().numpy().tobytes(),
+                           np.arange(2 * ns + 1, dtype=np.uint64) * L, ns, True, params)
+    out["paired_2x150"] = {
+        "pairs": n_pairs, "confidence": 0.1, "fragment_len": "N(300, 50)", "substitutions": 0.01,
+        "mreads_min": round(n_pairs / t_batched * 60 / 1e6, 3),
+        "plain_mreads_min": round(n_pairs / t_plain * 60 / 1e6, 3),
+        "plain_form": "one synchronous launch per 10,000-pair reader batch",
+        "batched_over_plain": round(t_plain / t_batched, 3),
+        "parity": {"pairs": ns, "call_mismatches_vs_oracle": int((gcalls != ocalls).sum())}}
+    del bases, buf, res, off, frag, start
+    torch.cuda.empty_cache()
+
+    # -- uneven lengths: 1M log-normal (mean 5 kb, 150 bp - 50 kb) + 5M x 150 bp
+    rng = np.random.default_rng(23)
+    sigma = 0.8
+    lens = np.concatenate([np.clip(rng.lognormal(np.log(5000) - sigma * sigma / 2, sigma, 1_000_000),
+                                   150, 50_000).astype(np.int64), np.full(5_000_000, 150, np.int64)])
+    rng.shuffle(lens)
+    n = len(lens)
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    tot = int(offs[-1])
+    starts = torch.from_numpy(rng.integers(0, wl.src.numel() - 50_001, n)).to(wl.dev)
+    ln_t = torch.from_numpy(lens).to(wl.dev)
+    seqs = torch.empty(tot + 16, dtype=torch.uint8, device=wl.dev)
+    seqs[tot:] = 0
+    for r0 in range(0, n, 200_000):
+        r1 = min(n, r0 + 200_000)
+        l = ln_t[r0:r1]
+        first = torch.cumsum(l, 0) - l
+        within = torch.arange(int(l.sum()), device=wl.dev) - torch.repeat_interleave(first, l)
+        seqs[offs[r0]:offs[r1]] = wl.src[torch.repeat_interleave(starts[r0:r1], l) + within]
+    _substitute(torch, seqs[:tot], 0.04, g, lut)
+    d_off = torch.from_numpy(offs).to(wl.dev)
+    params = k2g.ClassifyParams(0.1, 2, 0, 0, 0)
+    runs_cap = tot + 2 * n + 8
+    buf = _gpu_buffers(torch, n, runs_cap, cfg.nodes)
+    res = _results(k2g, buf, runs_cap)
+    rd = k2g.Reads(d_bases=seqs.data_ptr(), d_quals=None, d_seq_off=d_off.data_ptr(), n_frags=n,
+                   max_seq_len=int(lens.max()), total_bases=tot, d_frag_block=None, frag_base=0)
+    t_batched = _time_classify(wl, rd, res, params, k2g.MODE_PIPELINED, st)
+    calls_b = buf["call"].cpu().numpy().copy()
+    t_plain = _time_classify(wl, rd, res, params, k2g.MODE_PLAIN, st)
+    same = bool(np.array_equal(calls_b, buf["call"].cpu().numpy()))
+    # oracle parity on a sample: the first 1,000 long and 4,000 short reads
+    idx = np.concatenate([np.nonzero(lens > 150)[0][:1000], np.nonzero(lens == 150)[0][:4000]])
+    host = seqs[:tot].cpu().numpy()
+    sb = b"".join(host[offs[i]:offs[i + 1]].tobytes() for i in idx)
+    soff = np.concatenate([[0], np.cumsum(lens[idx])]).astype(np.uint64)
+    ocalls = _oracle_calls(wl, cells, sb, soff, len(idx), False, params)
+    gcalls = calls_b.view(np.uint32)[idx].astype(np.uint64)
+    out["uneven_lengths"] = {
+        "reads": n, "bases": tot, "lengths": "1M log-normal mean 5 kb (150 bp - 50 kb) + 5M x 150 bp",
+        "errors": "4% substitutions", "single_launch": True,
+        "mreads_min": round(n / t_batched * 60 / 1e6, 3), "gbases_per_s": round(tot / t_batched / 1e9, 2),
+        "plain_mreads_min": round(n / t_plain * 60 / 1e6, 3),
+        "plain_form": "one launch, one thread per read (no work stealing)",
+        "batched_over_plain": round(t_plain / t_batched, 3), "plain_calls_identical": same,
+        "parity": {"reads": int(len(idx)), "call_mismatches_vs_oracle": int((gcalls != ocalls).sum())}}
+    del seqs, buf, res, d_off, wl
+    torch.cuda.empty_cache()
+    return out
+
+
+def build_run(log, n_pairs: int = 2_000_000_000, capacity: int = 5_000_000_000) -> dict:
+    """CompareAndSet-with-LCA build of n_pairs (key, taxid) pairs into a
+    capacity-cell table, unordered and order-exact; the order-exact insert is
+    checked cell for cell against the oracle's sequential insert on a
+    2e7-pair sample."""
+    import torch
+    import oracle
+    import kraken2_gb300 as k2g
+    nodes = 50_000
+    parent = random_taxonomy(nodes, 3)
+    opts = k2g.IndexOptions(35, 31, spaced_mask(SEED_TEMPLATE), TOGGLE, 1, 1, 0)
+    g = torch.Generator(device="cuda").manual_seed(31)
+    keys = torch.randint(0, 2**62, (n_pairs,), generator=g, device="cuda", dtype=torch.int64)
+    dup = torch.randint(0, n_pairs, (n_pairs // 10,), generator=g, device="cuda")
+    keys[torch.randint(0, n_pairs, (n_pairs // 10,), generator=g, device="cuda")] = keys[dup]
+    taxa = torch.randint(1, nodes, (n_pairs,), generator=g, device="cuda", dtype=torch.int32)
+    out = {"pairs": n_pairs, "table_gb": round(capacity * 4 / 1e9, 1), "key_bits": 16, "value_bits": 16,
+           "duplicates": "10% of pairs repeat another pair's key"}
+    for ordered in (False, True):
+        db = k2g.Database.create(opts, capacity, 16, 16, parent)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        db.build_insert(keys.data_ptr(), taxa.data_ptr(), n_pairs, ordered,
+                        torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out["ordered" if ordered else "unordered"] = {"s": round(dt, 3),
+                                                      "mpairs_per_s": round(n_pairs / dt / 1e6, 1),
+                                                      "size": db.info().size}
+        db.close()
+    del keys, taxa, dup
+    torch.cuda.empty_cache()
+    # exact check on a sample
+    ns, cap_s = 20_000_000, 50_000_003
+    keys = torch.randint(0, 2**62, (ns,), generator=g, device="cuda", dtype=torch.int64)
+    keys[torch.randint(0, ns, (ns // 10,), generator=g, device="cuda")] = keys[torch.randint(0, ns, (ns // 10,), generator=g, device="cuda")]
+    taxa = torch.randint(1, nodes, (ns,), generator=g, device="cuda", dtype=torch.int32)
+    db = k2g.Database.create(opts, cap_s, 16, 16, parent)
+    db.build_insert(keys.data_ptr(), taxa.data_ptr(), ns, True, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    cells, size = db.download()
+    db.close()
+    ref = np.zeros(cap_s, np.uint32)
+    osize = oracle.C.c_uint64(0)
+    hk = keys.cpu().numpy().view(np.uint64)
+    ht = taxa.cpu().numpy().view(np.uint32)
+    oracle.lib().ko_insert_lca(ref, cap_s, 16, 16, parent, hk, ht, ns, oracle.C.byref(osize))
+    out["parity"] = {"pairs": ns, "capacity": cap_s, "cells_differing": int((cells[:cap_s] != ref).sum()),
+                     "size_equal": bool(size == osize.value)}
+    return out
+
+
 def e2e_run(wl: Workload, n_reads: int, steps: int):
     """k2g_classify_host over pinned host buffers, copies inside the timing."""
     torch, cfg, k2g = wl.torch, wl.cfg, wl.k2g
@@ -680,6 +1018,13 @@ def run_ours(args, log):
     del cells
 
     e2e_t, h2d, d2h, e2e_calls = e2e_run(wl, cfg.e2e_reads, max(2, min(args.steps, 5)))
+    serving = None if args.skip_serving else serving_run(wl, log)
+    configs = None
+    if not args.skip_configs:
+        del runner
+        torch.cuda.empty_cache()
+        configs = paired_and_uneven_run(log)
+        configs["build"] = build_run(log)
     e2e_rate = cfg.e2e_reads / e2e_t
 
     out = {
@@ -726,6 +1071,8 @@ def run_ours(args, log):
                               "plain_form": "one synchronous launch per 3 MiB reader block",
                               "batched_over_plain": round(reads_s / plain, 3)} if plain else None),
         "minimizer_data": kmer,
+        "serving": serving,
+        "configs": configs,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -778,6 +1125,10 @@ def main():
                     help="fraction of the full-size workload (tests and probes only)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-configs", action="store_true",
+                    help="skip the paired, uneven-length and build measurements")
+    ap.add_argument("--skip-serving", action="store_true",
+                    help="skip the serving (Poisson request stream) measurement")
     ap.add_argument("--skip-kmer", action="store_true",
                     help="skip the -K (minimizer data) measurement")
     ap.add_argument("--profile", action="store_true",

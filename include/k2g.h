@@ -171,7 +171,10 @@ typedef enum {
   K2G_MODE_PLAIN = 0,         /* fused kernel, one thread per fragment      */
   K2G_MODE_PERSISTENT = 1,    /* fused kernel, work-stealing lanes          */
   K2G_MODE_PIPELINED = 2      /* scan / probe / resolve stages over
-                                 overlapping sub-batches (fastest)          */
+                                 overlapping sub-batches (fastest); long
+                                 fragments go to the fused kernel, and a
+                                 batch averaging over 512 bases per
+                                 fragment runs it as K2G_MODE_PERSISTENT   */
 } k2g_mode;
 
 /* Classifies a batch of fragments held in device memory. */

@@ -279,10 +279,14 @@ class Server:
         check(lib().k2g_server_create(db.h, C.byref(params), int(hbm_budget_bytes),
                                       C.byref(self.h)))
 
-    def submit(self, bases: bytes, seq_off: np.ndarray, n_frags: int, quals: bytes | None = None) -> int:
+    def submit(self, bases, seq_off: np.ndarray, n_frags: int, quals=None) -> int:
+        """bases / quals: bytes or a contiguous uint8 array; seq_off indexes them."""
+        def ptr(x):
+            return x.ctypes.data if isinstance(x, np.ndarray) else x
         off = np.ascontiguousarray(seq_off, dtype=np.uint64)
         t = C.c_uint64(0)
-        check(lib().k2g_server_submit(self.h, bases, quals, off.ctypes.data, n_frags, C.byref(t)))
+        check(lib().k2g_server_submit(self.h, ptr(bases), ptr(quals), off.ctypes.data, n_frags,
+                                      C.byref(t)))
         return t.value
 
     def wait(self, ticket: int, timeout_s: float = 60.0) -> bool:

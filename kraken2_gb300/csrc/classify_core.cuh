@@ -85,6 +85,9 @@ struct ClassifyArgs {
   unsigned long long *hits_used;
   uint32_t *status;
   // scheduling
+  const uint64_t *in_list;         // persistent lanes take fragments from this list
+  const unsigned long long *in_count;   // (its length, on the device) when set
+  uint64_t in_cap;
   unsigned long long *next_frag;   // persistent work counter
   unsigned long long *defer_count; // fragments whose taxon map overflowed
   uint64_t *defer_list;

@@ -42,8 +42,15 @@ __device__ __forceinline__ bool lane_fetch(Lane<W> &s, const ClassifyArgs &a, bo
     base = __shfl_sync(0xffffffffu, base, leader);
     if (need) {
       uint64_t f = base + __popc(m & ((1u << lane) - 1));
-      if (f < a.n_frags) lane_begin(s, a, f);
-      else exhausted = true;
+      if (a.in_list) {   // list mode: the fragments deferred by the pipeline
+        const uint64_t n = min((uint64_t)*a.in_count, a.in_cap);
+        if (f < n) lane_begin(s, a, a.in_list[f]);
+        else exhausted = true;
+      } else if (f < a.n_frags) {
+        lane_begin(s, a, f);
+      } else {
+        exhausted = true;
+      }
     }
   }
   return s.frag != ~0ull;

@@ -235,7 +235,7 @@ static void launch_scan(const ScanView &sv, const uint8_t *bases, const uint64_t
 struct ExecCtx {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
-  unsigned long long *counters = nullptr;   // [0] next_frag, [1] defer_count
+  unsigned long long *counters = nullptr;   // [0] next_frag, [1] defer_count, [2] defer2 count
   uint64_t *defer_list = nullptr;
   uint64_t defer_cap = 0;
   uint64_t *slow = nullptr;
@@ -258,6 +258,11 @@ struct DeviceState {
   cudaStream_t st = nullptr;      // all classification work of the device
   cudaEvent_t start = nullptr, done = nullptr;
   ExecCtx ctx[3];
+  // pipelined mode: fragments the pipeline defers (whole-batch indices), and
+  // what the fused kernel defers from those; counters [0] next, [1], [2] counts
+  uint64_t *defer = nullptr, *defer2 = nullptr;
+  uint64_t defer_cap = 0, defer2_cap = 0;
+  unsigned long long *counters = nullptr;
 };
 static DeviceState g_state[64];
 
@@ -274,7 +279,7 @@ static cudaError_t grow(T *&p, uint64_t &cap, uint64_t want) {
 
 static k2g_status ctx_reserve(ExecCtx &c, uint64_t frags, uint64_t slots, size_t slow_bytes,
                               bool pipeline, bool keys) {
-  if (!c.counters) K2G_CUDA_TRY(cudaMalloc(&c.counters, 2 * sizeof(unsigned long long)));
+  if (!c.counters) K2G_CUDA_TRY(cudaMalloc(&c.counters, 3 * sizeof(unsigned long long)));
   K2G_CUDA_TRY(grow(c.defer_list, c.defer_cap, std::max<uint64_t>(1024, frags)));
   if (c.slow_bytes < slow_bytes) {
     if (c.slow) cudaFree(c.slow);
@@ -378,9 +383,10 @@ static void sub_batch_plan(uint64_t n, uint64_t total_bases, int per, uint64_t m
   sb_frags = std::max<uint64_t>(kPipeBlock, sb_frags / kPipeBlock * kPipeBlock);
   sb_frags = std::min<uint64_t>(sb_frags, n);
   // Twice the average sub-batch, and room for at least a block of the
-  // longest fragments; fragments beyond the capacity take the slow path.
+  // longest fragments the pipeline keeps; fragments beyond the capacity go
+  // to the fused kernel.
   cap_slots = (uint64_t)(2.0 * avg * sb_frags) + 2 * sb_frags +
-              (uint64_t)kPipeBlock * (per * max_len + 2) + 64;
+              (uint64_t)kPipeBlock * (std::min<uint64_t>(per * max_len, kPipeLongFrag) + 2) + 64;
 }
 
 // The view of sub-batch [f0, f0 + n) of a batch, bound to context c.
@@ -396,6 +402,9 @@ static ClassifyArgs sub_view(const ClassifyArgs &a0, uint64_t f0, uint64_t n, co
   if (a0.hit_groups) a.hit_groups = a0.hit_groups + f0;
   if (a0.hitlist_off) a.hitlist_off = a0.hitlist_off + f0;
   if (a0.hitlist_len) a.hitlist_len = a0.hitlist_len + f0;
+  a.in_list = nullptr;
+  a.in_count = nullptr;
+  a.in_cap = 0;
   a.next_frag = c.counters;
   a.defer_count = c.counters + 1;
   a.defer_list = c.defer_list;
@@ -432,7 +441,14 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     ds.init = true;
   }
   const int per = a0.cls.paired ? 2 : 1;
-  const bool pipeline = mode == K2G_MODE_PIPELINED;
+  // The pipeline is fastest on short fragments.  A batch whose fragments
+  // average more than kPipeMaxAvg bases (mates together) is mostly long
+  // fragments, which the fused persistent kernel walks in segments with work
+  // stealing; the pipeline would defer most of them to it anyway.
+  constexpr double kPipeMaxAvg = 512.0;
+  const bool pipeline = mode == K2G_MODE_PIPELINED &&
+                        (double)total_bases <= kPipeMaxAvg * (double)a0.n_frags;
+  if (mode == K2G_MODE_PIPELINED && !pipeline) mode = K2G_MODE_PERSISTENT;
   uint64_t sb = a0.n_frags, cap_slots = 0;
   if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, sb, cap_slots);
   const SlowPlan sp = slow_plan(max_len, a0.cls.paired != 0);
@@ -450,7 +466,34 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
     return dispatch_slow(sub_view(a0, f0, n, c, sp), sp.mcap, (unsigned)(sp.threads / 128), 128, st);
   };
+  // Pipelined mode: the fragments the pipeline deferred (long ones, and
+  // those whose staging or taxon map overflowed) go to the fused kernel as
+  // one list after the last beat, so its work stealing spreads the long
+  // ones over the whole device; what that kernel defers goes to the slow
+  // kernel.
+  auto deferred = [&]() -> cudaError_t {
+    ClassifyArgs a = a0;
+    a.in_list = ds.defer;
+    a.in_count = ds.counters + 1;
+    a.in_cap = ds.defer_cap;
+    a.next_frag = ds.counters;
+    a.defer_list = ds.defer2;
+    a.defer_count = ds.counters + 2;
+    a.defer_cap = ds.defer2_cap;
+    a.frag_list = ds.defer2;
+    a.scratch = ds.ctx[0].slow;
+    a.scratch_stride = sp.stride;
+    cudaError_t e = dispatch_fast(a, 1, sm_count(dev), st);
+    if (e != cudaSuccess) return e;
+    a.in_list = nullptr;
+    return dispatch_slow(a, sp.mcap, (unsigned)(sp.threads / 128), 128, st);
+  };
+
   if (pipeline) {
+    K2G_CUDA_TRY(grow(ds.defer, ds.defer_cap, std::max<uint64_t>(1024, a0.n_frags)));
+    K2G_CUDA_TRY(grow(ds.defer2, ds.defer2_cap, std::max<uint64_t>(1024, a0.n_frags)));
+    if (!ds.counters) K2G_CUDA_TRY(cudaMalloc(&ds.counters, 3 * sizeof(unsigned long long)));
+    K2G_CUDA_TRY(cudaMemsetAsync(ds.counters, 0, 3 * sizeof(unsigned long long), st));
     // beat t: scan t, probe t-1, resolve t-2
     for (uint64_t t = 0; t < S + 2; t++) {
       StepArgs sa{};
@@ -462,19 +505,19 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
         const ExecCtx &c = ds.ctx[i % 3];
         const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
         p = pipe_view(sub_view(a0, f0, n, c, sp), c);
+        p.a.defer_list = ds.defer;   // one list for the whole batch
+        p.a.defer_count = ds.counters + 1;
+        p.a.defer_cap = ds.defer_cap;
         nb = (uint32_t)((n + kPipeBlock - 1) / kPipeBlock);
       };
-      if (t < S) {
-        K2G_CUDA_TRY(cudaMemsetAsync(ds.ctx[t % 3].counters, 0, 2 * sizeof(unsigned long long), st));
-        bind(t, sa.scan, sa.n_scan);
-      }
+      if (t < S) bind(t, sa.scan, sa.n_scan);
       if (t >= 1 && t - 1 < S) bind(t - 1, sa.probe, sa.n_probe);
       if (t >= 2 && t - 2 < S) bind(t - 2, sa.resolve, sa.n_resolve);
       if (!sa.n_scan) sa.scan = sa.probe.a.n_frags ? sa.probe : sa.resolve;   // scan config for dispatch
       if (!sa.n_scan) sa.scan.a.n_frags = 0;
       K2G_CUDA_TRY(dispatch_pipe_step(sa, st));
-      if (t >= 2 && t - 2 < S) K2G_CUDA_TRY(slow(t - 2));
     }
+    K2G_CUDA_TRY(deferred());
   } else {
     for (uint64_t i = 0; i < S; i++) {
       const ExecCtx &c = ds.ctx[0];

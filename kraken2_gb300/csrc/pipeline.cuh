@@ -28,6 +28,7 @@
 namespace k2g {
 
 constexpr int kPipeBlock = 128;     // fragments per scan / resolve block
+constexpr uint64_t kPipeLongFrag = 2048;   // bases (both mates) handled in the pipeline
 constexpr int kStage = 16;          // staged keys per lane (one chunk)
 
 struct PipeArgs {
@@ -162,11 +163,13 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
     s.glen = 0;
     s.ng = 0;
     s.gbase = o0 - a.seq_off[0] + 2 * f;
-    // a fragment that does not fit the slot capacity goes to the slow path
+    // A long fragment (one thread would hold its block's beat for its whole
+    // length) or one that does not fit the slot capacity is handed to the
+    // fused kernel, which walks it in segments with work stealing.
     const uint64_t need = (per == 2 ? (uint64_t)(a.seq_off[f * per + 2] - o0) : (uint64_t)(o1 - o0)) + 2;
-    if (s.gbase + need > pa.cap_slots) {
+    if (need > kPipeLongFrag || s.gbase + need > pa.cap_slots) {
       unsigned long long at = atomicAdd(a.defer_count, 1ull);
-      if (at < a.defer_cap) a.defer_list[at] = f;
+      if (at < a.defer_cap) a.defer_list[at] = f + a.frag_off;   // index in the whole batch
       else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
       pa.gcount[f] = 0xFFFFFFFFu;
       s.done = true;
@@ -397,7 +400,7 @@ __device__ __forceinline__ void pipe_resolve_body(const PipeArgs &pa, uint32_t b
       }
       if (taxon && !map_add(st, s.distinct, taxon, len)) {
         unsigned long long at = atomicAdd(a.defer_count, 1ull);
-        if (at < a.defer_cap) a.defer_list[at] = f;
+        if (at < a.defer_cap) a.defer_list[at] = f + a.frag_off;   // index in the whole batch
         else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
         done = false;
       }
