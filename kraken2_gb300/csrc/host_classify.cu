@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "k2g_internal.h"
@@ -103,6 +104,9 @@ using namespace k2g;
 
 namespace {
 
+// Device buffers of one chunk in flight.  They are kept per device across
+// calls (grown when a call needs more), so a call allocates nothing once
+// the sizes have been seen.
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
@@ -115,21 +119,85 @@ struct Slot {
   // add_kmer events (only with counters)
   uint64_t *hit_keys = nullptr, *hit_order = nullptr, *hits_used = nullptr;
   uint32_t *hit_taxa = nullptr, *blocks = nullptr;
+  uint64_t cap_bases = 0, cap_frags = 0, cap_quals = 0, cap_hits = 0;
   // chunk bookkeeping for the deferred runs copy
   bool pending = false;
   uint64_t f0 = 0, nf = 0;
 };
 
-void free_slot(Slot &s) {
-  if (s.st) cudaStreamSynchronize(s.st);
-  void *dev[] = {s.bases, s.quals, s.off, s.call, s.hg, s.hlen, s.status, s.sparse,
-                 s.dense, s.excl, s.sums, s.total, s.hit_keys, s.hit_order, s.hits_used,
-                 s.hit_taxa, s.blocks};
-  for (void *p : dev)
-    if (p) cudaFree(p);
-  if (s.h_total) cudaFreeHost(s.h_total);
-  if (s.done) cudaEventDestroy(s.done);
-  if (s.st) cudaStreamDestroy(s.st);
+struct HostCache {
+  std::mutex mu;
+  Slot slots[2];
+  unsigned long long *taxon_reads = nullptr;
+  uint64_t taxon_cap = 0;
+};
+HostCache g_host[64];
+
+template <class T>
+cudaError_t regrow(T *&p, uint64_t n) {
+  if (p) cudaFree(p);
+  p = nullptr;
+  return cudaMalloc(&p, std::max<uint64_t>(n, 1) * sizeof(T));
+}
+
+// Makes the slot hold chunks of up to fb fragments / bb bases.
+cudaError_t fit_slot(Slot &s, uint64_t bb, uint64_t fb, int per, bool quals, uint64_t hits) {
+  cudaError_t e;
+#define TRY(x) if ((e = (x)) != cudaSuccess) return e
+  if (!s.st) {
+    TRY(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    TRY(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    TRY(cudaHostAlloc(&s.h_total, 8, cudaHostAllocDefault));
+    TRY(cudaMalloc(&s.status, 4));
+    TRY(cudaMalloc(&s.total, 8));
+    TRY(cudaMalloc(&s.hits_used, 8));
+  }
+  if (bb > s.cap_bases || fb > s.cap_frags) {
+    bb = std::max(bb, s.cap_bases);
+    fb = std::max(fb, s.cap_frags);
+    const uint64_t sparse_cap = bb + 2 * fb + 8;
+    TRY(regrow(s.bases, bb + 16));
+    TRY(regrow(s.off, fb * 2 + 1));
+    TRY(regrow(s.call, fb));
+    TRY(regrow(s.hg, fb));
+    TRY(regrow(s.hlen, fb));
+    TRY(regrow(s.sparse, sparse_cap));
+    TRY(regrow(s.dense, sparse_cap));
+    TRY(regrow(s.excl, fb));
+    TRY(regrow(s.sums, (fb + kScanBlock - 1) / kScanBlock + 1));
+    TRY(regrow(s.blocks, fb));
+    s.cap_bases = bb;
+    s.cap_frags = fb;
+    s.cap_quals = 0;
+    s.cap_hits = 0;
+  }
+  if (quals && s.cap_quals < s.cap_bases) {
+    TRY(regrow(s.quals, s.cap_bases + 16));
+    s.cap_quals = s.cap_bases;
+  }
+  if (hits > s.cap_hits) {
+    TRY(regrow(s.hit_keys, hits));
+    TRY(regrow(s.hit_taxa, hits));
+    TRY(regrow(s.hit_order, hits));
+    s.cap_hits = hits;
+  }
+#undef TRY
+  (void)per;
+  return cudaSuccess;
+}
+
+// Largest g in [f, n] with seq_off[g * per] - seq_off[f * per] <= max_bases
+// (offsets are non-decreasing).
+uint64_t cut_by_bases(const uint64_t *seq_off, int per, uint64_t f, uint64_t n,
+                      uint64_t max_bases) {
+  const uint64_t b0 = seq_off[f * per];
+  uint64_t lo = f, hi = n;
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo + 1) / 2;
+    if (seq_off[mid * per] - b0 <= max_bases) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
 }  // namespace
@@ -151,85 +219,53 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
   if (!n_frags) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   const int per = params->paired ? 2 : 1;
-  const uint64_t n_seqs = n_frags * per;
 
   // chunk plan: ~256 MB of bases (64 MB with hit events) or 2M fragments
   const uint64_t max_bases = counters ? 64ull << 20 : 256ull << 20, max_frags = 2ull << 20;
   std::vector<uint64_t> cuts{0};
-  {
-    uint64_t f = 0;
-    while (f < n_frags) {
-      uint64_t g = f;
-      uint64_t b0 = seq_off[f * per];
-      while (g < n_frags && g - f < max_frags && seq_off[(g + 1) * per] - b0 <= max_bases) g++;
-      if (g == f) g = f + 1;   // a single oversized fragment forms its own chunk
-      if (counters && g < n_frags) {
-        // end the chunk at the last block boundary; a block larger than a
-        // chunk forms its own chunk
-        uint64_t h = g;
-        while (h > f && frag_block[h] == frag_block[h - 1]) h--;
-        if (h == f) {
-          h = g;
-          while (h < n_frags && frag_block[h] == frag_block[h - 1]) h++;
-        }
-        g = h;
+  while (cuts.back() < n_frags) {
+    const uint64_t f = cuts.back();
+    uint64_t g = std::min(cut_by_bases(seq_off, per, f, n_frags, max_bases), f + max_frags);
+    if (g == f) g = f + 1;   // a single oversized fragment forms its own chunk
+    if (counters && g < n_frags) {
+      // end the chunk at the last block boundary; a block larger than a
+      // chunk forms its own chunk
+      uint64_t h = g;
+      while (h > f && frag_block[h] == frag_block[h - 1]) h--;
+      if (h == f) {
+        h = g;
+        while (h < n_frags && frag_block[h] == frag_block[h - 1]) h++;
       }
-      cuts.push_back(g);
-      f = g;
+      g = h;
     }
+    cuts.push_back(g);
   }
-  uint64_t chunk_frags = 0, chunk_bases = 0, max_len = 0;
+  uint64_t chunk_frags = 0, chunk_bases = 0;
   for (size_t c = 0; c + 1 < cuts.size(); c++) {
     chunk_frags = std::max(chunk_frags, cuts[c + 1] - cuts[c]);
     chunk_bases = std::max(chunk_bases, seq_off[cuts[c + 1] * per] - seq_off[cuts[c] * per]);
   }
-  for (uint64_t i = 0; i < n_seqs; i++) max_len = std::max(max_len, seq_off[i + 1] - seq_off[i]);
+  const uint64_t hits_cap = counters ? chunk_bases + 4 * chunk_frags + 16 : 0;
 
-  unsigned long long *d_taxon_reads = nullptr;
-  if (taxon_reads) {
-    K2G_CUDA_TRY(cudaMalloc(&d_taxon_reads, db->node_count * 8));
-    K2G_CUDA_TRY(cudaMemset(d_taxon_reads, 0, db->node_count * 8));
-  }
-  Slot slots[2];
+  HostCache &hc = g_host[db->device & 63];
+  std::lock_guard<std::mutex> lock(hc.mu);
+  Slot *slots = hc.slots;
   k2g_status status = K2G_OK;
-  auto cleanup = [&]() {
-    for (auto &s : slots) free_slot(s);
-    if (d_taxon_reads) cudaFree(d_taxon_reads);
-  };
 #define SLOT_TRY(call_)                                     \
   do {                                                      \
     cudaError_t _e = (call_);                               \
-    if (_e != cudaSuccess) {                                \
-      status = cuda_fail((int)_e, #call_);                  \
-      cleanup();                                            \
-      return status;                                        \
-    }                                                       \
+    if (_e != cudaSuccess) return cuda_fail((int)_e, #call_); \
   } while (0)
-  const uint64_t sparse_cap = chunk_bases + 2 * chunk_frags + 8;
-  const uint64_t hits_cap = counters ? chunk_bases + 4 * chunk_frags + 16 : 0;
-  for (auto &s : slots) {
-    SLOT_TRY(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
-    SLOT_TRY(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
-    SLOT_TRY(cudaMalloc(&s.bases, chunk_bases + 16));
-    if (quals) SLOT_TRY(cudaMalloc(&s.quals, chunk_bases + 16));
-    SLOT_TRY(cudaMalloc(&s.off, (chunk_frags * per + 1) * 8));
-    SLOT_TRY(cudaMalloc(&s.call, chunk_frags * 4));
-    SLOT_TRY(cudaMalloc(&s.hg, chunk_frags * 4));
-    SLOT_TRY(cudaMalloc(&s.hlen, chunk_frags * 4));
-    SLOT_TRY(cudaMalloc(&s.status, 4));
-    SLOT_TRY(cudaMalloc(&s.sparse, sparse_cap * 8));
-    SLOT_TRY(cudaMalloc(&s.dense, sparse_cap * 8));
-    SLOT_TRY(cudaMalloc(&s.excl, chunk_frags * 8));
-    SLOT_TRY(cudaMalloc(&s.sums, ((chunk_frags + kScanBlock - 1) / kScanBlock + 1) * 8));
-    SLOT_TRY(cudaMalloc(&s.total, 8));
-    SLOT_TRY(cudaHostAlloc(&s.h_total, 8, cudaHostAllocDefault));
-    if (counters) {
-      SLOT_TRY(cudaMalloc(&s.hit_keys, hits_cap * 8));
-      SLOT_TRY(cudaMalloc(&s.hit_taxa, hits_cap * 4));
-      SLOT_TRY(cudaMalloc(&s.hit_order, hits_cap * 8));
-      SLOT_TRY(cudaMalloc(&s.hits_used, 8));
-      SLOT_TRY(cudaMalloc(&s.blocks, chunk_frags * 4));
+  for (int i = 0; i < 2; i++)
+    SLOT_TRY(fit_slot(slots[i], chunk_bases, chunk_frags, per, quals != nullptr, hits_cap));
+  unsigned long long *d_taxon_reads = nullptr;
+  if (taxon_reads) {
+    if (hc.taxon_cap < db->node_count) {
+      SLOT_TRY(regrow(hc.taxon_reads, db->node_count));
+      hc.taxon_cap = db->node_count;
     }
+    d_taxon_reads = hc.taxon_reads;
+    SLOT_TRY(cudaMemset(d_taxon_reads, 0, db->node_count * 8));
   }
 
   uint64_t runs_written = 0;
@@ -252,13 +288,24 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
     runs_written += nr;
     return K2G_OK;
   };
+  // On an error, let the chunks in flight finish before the slots are reused.
+  auto settle = [&]() {
+    for (int i = 0; i < 2; i++) {
+      if (slots[i].st) cudaStreamSynchronize(slots[i].st);
+      slots[i].pending = false;
+    }
+  };
 
   for (size_t c = 0; c + 1 < cuts.size(); c++) {
     Slot &s = slots[c & 1];
     status = drain(s);
-    if (status != K2G_OK) { cleanup(); return status; }
+    if (status != K2G_OK) { settle(); return status; }
     const uint64_t f0 = cuts[c], nf = cuts[c + 1] - f0;
     const uint64_t b0 = seq_off[f0 * per], nb = seq_off[(f0 + nf) * per] - b0;
+    // longest sequence of this chunk (overlaps the previous chunk's work)
+    uint64_t max_len = 0;
+    for (uint64_t i = f0 * per; i < (f0 + nf) * per; i++)
+      max_len = std::max(max_len, seq_off[i + 1] - seq_off[i]);
     SLOT_TRY(cudaMemcpyAsync(s.bases, bases + b0, nb, cudaMemcpyHostToDevice, s.st));
     if (quals) SLOT_TRY(cudaMemcpyAsync(s.quals, quals + b0, nb, cudaMemcpyHostToDevice, s.st));
     SLOT_TRY(cudaMemcpyAsync(s.off, seq_off + f0 * per, (nf * per + 1) * 8,
@@ -279,7 +326,7 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
     rs.d_hit_groups = s.hg;
     rs.d_hitlist_len = s.hlen;
     rs.d_runs = s.sparse;
-    rs.runs_cap = sparse_cap;
+    rs.runs_cap = s.cap_bases + 2 * s.cap_frags + 8;
     rs.d_taxon_reads = reinterpret_cast<uint64_t *>(d_taxon_reads);
     rs.d_status = s.status;
     if (counters) {
@@ -289,17 +336,17 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
       rs.d_hit_keys = s.hit_keys;
       rs.d_hit_taxa = s.hit_taxa;
       rs.d_hit_order = s.hit_order;
-      rs.hits_cap = hits_cap;
+      rs.hits_cap = s.cap_hits;
       rs.d_hits_used = s.hits_used;
     }
     status = k2g_classify(db, &rd, params, &rs, K2G_MODE_PIPELINED, s.st);
-    if (status != K2G_OK) { cleanup(); return status; }
+    if (status != K2G_OK) { settle(); return status; }
     if (counters) {
       status = k2g_counters_add(counters, &rd, &rs, s.st);
-      if (status != K2G_OK) { cleanup(); return status; }
+      if (status != K2G_OK) { settle(); return status; }
     }
     status = compact_runs(s.sparse, s.off, per, s.hlen, nf, s.excl, s.sums, s.total, s.dense, s.st);
-    if (status != K2G_OK) { cleanup(); return status; }
+    if (status != K2G_OK) { settle(); return status; }
     SLOT_TRY(cudaMemcpyAsync(s.h_total, s.total, 8, cudaMemcpyDeviceToHost, s.st));
     SLOT_TRY(cudaMemcpyAsync(call + f0, s.call, nf * 4, cudaMemcpyDeviceToHost, s.st));
     if (hit_groups)
@@ -313,20 +360,18 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
     // keep chunk order for the runs: drain the other slot (older chunk) now
     Slot &o = slots[(c + 1) & 1];
     status = drain(o);
-    if (status != K2G_OK) { cleanup(); return status; }
+    if (status != K2G_OK) { settle(); return status; }
   }
   for (size_t c = cuts.size() - 1; c < cuts.size() + 1; c++) {
     status = drain(slots[c & 1]);
-    if (status != K2G_OK) { cleanup(); return status; }
+    if (status != K2G_OK) { settle(); return status; }
   }
   if (taxon_reads) {
     std::vector<uint64_t> tr(db->node_count);
-    cudaError_t e = cudaMemcpy(tr.data(), d_taxon_reads, db->node_count * 8, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) { status = cuda_fail(e, "taxon reads"); cleanup(); return status; }
+    SLOT_TRY(cudaMemcpy(tr.data(), d_taxon_reads, db->node_count * 8, cudaMemcpyDeviceToHost));
     for (uint64_t i = 0; i < db->node_count; i++) taxon_reads[i] += tr[i];
   }
   if (n_runs) *n_runs = runs_written;
-  cleanup();
   return K2G_OK;
 #undef SLOT_TRY
 }

@@ -280,6 +280,70 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
   }
 }
 
+// Probe with the sector loads landing in shared memory (cp.async): each
+// thread keeps kProbeSlots sectors in flight without holding them in
+// registers, in a rolling pipeline -- wait for the oldest, resolve it, issue
+// the next key into its slot.  Probe blocks have the step kernel's shared
+// memory to themselves.
+#ifndef K2G_PROBE_SLOTS
+#define K2G_PROBE_SLOTS 6
+#endif
+constexpr int kProbeSlots = K2G_PROBE_SLOTS;
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void pipe_probe_body_async(const PipeArgs &pa, uint32_t blk,
+                                                      unsigned char *smem) {
+  constexpr int D = kProbeSlots;
+  const uint64_t f0 = (uint64_t)blk * kPipeBlock;
+  const uint64_t rbase = pipe_gbase(pa, f0);
+  const uint32_t cnt = pa.bcount[blk];
+  const TableView &t = pa.a.table;
+  uint4 *slots = reinterpret_cast<uint4 *>(smem);   // [D][kPipeBlock][2]
+  uint64_t hc[D];
+  auto issue = [&](int d, uint32_t i) {
+    hc[d] = murmur3(pa.rkey[rbase + i]);
+    const uint4 *src = reinterpret_cast<const uint4 *>(t.cells + (fast_mod(hc[d], t.div) & ~7ull));
+    uint4 *dst = slots + ((size_t)d * kPipeBlock + threadIdx.x) * 2;
+    cp_async16(dst, src);
+    cp_async16(dst + 1, src + 1);
+  };
+#pragma unroll
+  for (int d = 0; d < D; d++) {
+    const uint32_t i = threadIdx.x + d * kPipeBlock;
+    if (i < cnt) issue(d, i);
+    cp_async_commit();
+  }
+  for (uint32_t j0 = 0; threadIdx.x + j0 * kPipeBlock < cnt; j0 += D) {
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      const uint32_t i = threadIdx.x + (j0 + d) * kPipeBlock;
+      cp_async_wait<D - 1>();   // the group of key j0 + d has landed
+      if (i < cnt) {
+        const uint4 *src = slots + ((size_t)d * kPipeBlock + threadIdx.x) * 2;
+        Sector sec;
+        sec.lo = src[0];
+        sec.hi = src[1];
+        const uint32_t slot = pa.rslot[rbase + i];
+        pa.gtax[rbase + slot] = probe_sectors(t, hc[d], fast_mod(hc[d], t.div), sec);
+        if (pa.gkey) pa.gkey[rbase + slot] = pa.rkey[rbase + i];
+      }
+      const uint32_t in = i + D * kPipeBlock;
+      if (in < cnt) issue(d, in);
+      cp_async_commit();
+    }
+  }
+  cp_async_wait<0>();
+}
+
 // Taxon map of one resolve thread in shared memory, interleaved by thread.
 struct ResolveMap {
   static constexpr int kMapResolve = 16;
@@ -429,15 +493,28 @@ struct StepArgs {
   uint32_t n_scan, n_probe, n_resolve;   // blocks per role
 };
 
+#ifndef K2G_PROBE_ASYNC
+#define K2G_PROBE_ASYNC 0
+#endif
+
+// Resident blocks per SM the register allocation is fitted to.
+#ifndef K2G_PIPE_MIN_BLOCKS
+#define K2G_PIPE_MIN_BLOCKS 6
+#endif
+
 template <int W, bool QUAL, bool RC1>
-__global__ void __launch_bounds__(kPipeBlock, 6)
+__global__ void __launch_bounds__(kPipeBlock, K2G_PIPE_MIN_BLOCKS)
 pipe_step_kernel(StepArgs sa) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t role = blockIdx.x % 3, blk = blockIdx.x / 3;
   if (role == 0) {
     if (blk < sa.n_scan) pipe_scan_body<W, QUAL, RC1>(sa.scan, blk, smem);
   } else if (role == 1) {
+#if K2G_PROBE_ASYNC
+    if (blk < sa.n_probe) pipe_probe_body_async(sa.probe, blk, smem);
+#else
     if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk);
+#endif
   } else {
     if (blk < sa.n_resolve) pipe_resolve_body(sa.resolve, blk, smem);
   }
@@ -447,8 +524,10 @@ template <int W, bool QUAL, bool RC1>
 cudaError_t launch_pipe_step(const StepArgs &sa, cudaStream_t st) {
   const uint32_t most = max(sa.n_scan, max(sa.n_probe, sa.n_resolve));
   if (!most) return cudaSuccess;
-  const size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
-                          ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
+  size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
+                    ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
+  if (K2G_PROBE_ASYNC && smem < (size_t)kProbeSlots * kPipeBlock * 32)
+    smem = (size_t)kProbeSlots * kPipeBlock * 32;
   pipe_step_kernel<W, QUAL, RC1><<<3 * most, kPipeBlock, smem, st>>>(sa);
   note_launches();
   return cudaGetLastError();
