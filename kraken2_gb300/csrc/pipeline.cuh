@@ -250,18 +250,28 @@ namespace k2g {
 
 // Probe: every record of a scan block, several table loads in flight per
 // thread, result stored at the record's group slot.
-__device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk) {
+// Probe blocks per scan block: each takes every kProbeSplit-th run of
+// kPipeBlock keys of the scan block's range.  Two keep more probe warps
+// resident beside the scan and resolve blocks (measured +3% at 40 GB).
+#ifndef K2G_PROBE_SPLIT
+#define K2G_PROBE_SPLIT 2
+#endif
+constexpr int kProbeSplit = K2G_PROBE_SPLIT;
+
+__device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk,
+                                                uint32_t part = 0) {
   constexpr int B = 4;
+  constexpr uint32_t stride = kProbeSplit * kPipeBlock;
   const uint64_t f0 = (uint64_t)blk * kPipeBlock;
   const uint64_t rbase = pipe_gbase(pa, f0);
   const uint32_t cnt = pa.bcount[blk];
   const TableView &t = pa.a.table;
-  for (uint32_t i0 = threadIdx.x; i0 < cnt; i0 += B * kPipeBlock) {
+  for (uint32_t i0 = part * kPipeBlock + threadIdx.x; i0 < cnt; i0 += B * stride) {
     uint64_t hc[B], idx[B];
     Sector sec[B];
 #pragma unroll
     for (int b = 0; b < B; b++) {
-      const uint32_t i = i0 + b * kPipeBlock;
+      const uint32_t i = i0 + b * stride;
       if (i < cnt) {
         hc[b] = murmur3(pa.rkey[rbase + i]);
         idx[b] = fast_mod(hc[b], t.div);
@@ -270,7 +280,7 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
     }
 #pragma unroll
     for (int b = 0; b < B; b++) {
-      const uint32_t i = i0 + b * kPipeBlock;
+      const uint32_t i = i0 + b * stride;
       if (i < cnt) {
         const uint32_t slot = pa.rslot[rbase + i];
         pa.gtax[rbase + slot] = probe_sectors(t, hc[b], idx[b], sec[b]);
@@ -278,70 +288,6 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
       }
     }
   }
-}
-
-// Probe with the sector loads landing in shared memory (cp.async): each
-// thread keeps kProbeSlots sectors in flight without holding them in
-// registers, in a rolling pipeline -- wait for the oldest, resolve it, issue
-// the next key into its slot.  Probe blocks have the step kernel's shared
-// memory to themselves.
-#ifndef K2G_PROBE_SLOTS
-#define K2G_PROBE_SLOTS 6
-#endif
-constexpr int kProbeSlots = K2G_PROBE_SLOTS;
-
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-__device__ __forceinline__ void pipe_probe_body_async(const PipeArgs &pa, uint32_t blk,
-                                                      unsigned char *smem) {
-  constexpr int D = kProbeSlots;
-  const uint64_t f0 = (uint64_t)blk * kPipeBlock;
-  const uint64_t rbase = pipe_gbase(pa, f0);
-  const uint32_t cnt = pa.bcount[blk];
-  const TableView &t = pa.a.table;
-  uint4 *slots = reinterpret_cast<uint4 *>(smem);   // [D][kPipeBlock][2]
-  uint64_t hc[D];
-  auto issue = [&](int d, uint32_t i) {
-    hc[d] = murmur3(pa.rkey[rbase + i]);
-    const uint4 *src = reinterpret_cast<const uint4 *>(t.cells + (fast_mod(hc[d], t.div) & ~7ull));
-    uint4 *dst = slots + ((size_t)d * kPipeBlock + threadIdx.x) * 2;
-    cp_async16(dst, src);
-    cp_async16(dst + 1, src + 1);
-  };
-#pragma unroll
-  for (int d = 0; d < D; d++) {
-    const uint32_t i = threadIdx.x + d * kPipeBlock;
-    if (i < cnt) issue(d, i);
-    cp_async_commit();
-  }
-  for (uint32_t j0 = 0; threadIdx.x + j0 * kPipeBlock < cnt; j0 += D) {
-#pragma unroll
-    for (int d = 0; d < D; d++) {
-      const uint32_t i = threadIdx.x + (j0 + d) * kPipeBlock;
-      cp_async_wait<D - 1>();   // the group of key j0 + d has landed
-      if (i < cnt) {
-        const uint4 *src = slots + ((size_t)d * kPipeBlock + threadIdx.x) * 2;
-        Sector sec;
-        sec.lo = src[0];
-        sec.hi = src[1];
-        const uint32_t slot = pa.rslot[rbase + i];
-        pa.gtax[rbase + slot] = probe_sectors(t, hc[d], fast_mod(hc[d], t.div), sec);
-        if (pa.gkey) pa.gkey[rbase + slot] = pa.rkey[rbase + i];
-      }
-      const uint32_t in = i + D * kPipeBlock;
-      if (in < cnt) issue(d, in);
-      cp_async_commit();
-    }
-  }
-  cp_async_wait<0>();
 }
 
 // Taxon map of one resolve thread in shared memory, interleaved by thread.
@@ -493,28 +439,22 @@ struct StepArgs {
   uint32_t n_scan, n_probe, n_resolve;   // blocks per role
 };
 
-#ifndef K2G_PROBE_ASYNC
-#define K2G_PROBE_ASYNC 0
-#endif
-
-// Resident blocks per SM the register allocation is fitted to.
+// Resident blocks per SM the register allocation is fitted to (7 measured
+// fastest on the 40 GB workload: 6 leaves too few warps, 8 spills).
 #ifndef K2G_PIPE_MIN_BLOCKS
-#define K2G_PIPE_MIN_BLOCKS 6
+#define K2G_PIPE_MIN_BLOCKS 7
 #endif
 
 template <int W, bool QUAL, bool RC1>
 __global__ void __launch_bounds__(kPipeBlock, K2G_PIPE_MIN_BLOCKS)
 pipe_step_kernel(StepArgs sa) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t role = blockIdx.x % 3, blk = blockIdx.x / 3;
+  constexpr uint32_t kRoles = 2 + kProbeSplit;
+  const uint32_t role = blockIdx.x % kRoles, blk = blockIdx.x / kRoles;
   if (role == 0) {
     if (blk < sa.n_scan) pipe_scan_body<W, QUAL, RC1>(sa.scan, blk, smem);
-  } else if (role == 1) {
-#if K2G_PROBE_ASYNC
-    if (blk < sa.n_probe) pipe_probe_body_async(sa.probe, blk, smem);
-#else
-    if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk);
-#endif
+  } else if (role <= (uint32_t)kProbeSplit) {
+    if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk, role - 1);
   } else {
     if (blk < sa.n_resolve) pipe_resolve_body(sa.resolve, blk, smem);
   }
@@ -524,11 +464,9 @@ template <int W, bool QUAL, bool RC1>
 cudaError_t launch_pipe_step(const StepArgs &sa, cudaStream_t st) {
   const uint32_t most = max(sa.n_scan, max(sa.n_probe, sa.n_resolve));
   if (!most) return cudaSuccess;
-  size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
-                    ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
-  if (K2G_PROBE_ASYNC && smem < (size_t)kProbeSlots * kPipeBlock * 32)
-    smem = (size_t)kProbeSlots * kPipeBlock * 32;
-  pipe_step_kernel<W, QUAL, RC1><<<3 * most, kPipeBlock, smem, st>>>(sa);
+  const size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
+                          ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
+  pipe_step_kernel<W, QUAL, RC1><<<(2 + kProbeSplit) * most, kPipeBlock, smem, st>>>(sa);
   note_launches();
   return cudaGetLastError();
 }
