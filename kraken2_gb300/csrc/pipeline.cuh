@@ -128,6 +128,77 @@ __device__ __forceinline__ void pipe_scan_base(ScanLane<W> &s, const PipeArgs &p
   nst += is_key ? 1 : 0;
 }
 
+// The part of pipe_scan_base after the window minimum: token kind, groups,
+// keys.  m is the minimizer (toggle already removed).
+__device__ __forceinline__ void pipe_scan_emit(ScanLane<5> &s, const PipeArgs &pa, const ScanConst &c,
+                                               int32_t p, bool amb, uint64_t m, uint64_t *skey,
+                                               uint32_t *sslot, int &nst) {
+  const bool emit = (p >= c.k - 1) && (p < (int32_t)s.len);
+  const bool nonamb = emit && !amb;
+  const bool is_new = nonamb && (m != s.last_min);
+  s.last_min = nonamb ? m : s.last_min;
+  bool skip = false;
+  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  const bool is_key = is_new && !skip;
+  const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
+  const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
+                                       : (tkind == G_CONT && s.gkind != G_AMBIG && s.gkind != G_NONE);
+  const bool newg = emit && !cont;
+  const bool close = newg && (s.gkind != G_NONE);
+  if (close) pa.gstream[s.gbase + s.ng] = make_group(s.gkind, s.glen);
+  s.ng += close ? 1u : 0u;
+  s.glen = emit ? (newg ? 1u : s.glen + 1u) : s.glen;
+  s.gkind = newg ? tkind : s.gkind;
+  if (is_key) {
+    skey[nst * kPipeBlock] = m;
+    sslot[nst * kPipeBlock] = (uint32_t)s.ng;
+  }
+  nst += is_key ? 1 : 0;
+}
+
+__device__ __forceinline__ uint64_t min64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+// Four bases (one 32-bit word of the chunk) with a window of w = 5 l-mers:
+// the minimum over positions p-4..p is min(suffix minimum of the previous
+// word's candidates from p-4 on, prefix minimum of this word's up to p), so
+// a word costs 10 minimum operations instead of 16 and no window shifts.
+// win.r[0..3] hold the previous word's suffix minima (all ~0 at a mate start,
+// like an empty window).
+template <bool RC1>
+__device__ __forceinline__ void pipe_scan_word5(ScanLane<5> &s, const PipeArgs &pa, const ScanConst &c,
+                                                int32_t p0, uint32_t ok, uint32_t codes,
+                                                uint64_t *skey, uint32_t *sslot, int &nst) {
+  uint64_t cand[4];
+  bool amb[4];
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const uint32_t valid = (ok >> (8 * b)) & 1u, code = (codes >> (8 * b)) & 3u;
+    s.fwd = ((s.fwd << 2) | code) & c.lmer_mask;
+    s.rc = (s.rc >> 2) | ((uint64_t)(code ^ 3u) << c.top_shift);
+    s.run = valid ? s.run + 1 : 0;
+    s.last_amb = valid ? s.last_amb : p0 + b;
+    amb[b] = (p0 + b - s.last_amb) <= c.amb_span;
+    const uint64_t rcv = RC1 ? s.rc : revcomp_v0(s.fwd, c.lmer_mask);
+    const uint64_t cd = ((s.fwd < rcv ? s.fwd : rcv) & c.smask) ^ c.toggle;
+    cand[b] = (s.run >= c.l) ? cd : ~0ull;
+  }
+  const uint64_t q1 = min64(cand[0], cand[1]), q2 = min64(q1, cand[2]), q3 = min64(q2, cand[3]);
+  const uint64_t m0 = min64(s.win.r[0], cand[0]), m1 = min64(s.win.r[1], q1),
+                 m2 = min64(s.win.r[2], q2), m3 = min64(s.win.r[3], q3);
+  s.win.r[3] = cand[3];
+  s.win.r[2] = min64(cand[2], cand[3]);
+  s.win.r[1] = min64(cand[1], s.win.r[2]);
+  s.win.r[0] = min64(cand[0], s.win.r[1]);
+  pipe_scan_emit(s, pa, c, p0, amb[0], m0 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit(s, pa, c, p0 + 1, amb[1], m1 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit(s, pa, c, p0 + 2, amb[2], m2 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit(s, pa, c, p0 + 3, amb[3], m3 ^ c.toggle, skey, sslot, nst);
+}
+
+#ifndef K2G_SCAN_WORD5
+#define K2G_SCAN_WORD5 1
+#endif
+
 constexpr size_t kScanSmem = (size_t)kStage * kPipeBlock * 12 + 16;
 
 template <int W, bool QUAL, bool RC1>
@@ -214,10 +285,14 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
           const int32_t before = -(pbase + 4 * wi);
           if (before > 0) ok = before >= 4 ? 0u : (ok & (0xFFFFFFFFu << (8 * before)));
           const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
+          if constexpr (W == 5 && K2G_SCAN_WORD5) {
+            pipe_scan_word5<RC1>(s, pa, c, pbase + 4 * wi, ok, codes, skey, sslot, nst);
+          } else {
 #pragma unroll
-          for (int b = 0; b < 4; b++) {
-            pipe_scan_base<W, RC1>(s, pa, c, pbase + 4 * wi + b, (ok >> (8 * b)) & 1u,
-                                   (codes >> (8 * b)) & 3u, skey, sslot, nst);
+            for (int b = 0; b < 4; b++) {
+              pipe_scan_base<W, RC1>(s, pa, c, pbase + 4 * wi + b, (ok >> (8 * b)) & 1u,
+                                     (codes >> (8 * b)) & 3u, skey, sslot, nst);
+            }
           }
         }
         s.ci++;
