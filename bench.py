@@ -850,12 +850,9 @@ def dist_setup(n_gpus: int):
 
 
 def max_over_ranks(pg, value: float) -> float:
-    if pg is None:
-        return value
-    import torch
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    return float(t.item())
+    """Slowest rank's time (replicas: every rank classifies its own reads)."""
+    from kraken2_gb300.replicas import max_over_ranks as _max
+    return _max(pg, value, device="cuda")
 
 
 def barrier(pg):
