@@ -273,6 +273,8 @@ k2g_status k2g_server_wait(k2g_server *s, uint64_t ticket, double timeout_s, int
 k2g_status k2g_server_fetch(k2g_server *s, uint64_t ticket, uint32_t *call, uint32_t *hit_groups,
                             uint32_t *hitlist_len, uint64_t *runs, uint64_t *n_runs,
                             double *latency_s);
+/* Result sizes of a finished request (to size the buffers for fetch). */
+k2g_status k2g_server_sizes(k2g_server *s, uint64_t ticket, uint64_t *n_frags, uint64_t *n_runs);
 k2g_status k2g_server_destroy(k2g_server *s);
 
 /* Pinned host memory helpers for callers that stage their own buffers. */

@@ -40,7 +40,7 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
            "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
            "k2g_classify_host_blocks", "k2g_server_create", "k2g_server_submit",
-           "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy"]
+           "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy", "k2g_server_sizes"]
 
 
 class K2GError(RuntimeError):
@@ -130,6 +130,7 @@ def lib():
             "k2g_server_wait": [vp, u64, C.c_double, C.POINTER(i32)],
             "k2g_server_fetch": [vp, u64, vp, vp, vp, vp, C.POINTER(u64), C.POINTER(C.c_double)],
             "k2g_server_destroy": [vp],
+            "k2g_server_sizes": [vp, u64, C.POINTER(u64), C.POINTER(u64)],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -294,12 +295,16 @@ class Server:
         check(lib().k2g_server_wait(self.h, ticket, timeout_s, C.byref(done)))
         return bool(done.value)
 
-    def fetch(self, ticket: int, n_frags: int, runs_cap: int):
-        """-> (call, hit_groups, hitlist_len, runs, latency_s)"""
-        call = np.zeros(n_frags, np.uint32)
-        hg = np.zeros(n_frags, np.uint32)
-        hl = np.zeros(n_frags, np.uint32)
-        runs = np.zeros(max(runs_cap, 1), np.uint64)
+    def fetch(self, ticket: int, n_frags: int | None = None, runs_cap: int | None = None):
+        """-> (call, hit_groups, hitlist_len, runs, latency_s) of a finished
+        request, which is released.  Buffers are sized from the request."""
+        nf, nr0 = C.c_uint64(0), C.c_uint64(0)
+        lib().k2g_server_sizes(self.h, ticket, C.byref(nf), C.byref(nr0))
+        n_frags = nf.value if n_frags is None or nf.value else n_frags
+        call = np.empty(n_frags, np.uint32)
+        hg = np.empty(n_frags, np.uint32)
+        hl = np.empty(n_frags, np.uint32)
+        runs = np.empty(max(nr0.value, 1), np.uint64)
         nr = C.c_uint64(len(runs))
         lat = C.c_double(0)
         check(lib().k2g_server_fetch(self.h, ticket, call.ctypes.data, hg.ctypes.data,

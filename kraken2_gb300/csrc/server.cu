@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -36,13 +37,37 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// memcpy split over a few threads: request and batch copies are large
+// (hundreds of MB), and one thread moves only a fraction of what the host
+// memory system can.
+void par_copy(void *dst, const void *src, size_t n) {
+  constexpr size_t kPiece = 8u << 20;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t parts = std::min<size_t>(std::min(8u, hw), n / kPiece);
+  if (parts <= 1) {
+    memcpy(dst, src, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const size_t step = (n + parts - 1) / parts;
+  for (size_t i = 1; i < parts; i++) {
+    const size_t a = i * step, b = std::min(n, a + step);
+    if (a < b)
+      th.emplace_back([=] { memcpy((char *)dst + a, (const char *)src + a, b - a); });
+  }
+  memcpy(dst, src, std::min(n, step));
+  for (auto &t : th) t.join();
+}
+
 struct Request {
-  std::vector<char> bases, quals;
+  std::unique_ptr<char[]> bases, quals;   // not value-initialised: copied over at once
   std::vector<uint64_t> off;        // n_seqs + 1, from 0
   uint64_t n_frags = 0, next = 0, done_frags = 0;
   std::vector<uint32_t> call, hg, hlen;
-  std::map<uint64_t, std::vector<uint64_t>> piece_runs;   // first fragment -> runs
-  std::vector<uint64_t> runs;
+  // pieces that finished before an earlier piece: first fragment -> (count, runs)
+  std::map<uint64_t, std::pair<uint64_t, std::vector<uint64_t>>> piece_runs;
+  std::vector<uint64_t> runs;       // runs of fragments [0, runs_frags), in order
+  uint64_t runs_frags = 0;
   Clock::time_point t_submit, t_done;
   bool done = false;
   k2g_status status = K2G_OK;
@@ -188,8 +213,8 @@ k2g_status launch(k2g_server *sv, Slot &s) {
   for (const Piece &p : s.pieces) {
     const Request &r = *p.req;   // inputs are immutable after submit
     const uint64_t b0 = r.off[p.f0 * sv->per], b1 = r.off[(p.f0 + p.nf) * sv->per];
-    memcpy(s.h_bases + bb, r.bases.data() + b0, b1 - b0);
-    if (sv->quals) memcpy(s.h_quals + bb, r.quals.data() + b0, b1 - b0);
+    par_copy(s.h_bases + bb, r.bases.get() + b0, b1 - b0);
+    if (sv->quals) par_copy(s.h_quals + bb, r.quals.get() + b0, b1 - b0);
     for (uint64_t i = 1; i <= p.nf * sv->per; i++)
       s.h_off[fb * sv->per + i] = bb + (r.off[p.f0 * sv->per + i] - b0);
     fb += p.nf;
@@ -244,13 +269,26 @@ k2g_status finish(k2g_server *sv, Slot &s) {
     memcpy(r.hlen.data() + p.f0, s.h_hlen + fb, p.nf * 4);
     uint64_t n = 0;
     for (uint64_t i = 0; i < p.nf; i++) n += s.h_hlen[fb + i];
-    r.piece_runs[p.f0].assign(s.h_runs + rb, s.h_runs + rb + n);
+    if (p.f0 == r.runs_frags) {
+      // the next piece in order (the usual case): append it, then any
+      // pieces that finished before it and now follow on
+      const size_t at = r.runs.size();
+      r.runs.resize(at + n);
+      par_copy(r.runs.data() + at, s.h_runs + rb, n * 8);
+      r.runs_frags += p.nf;
+      for (auto it = r.piece_runs.find(r.runs_frags); it != r.piece_runs.end();
+           it = r.piece_runs.find(r.runs_frags)) {
+        r.runs.insert(r.runs.end(), it->second.second.begin(), it->second.second.end());
+        r.runs_frags += it->second.first;
+        r.piece_runs.erase(it);
+      }
+    } else {
+      r.piece_runs[p.f0] = {p.nf, std::vector<uint64_t>(s.h_runs + rb, s.h_runs + rb + n)};
+    }
     rb += n;
     fb += p.nf;
     r.done_frags += p.nf;
-    if (r.done_frags == r.n_frags) {
-      for (auto &kv : r.piece_runs) r.runs.insert(r.runs.end(), kv.second.begin(), kv.second.end());
-      r.piece_runs.clear();
+    if (r.done_frags == r.n_frags) {   // every piece is in: runs are complete and in order
       r.done = true;
       r.t_done = Clock::now();
     }
@@ -355,8 +393,12 @@ extern "C" k2g_status k2g_server_submit(k2g_server *sv, const char *bases, const
   const uint64_t n_seqs = n_frags * sv->per;
   const uint64_t b0 = n_frags ? seq_off[0] : 0, b1 = n_frags ? seq_off[n_seqs] : 0;
   if (b1 < b0) return fail(K2G_ERR_ARG, "seq_off must be non-decreasing");
-  r->bases.assign(bases + b0, bases + b1);
-  if (sv->quals && n_frags) r->quals.assign(quals + b0, quals + b1);
+  r->bases.reset(new char[b1 - b0 + 1]);
+  par_copy(r->bases.get(), bases + b0, b1 - b0);
+  if (sv->quals && n_frags) {
+    r->quals.reset(new char[b1 - b0 + 1]);
+    par_copy(r->quals.get(), quals + b0, b1 - b0);
+  }
   r->off.resize(n_seqs + 1);
   for (uint64_t i = 0; i <= n_seqs; i++) r->off[i] = seq_off[i] - b0;
   r->n_frags = n_frags;
@@ -412,9 +454,21 @@ extern "C" k2g_status k2g_server_fetch(k2g_server *sv, uint64_t ticket, uint32_t
   if (call) memcpy(call, r->call.data(), r->n_frags * 4);
   if (hit_groups) memcpy(hit_groups, r->hg.data(), r->n_frags * 4);
   if (hitlist_len) memcpy(hitlist_len, r->hlen.data(), r->n_frags * 4);
-  if (runs) memcpy(runs, r->runs.data(), r->runs.size() * 8);
+  if (runs) par_copy(runs, r->runs.data(), r->runs.size() * 8);
   if (n_runs) *n_runs = r->runs.size();
   if (latency_s) *latency_s = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_server_sizes(k2g_server *sv, uint64_t ticket, uint64_t *n_frags,
+                                       uint64_t *n_runs) {
+  if (!sv) return fail(K2G_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(sv->mu);
+  auto it = sv->reqs.find(ticket);
+  if (it == sv->reqs.end()) return fail(K2G_ERR_ARG, "unknown ticket");
+  if (!it->second->done) return fail(K2G_ERR_ARG, "request not finished");
+  if (n_frags) *n_frags = it->second->n_frags;
+  if (n_runs) *n_runs = it->second->runs.size();
   return K2G_OK;
 }
 
