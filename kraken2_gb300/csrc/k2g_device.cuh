@@ -103,6 +103,81 @@ __device__ __forceinline__ uint32_t probe_sectors(const TableView &t, uint64_t h
   }
 }
 
+// probe_sectors split in two: the loaded home sector alone, and the walk
+// from a later sector.  `probe_first` returns true with *v set when the home
+// sector ends the walk; otherwise *next (the next sector's base) and *walked
+// are where probe_continue picks it up.
+__device__ __forceinline__ bool probe_first(const TableView &t, uint64_t hc, uint64_t idx,
+                                            const Sector &sec, uint32_t *v, uint64_t *next,
+                                            uint64_t *walked) {
+  const uint32_t ck = (uint32_t)(hc >> t.key_shift);
+  const uint64_t base = idx & ~7ull;
+  const uint32_t off = (uint32_t)(idx & 7u);
+  const uint32_t c[8] = {sec.lo.x, sec.lo.y, sec.lo.z, sec.lo.w, sec.hi.x, sec.hi.y, sec.hi.z, sec.hi.w};
+  const uint64_t left = t.capacity - base;
+  const uint32_t real = left >= 8 ? 0xFFu : ((1u << (uint32_t)left) - 1u);
+  uint32_t stop = 0, match = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const bool empty = (c[i] & t.value_mask) == 0;
+    const bool hit = !empty && (c[i] >> t.value_bits) == ck;
+    stop |= (uint32_t)(empty || hit) << i;
+    match |= (uint32_t)hit << i;
+  }
+  const uint32_t window = real & (0xFFu << off);
+  stop &= window;
+  if (stop) {
+    const int i = __ffs(stop) - 1;
+    if ((uint64_t)(i - (int)off) >= t.capacity || !((match >> i) & 1u)) {
+      *v = 0;
+    } else {
+      uint32_t x = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) x = (j == i) ? c[j] : x;
+      *v = x & t.value_mask;
+    }
+    return true;
+  }
+  *walked = __popc(window);
+  if (*walked >= t.capacity) {
+    *v = 0;
+    return true;
+  }
+  *next = base + 8 >= t.capacity ? 0 : base + 8;
+  return false;
+}
+
+__device__ __forceinline__ uint32_t probe_continue(const TableView &t, uint64_t hc, uint64_t base,
+                                                   uint64_t walked) {
+  const uint32_t ck = (uint32_t)(hc >> t.key_shift);
+  while (true) {
+    const Sector sec = load_sector(t.cells, base);
+    const uint32_t c[8] = {sec.lo.x, sec.lo.y, sec.lo.z, sec.lo.w, sec.hi.x, sec.hi.y, sec.hi.z, sec.hi.w};
+    const uint64_t left = t.capacity - base;
+    const uint32_t window = left >= 8 ? 0xFFu : ((1u << (uint32_t)left) - 1u);
+    uint32_t stop = 0, match = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const bool empty = (c[i] & t.value_mask) == 0;
+      const bool hit = !empty && (c[i] >> t.value_bits) == ck;
+      stop |= (uint32_t)(empty || hit) << i;
+      match |= (uint32_t)hit << i;
+    }
+    stop &= window;
+    if (stop) {
+      const int i = __ffs(stop) - 1;
+      if (walked + (uint32_t)i >= t.capacity || !((match >> i) & 1u)) return 0;
+      uint32_t x = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) x = (j == i) ? c[j] : x;
+      return x & t.value_mask;
+    }
+    walked += __popc(window);
+    if (walked >= t.capacity) return 0;
+    base = base + 8 >= t.capacity ? 0 : base + 8;
+  }
+}
+
 __device__ __forceinline__ uint32_t table_get(const TableView &t, uint64_t key) {
   uint64_t hc = murmur3(key);
   uint64_t idx = fast_mod(hc, t.div);
