@@ -71,7 +71,7 @@ def _build_classify(lib: str):
     gxx = shutil.which("g++") or "g++"
     exe = classify_path()
     tmp = exe + ".tmp"
-    _run([gxx, "-O2", "-std=c++17", "-Wall", "-I", INCLUDE,
+    _run([gxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I", INCLUDE,
           *[os.path.join(HOST, s) for s in HOST_SOURCES],
           "-L", OUT, "-lk2g", "-Wl,-rpath,$ORIGIN", "-o", tmp])
     os.replace(tmp, exe)

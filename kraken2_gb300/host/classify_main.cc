@@ -6,32 +6,40 @@
 // Input is read in the reference's blocks (3 MiB of sequence single-end,
 // 10,000 records per file for pairs in two files, 20,000 records for
 // interleaved pairs) because the -K counters depend on them; blocks are
-// gathered into large batches for the GPU and written out in input order.
+// gathered into batches of about 64 M bases for the GPU.  Reading,
+// classification and output run as a three-thread pipeline over a pool of
+// batches; output is formatted on up to -p threads and written in input
+// order, so every output file is byte for byte what one thread would write.
 #include <err.h>
 #include <getopt.h>
 #include <sys/time.h>
 #include <sysexits.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <charconv>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <iostream>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "k2g.h"
 #include "report.h"
 #include "seq_reader.h"
 
-using k2host::Record;
-
 namespace {
 
 constexpr size_t kBlockBytes = 3 * 1024 * 1024;      // src/classify.cc:526
 constexpr size_t kFragmentsPerBatch = 10000;          // src/classify.cc:32
-constexpr uint64_t kGpuBatchBases = 256ull << 20;     // bases gathered per GPU call
+constexpr uint64_t kGpuBatchBases = 64ull << 20;      // bases gathered per GPU call
+constexpr int kBatchesInFlight = 4;                   // reading, classifying, writing, spare
 
 struct Options {
   std::string index_filename, taxonomy_filename, options_filename;
@@ -173,11 +181,57 @@ struct Stats {
   uint64_t total_sequences = 0, total_bases = 0, total_classified = 0;
 };
 
-// Fragments gathered for one GPU call.
+// FIFO between the pipeline's threads; pop() returns nullptr once the
+// channel is closed and drained.  Batches circulate through a fixed pool,
+// which bounds the memory in flight.
+template <class T>
+class Channel {
+ public:
+  void push(T *v) {
+    std::lock_guard<std::mutex> l(mu_);
+    q_.push_back(v);
+    cv_.notify_one();
+  }
+  T *pop() {
+    std::unique_lock<std::mutex> l(mu_);
+    cv_.wait(l, [&] { return !q_.empty() || closed_; });
+    if (q_.empty()) return nullptr;
+    T *v = q_.front();
+    q_.pop_front();
+    return v;
+  }
+  void close() {
+    std::lock_guard<std::mutex> l(mu_);
+    closed_ = true;
+    cv_.notify_all();
+  }
+
+ private:
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<T *> q_;
+  bool closed_ = false;
+};
+
+// Fragments of one GPU call: whole reader blocks of one input, parsed into
+// arenas, and their results.
 struct Batch {
-  std::vector<Record> r1, r2;
-  std::vector<uint32_t> block;
-  uint64_t bases = 0;
+  k2host::RecordSet m1;               // single reads, first mates, or interleaved pairs
+  k2host::RecordSet m2;               // second mates read from a second file
+  std::vector<uint32_t> block;        // reader block of each fragment
+  std::vector<char> mates;            // two-file pairs interleaved for the call
+  std::vector<uint64_t> mates_off;
+  std::vector<uint32_t> call, hlen;
+  std::unique_ptr<uint64_t[]> runs;   // hit-list runs, uninitialised until written
+  uint64_t runs_cap = 0;
+  std::vector<uint64_t> run_start;    // first run of each fragment
+
+  uint64_t frags() const { return block.size(); }
+  void clear() {
+    m1.clear();
+    m2.clear();
+    block.clear();
+  }
 };
 
 void append_u64(std::string &s, uint64_t v) {
@@ -186,153 +240,230 @@ void append_u64(std::string &s, uint64_t v) {
   s.append(b, r.ptr);
 }
 
-// TrimPairInfo (src/classify.cc:764-771): drop a trailing "/1" or "/2".
-std::string trim_pair_info(const std::string &id) {
-  const size_t sz = id.size();
-  if (sz <= 2) return id;
-  if (id[sz - 2] == '/' && (id[sz - 1] == '1' || id[sz - 1] == '2')) return id.substr(0, sz - 2);
-  return id;
-}
-
-// Sequence::to_string (src/seqreader.cc:20-50).
-void append_record(std::string &s, const Record &r, const char *tag) {
+// Sequence::to_string (src/seqreader.cc:20-50) of record i of set, with an
+// optional tag after the name.
+void append_record(std::string &s, const k2host::RecordSet &set, size_t i, const char *tag,
+                   size_t tag_len) {
+  const k2host::RecordRef &r = set.recs[i];
   s.push_back(r.fastq ? '@' : '>');
-  s += r.name;
-  if (tag) s += tag;
-  if (!r.comment.empty()) {
+  s.append(set.name(i), r.name_len);
+  s.append(tag, tag_len);
+  if (r.comment_len) {
     s.push_back(' ');
-    s += r.comment;
+    s.append(set.comment(i), r.comment_len);
   }
   s.push_back('\n');
-  s += r.seq;
+  s.append(set.seq_at(i), set.seq_len(i));
   if (r.fastq) {
     s += "\n+\n";
-    s += r.qual;
+    s.append(set.qual(i), set.seq_len(i));
   }
   s.push_back('\n');
 }
 
-class Classifier {
- public:
-  Classifier(const Options &o, k2g_db *db, const k2host::TaxonomyFile &tax, k2g_counters *counters,
-             k2host::RunCounts &rc, Stats &stats, Outputs &out)
-      : o_(o), db_(db), tax_(tax), counters_(counters), rc_(rc), stats_(stats), out_(out) {}
+// Output text of a range of fragments, formatted by one worker.
+struct Piece {
+  std::string ko, c1, c2, u1, u2;
+  Stats stats;
+};
 
-  // Classifies the batch and writes its output in input order.
-  void run(Batch &b) {
-    const uint64_t n = b.r1.size();
-    if (!n) return;
-    const bool paired = o_.paired_end_processing;
-    const int per = paired ? 2 : 1;
-    std::string bases;
-    bases.reserve(b.bases + 16);
-    std::vector<uint64_t> off;
-    off.reserve(n * per + 1);
-    off.push_back(0);
-    auto add = [&](Record &r) {
-      if (o_.minimum_quality_score > 0 && r.fastq) mask(r);
-      bases += r.seq;
-      off.push_back(bases.size());
-    };
-    for (uint64_t i = 0; i < n; i++) {
-      add(b.r1[i]);
-      if (paired) add(b.r2[i]);
+// Reads, classifies and writes on three threads: this one reads blocks into
+// batches, one thread runs each batch through k2g_classify_host_blocks (in
+// input order, so reader blocks and the -K counters see the reference's
+// sequence), and one thread formats each batch's output on up to -p
+// workers and writes it in input order.
+class Pipeline {
+ public:
+  Pipeline(const Options &o, k2g_db *db, const k2host::TaxonomyFile &tax,
+           k2g_counters *counters, k2host::RunCounts &rc, Outputs &out)
+      : o_(o), db_(db), tax_(tax), counters_(counters), rc_(rc), out_(out),
+        paired_(o.paired_end_processing), two_files_(paired_ && !o.single_file_pairs) {
+    for (auto &b : pool_) {
+      b.m1.reserve(kGpuBatchBases + kBlockBytes, kGpuBatchBases + kBlockBytes, 1 << 20);
+      free_.push(&b);
     }
-    std::vector<uint32_t> call(n), hlen(n);
-    uint64_t n_runs = bases.size() + 2 * n + 8;
-    std::vector<uint64_t> runs(n_runs);
-    k2g_classify_params p{o_.confidence_threshold, o_.minimum_hit_groups, o_.quick_mode ? 1 : 0,
-                          paired ? 1 : 0, 0};
-    k2g_status s = k2g_classify_host_blocks(db_, bases.data(), nullptr, off.data(), n,
-                                            b.block.data(), counters_, &p, call.data(), nullptr,
-                                            hlen.data(), runs.data(), &n_runs,
-                                            rc_.taxon_reads.data());
-    if (s != K2G_OK) errx(EX_SOFTWARE, "classification failed: %s", k2g_last_error());
-    write(b, call, hlen, runs);
+    gpu_ = std::thread([this] { gpu_loop(); });
+    writer_ = std::thread([this] { writer_loop(); });
+  }
+
+  // Waits for every batch to be written.
+  const Stats &finish() {
+    full_.close();
+    gpu_.join();
+    writer_.join();
+    return stats_;
+  }
+
+  Batch *take() { return free_.pop(); }
+
+  // Hands a batch on (an empty one goes back to the pool).
+  void submit(Batch *b) {
+    if (b->frags()) full_.push(b);
+    else free_.push(b);
   }
 
  private:
-  // MaskLowQualityBases (src/classify.cc:1060-1070)
-  void mask(Record &r) {
-    for (size_t i = 0; i < r.seq.size(); i++)
-      if ((r.qual[i] - '!') < o_.minimum_quality_score) r.seq[i] = 'x';
+  void gpu_loop() {
+    while (Batch *b = full_.pop()) {
+      classify(*b);
+      done_.push(b);
+    }
+    done_.close();
   }
 
-  void write(Batch &b, const std::vector<uint32_t> &call, const std::vector<uint32_t> &hlen,
-             const std::vector<uint64_t> &runs) {
-    const bool paired = o_.paired_end_processing;
-    std::string ko, c1, c2, u1, u2;
-    uint64_t ri = 0;
-    for (size_t i = 0; i < b.r1.size(); i++) {
-      Record &m1 = b.r1[i];
-      const uint32_t c = call[i];
+  void writer_loop() {
+    while (Batch *b = done_.pop()) {
+      write(*b);
+      b->clear();
+      free_.push(b);
+    }
+  }
+
+  void classify(Batch &b) {
+    const uint64_t n = b.frags();
+    const char *bases = b.m1.seq.data();
+    const uint64_t *off = b.m1.seq_off.data();
+    if (two_files_) {   // mate 1, mate 2, mate 1, ... as the call reads pairs
+      b.mates.resize(b.m1.seq.size() + b.m2.seq.size());
+      b.mates_off.resize(2 * n + 1);
+      b.mates_off[0] = 0;
+      char *w = b.mates.data();
+      for (uint64_t i = 0; i < n; i++) {
+        const uint64_t l1 = b.m1.seq_len(i), l2 = b.m2.seq_len(i);
+        memcpy(w, b.m1.seq_at(i), l1);
+        memcpy(w + l1, b.m2.seq_at(i), l2);
+        w += l1 + l2;
+        b.mates_off[2 * i + 1] = b.mates_off[2 * i] + l1;
+        b.mates_off[2 * i + 2] = b.mates_off[2 * i + 1] + l2;
+      }
+      bases = b.mates.data();
+      off = b.mates_off.data();
+    }
+    b.call.resize(n);
+    b.hlen.resize(n);
+    const uint64_t need = off[n * (paired_ ? 2 : 1)] + 2 * n + 8;
+    if (b.runs_cap < need) {
+      b.runs.reset(new uint64_t[need]);
+      b.runs_cap = need;
+    }
+    uint64_t n_runs = b.runs_cap;
+    k2g_classify_params p{o_.confidence_threshold, o_.minimum_hit_groups, o_.quick_mode ? 1 : 0,
+                          paired_ ? 1 : 0, 0};
+    const k2g_status s = k2g_classify_host_blocks(
+        db_, bases, nullptr, off, n, b.block.data(), counters_, &p, b.call.data(), nullptr,
+        b.hlen.data(), b.runs.get(), &n_runs, rc_.taxon_reads.data());
+    if (s != K2G_OK) errx(EX_SOFTWARE, "classification failed: %s", k2g_last_error());
+  }
+
+  // Record sets and indexes of fragment i's mates.
+  const k2host::RecordSet &set2(const Batch &b) const { return two_files_ ? b.m2 : b.m1; }
+  size_t idx1(size_t i) const { return paired_ && !two_files_ ? 2 * i : i; }
+  size_t idx2(size_t i) const { return two_files_ ? i : 2 * i + 1; }
+
+  void write(Batch &b) {
+    const uint64_t n = b.frags();
+    b.run_start.resize(n + 1);
+    b.run_start[0] = 0;
+    for (uint64_t i = 0; i < n; i++) b.run_start[i + 1] = b.run_start[i] + b.hlen[i];
+    // about 20,000 fragments per piece, at most -p pieces at a time
+    const uint64_t workers = (uint64_t)std::max(1, o_.num_threads);
+    const uint64_t pieces = std::max<uint64_t>(1, std::min<uint64_t>(workers, (n + 19999) / 20000));
+    std::vector<Piece> out(pieces);
+    std::vector<std::thread> th;
+    for (uint64_t k = 1; k < pieces; k++)
+      th.emplace_back([&, k] { format(b, n * k / pieces, n * (k + 1) / pieces, out[k]); });
+    format(b, 0, n / pieces, out[0]);
+    for (auto &t : th) t.join();
+    for (Piece &pc : out) {
+      if (out_.kraken) fwrite(pc.ko.data(), 1, pc.ko.size(), out_.kraken);
+      if (out_.c1) fwrite(pc.c1.data(), 1, pc.c1.size(), out_.c1);
+      if (out_.c2) fwrite(pc.c2.data(), 1, pc.c2.size(), out_.c2);
+      if (out_.u1) fwrite(pc.u1.data(), 1, pc.u1.size(), out_.u1);
+      if (out_.u2) fwrite(pc.u2.data(), 1, pc.u2.size(), out_.u2);
+      stats_.total_sequences += pc.stats.total_sequences;
+      stats_.total_bases += pc.stats.total_bases;
+      stats_.total_classified += pc.stats.total_classified;
+    }
+  }
+
+  void format(const Batch &b, uint64_t f0, uint64_t f1, Piece &pc) const {
+    const k2host::RecordSet &s1 = b.m1, &s2 = set2(b);
+    std::string &ko = pc.ko;
+    if (out_.kraken) ko.reserve((f1 - f0) * 64);
+    for (uint64_t i = f0; i < f1; i++) {
+      const size_t a = idx1(i), z = idx2(i);
+      const uint32_t c = b.call[i];
       const uint64_t ext = tax_.nodes[c].external_id;
-      stats_.total_sequences++;
-      stats_.total_bases += m1.seq.size() + (paired ? b.r2[i].seq.size() : 0);
-      if (c) stats_.total_classified++;
-      // kraken line (src/classify.cc:908-945)
-      ko += c ? "C\t" : "U\t";
-      ko += paired ? trim_pair_info(m1.name) : m1.name;
-      ko.push_back('\t');
-      if (o_.print_scientific_name) {
-        ko += c ? tax_.name(c) : "unclassified";
-        ko += " (taxid ";
-        append_u64(ko, ext);
-        ko.push_back(')');
-      } else {
-        append_u64(ko, ext);
-      }
-      ko.push_back('\t');
-      append_u64(ko, m1.seq.size());
-      if (paired) {
-        ko.push_back('|');
-        append_u64(ko, b.r2[i].seq.size());
-      }
-      ko.push_back('\t');
-      if (o_.quick_mode) {
-        append_u64(ko, ext);
-        ko += ":Q";
-      } else if (!hlen[i]) {
-        ko += "0:0";
-      } else {
-        // AddHitlistString (src/classify.cc:950-991)
-        for (uint32_t j = 0; j < hlen[i]; j++) {
-          const uint64_t r = runs[ri + j];
-          const uint32_t code = (uint32_t)(r >> 32), cnt = (uint32_t)r;
-          if (j) ko.push_back(' ');
-          if (code == K2G_CODE_MATE_BORDER) {
-            ko += "|:|";
-          } else if (code == K2G_CODE_AMBIGUOUS) {
-            ko += "A:";
-            append_u64(ko, cnt);
-            if (j + 1 == hlen[i]) ko.push_back(' ');
-          } else {
-            append_u64(ko, tax_.nodes[code].external_id);
-            ko.push_back(':');
-            append_u64(ko, cnt);
+      const uint64_t len1 = s1.seq_len(a), len2 = paired_ ? s2.seq_len(z) : 0;
+      pc.stats.total_sequences++;
+      pc.stats.total_bases += len1 + len2;
+      if (c) pc.stats.total_classified++;
+      if (out_.kraken) {
+        // kraken line (src/classify.cc:908-945)
+        ko += c ? "C\t" : "U\t";
+        size_t name_len = s1.recs[a].name_len;
+        const char *name = s1.name(a);
+        // TrimPairInfo (src/classify.cc:764-771): drop a trailing "/1" or "/2"
+        if (paired_ && name_len > 2 && name[name_len - 2] == '/' &&
+            (name[name_len - 1] == '1' || name[name_len - 1] == '2'))
+          name_len -= 2;
+        ko.append(name, name_len);
+        ko.push_back('\t');
+        if (o_.print_scientific_name) {
+          ko += c ? tax_.name(c) : "unclassified";
+          ko += " (taxid ";
+          append_u64(ko, ext);
+          ko.push_back(')');
+        } else {
+          append_u64(ko, ext);
+        }
+        ko.push_back('\t');
+        append_u64(ko, len1);
+        if (paired_) {
+          ko.push_back('|');
+          append_u64(ko, len2);
+        }
+        ko.push_back('\t');
+        if (o_.quick_mode) {
+          append_u64(ko, ext);
+          ko += ":Q";
+        } else if (!b.hlen[i]) {
+          ko += "0:0";
+        } else {
+          // AddHitlistString (src/classify.cc:950-991)
+          const uint64_t *runs = b.runs.get() + b.run_start[i];
+          const uint32_t hl = b.hlen[i];
+          for (uint32_t j = 0; j < hl; j++) {
+            const uint32_t code = (uint32_t)(runs[j] >> 32), cnt = (uint32_t)runs[j];
+            if (j) ko.push_back(' ');
+            if (code == K2G_CODE_MATE_BORDER) {
+              ko += "|:|";
+            } else if (code == K2G_CODE_AMBIGUOUS) {
+              ko += "A:";
+              append_u64(ko, cnt);
+              if (j + 1 == hl) ko.push_back(' ');
+            } else {
+              append_u64(ko, tax_.nodes[code].external_id);
+              ko.push_back(':');
+              append_u64(ko, cnt);
+            }
           }
         }
+        ko.push_back('\n');
       }
-      ko.push_back('\n');
-      ri += hlen[i];
       // classified / unclassified sequences (src/classify.cc:587-602)
       if (c) {
         if (out_.c1) {
           std::string tag = " kraken:taxid|";
           append_u64(tag, ext);
-          append_record(c1, m1, tag.c_str());
-          if (paired) append_record(c2, b.r2[i], tag.c_str());
+          append_record(pc.c1, s1, a, tag.data(), tag.size());
+          if (paired_) append_record(pc.c2, s2, z, tag.data(), tag.size());
         }
       } else if (out_.u1) {
-        append_record(u1, m1, nullptr);
-        if (paired) append_record(u2, b.r2[i], nullptr);
+        append_record(pc.u1, s1, a, "", 0);
+        if (paired_) append_record(pc.u2, s2, z, "", 0);
       }
     }
-    if (out_.kraken) fwrite(ko.data(), 1, ko.size(), out_.kraken);
-    if (out_.c1) fwrite(c1.data(), 1, c1.size(), out_.c1);
-    if (out_.c2) fwrite(c2.data(), 1, c2.size(), out_.c2);
-    if (out_.u1) fwrite(u1.data(), 1, u1.size(), out_.u1);
-    if (out_.u2) fwrite(u2.data(), 1, u2.size(), out_.u2);
   }
 
   const Options &o_;
@@ -340,61 +471,51 @@ class Classifier {
   const k2host::TaxonomyFile &tax_;
   k2g_counters *counters_;
   k2host::RunCounts &rc_;
-  Stats &stats_;
   Outputs &out_;
+  const bool paired_, two_files_;
+  Batch pool_[kBatchesInFlight];
+  Channel<Batch> free_, full_, done_;
+  Stats stats_;
+  std::thread gpu_, writer_;
 };
 
 // ProcessFiles (src/classify.cc:481-690): one input (or pair of inputs),
-// read block by block, classified in batches of blocks.
-void process_files(const char *f1, const char *f2, const Options &o, Classifier &cls,
+// read block by block into batches of whole blocks.
+void process_files(const char *f1, const char *f2, const Options &o, Pipeline &pl,
                    Outputs &out, uint32_t &block_id) {
   k2host::SeqReader reader1(k2host::open_input(f1));
   k2host::SeqReader reader2(f2 ? k2host::open_input(f2) : -1);
-  std::vector<Record> blk1, blk2;
-  Batch batch;
+  Batch *b = pl.take();
   while (true) {
-    size_t n1 = 0, n2 = 0;
-    bool ok;
+    const size_t s1 = b->m1.size(), s2 = b->m2.size();
+    size_t frags;
     if (!o.paired_end_processing) {
-      ok = reader1.load_block(blk1, n1, kBlockBytes);
-    } else if (!o.single_file_pairs) {
-      ok = reader1.load_batch(blk1, n1, kFragmentsPerBatch);
-      if (ok) ok = reader2.load_batch(blk2, n2, kFragmentsPerBatch);
-    } else {
-      ok = reader1.load_batch(blk1, n1, kFragmentsPerBatch * 2);
-    }
-    if (!ok) break;
-    const uint32_t id = block_id++;
-    auto take = [&](Record &r) {
-      batch.bases += r.seq.size();
-      return std::move(r);
-    };
-    if (!o.paired_end_processing) {
-      for (size_t i = 0; i < n1; i++) {
-        batch.r1.push_back(take(blk1[i]));
-        batch.block.push_back(id);
-      }
+      frags = reader1.load_block(b->m1, kBlockBytes);
+      if (!frags) break;
     } else if (!o.single_file_pairs) {
       // a fragment needs both mates; the rest of a longer block is dropped
-      for (size_t i = 0; i < n1 && i < n2; i++) {
-        batch.r1.push_back(take(blk1[i]));
-        batch.r2.push_back(take(blk2[i]));
-        batch.block.push_back(id);
-      }
+      const size_t n1 = reader1.load_batch(b->m1, kFragmentsPerBatch);
+      const size_t n2 = n1 ? reader2.load_batch(b->m2, kFragmentsPerBatch) : 0;
+      frags = std::min(n1, n2);
+      b->m1.truncate(s1 + frags);
+      b->m2.truncate(s2 + frags);
+      if (!frags) break;
     } else {
-      for (size_t i = 0; i + 1 < n1; i += 2) {
-        batch.r1.push_back(take(blk1[i]));
-        batch.r2.push_back(take(blk1[i + 1]));
-        batch.block.push_back(id);
-      }
+      const size_t n1 = reader1.load_batch(b->m1, kFragmentsPerBatch * 2);
+      frags = n1 / 2;
+      b->m1.truncate(s1 + 2 * frags);
+      if (!n1) break;
     }
+    b->m1.mask_low_quality(s1, o.minimum_quality_score);
+    b->m2.mask_low_quality(s2, o.minimum_quality_score);
+    b->block.insert(b->block.end(), frags, block_id++);
     initialize_outputs(o, out);
-    if (batch.bases >= kGpuBatchBases) {
-      cls.run(batch);
-      batch = Batch();
+    if (b->m1.seq.size() + b->m2.seq.size() >= kGpuBatchBases) {
+      pl.submit(b);
+      b = pl.take();
     }
   }
-  cls.run(batch);
+  pl.submit(b);
 }
 
 // ReportStats (src/classify.cc:443-476)
@@ -443,9 +564,8 @@ int main(int argc, char **argv) {
     errx(EX_SOFTWARE, "%s", k2g_last_error());
   k2host::RunCounts rc;
   rc.taxon_reads.assign(tax.nodes.size(), 0);
-  Stats stats;
   Outputs out;
-  Classifier cls(o, db, tax, counters, rc, stats, out);
+  Pipeline pl(o, db, tax, counters, rc, out);
   uint32_t block_id = 0;
 
   timeval tv1, tv2;
@@ -453,18 +573,22 @@ int main(int argc, char **argv) {
   if (o.filenames.empty()) {
     if (o.paired_end_processing && !o.single_file_pairs)
       errx(EX_USAGE, "paired end processing used with no files specified");
-    process_files(nullptr, nullptr, o, cls, out, block_id);
+    process_files(nullptr, nullptr, o, pl, out, block_id);
   } else {
     for (size_t i = 0; i < o.filenames.size(); i++) {
       if (o.paired_end_processing && !o.single_file_pairs) {
-        if (i + 1 == o.filenames.size()) errx(EX_USAGE, "paired end processing used with unpaired file");
-        process_files(o.filenames[i].c_str(), o.filenames[i + 1].c_str(), o, cls, out, block_id);
+        if (i + 1 == o.filenames.size()) {
+          pl.finish();   // the earlier inputs' output is written first
+          errx(EX_USAGE, "paired end processing used with unpaired file");
+        }
+        process_files(o.filenames[i].c_str(), o.filenames[i + 1].c_str(), o, pl, out, block_id);
         i++;
       } else {
-        process_files(o.filenames[i].c_str(), nullptr, o, cls, out, block_id);
+        process_files(o.filenames[i].c_str(), nullptr, o, pl, out, block_id);
       }
     }
   }
+  const Stats stats = pl.finish();
   for (FILE *f : {out.kraken, out.c1, out.c2, out.u1, out.u2})
     if (f) fflush(f);
   gettimeofday(&tv2, nullptr);

@@ -3,16 +3,58 @@
 #include <fcntl.h>
 #include <unistd.h>
 
-#include <cctype>
+#include <cstdio>
+#include <cstring>
 
 namespace k2host {
 
 namespace {
-constexpr size_t kBufSize = 65536;
+constexpr size_t kBufSize = 4u << 20;
+
+// isspace() in the C locale: '\t', '\n', '\v', '\f', '\r' and ' '.
+inline bool is_space(unsigned char c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
+
+template <class T>
+void grow_to(std::vector<T> &v, size_t n) {
+  if (v.capacity() < n) v.reserve(n);
+}
+}  // namespace
+
+int open_input(const char *path) { return path ? open(path, O_RDONLY) : fileno(stdin); }
+
+void RecordSet::clear() {
+  text.clear();
+  seq.clear();
+  seq_off.assign(1, 0);
+  recs.clear();
 }
 
-// Like the reference reader, a file that cannot be opened reads as empty.
-int open_input(const char *path) { return path ? open(path, O_RDONLY) : fileno(stdin); }
+void RecordSet::truncate(size_t n) {
+  if (n >= recs.size()) return;
+  text.resize(recs[n].text);
+  seq.resize(seq_off[n]);
+  seq_off.resize(n + 1);
+  recs.resize(n);
+}
+
+void RecordSet::reserve(size_t seq_bytes, size_t text_bytes, size_t records) {
+  grow_to(seq, seq_bytes);
+  grow_to(text, text_bytes);
+  grow_to(seq_off, records + 1);
+  grow_to(recs, records);
+}
+
+void RecordSet::mask_low_quality(size_t first, int min_quality) {
+  if (min_quality <= 0) return;
+  for (size_t i = first; i < recs.size(); i++) {
+    if (!recs[i].fastq) continue;
+    const signed char *q = reinterpret_cast<const signed char *>(qual(i));
+    char *s = seq_at(i);
+    const uint64_t n = seq_len(i);
+    for (uint64_t j = 0; j < n; j++)
+      if (q[j] - '!' < min_quality) s[j] = 'x';
+  }
+}
 
 SeqReader::SeqReader(int fd) : fd_(fd), own_fd_(fd > 2), buf_(kBufSize) {}
 
@@ -20,71 +62,65 @@ SeqReader::~SeqReader() {
   if (own_fd_) close(fd_);
 }
 
-// Next byte; -1 at the end of input, -3 after a read error.
-int SeqReader::getc() {
-  if (err_) return -3;
-  if (eof_ && begin_ >= end_) return -1;
-  if (begin_ >= end_) {
-    begin_ = 0;
-    end_ = fd_ >= 0 ? ::read(fd_, buf_.data(), kBufSize) : -1;
-    if (end_ == 0) {
-      eof_ = true;
-      return -1;
-    }
-    if (end_ < 0) {
-      eof_ = true;
-      err_ = true;
-      end_ = 0;
-      return -3;
-    }
+// Refills the empty buffer; false at the end of input or after a read error
+// (both are sticky, as in the reference's stream).
+bool SeqReader::refill() {
+  if (eof_ || err_) return false;
+  begin_ = 0;
+  end_ = 0;
+  const ssize_t got = fd_ >= 0 ? ::read(fd_, buf_.data(), buf_.size()) : -1;
+  if (got <= 0) {
+    eof_ = true;
+    err_ = got < 0;
+    return false;
   }
+  end_ = (size_t)got;
+  return true;
+}
+
+// Next byte; -1 at the end of input, -3 after a read error.
+inline int SeqReader::getc() {
+  if (begin_ >= end_ && !refill()) return err_ ? -3 : -1;
   return (unsigned char)buf_[begin_++];
 }
 
-// Reads up to (not including) the delimiter, which is consumed: whitespace
-// for kSpace, '\n' for kLine.  Returns the string length, -1 when the input
-// had ended before anything was read, -3 on a read error.
-int SeqReader::read_until(Until mode, std::string &s, bool append, int *delim) {
+// Appends the bytes up to the delimiter to dst and consumes the delimiter:
+// '\n' for line fields, whitespace otherwise.  `field` is where the field
+// starts in dst (a line field may continue earlier lines).  Returns the
+// field's length, -1 when the input had ended before anything was read, -3
+// on a read error.
+int SeqReader::read_until(bool line, std::vector<char> &dst, size_t field, int *delim) {
   if (delim) *delim = 0;
-  if (!append) s.clear();
   bool got = false;
   for (;;) {
     if (err_) return -3;
-    if (begin_ >= end_) {
-      if (eof_) break;
-      begin_ = 0;
-      end_ = fd_ >= 0 ? ::read(fd_, buf_.data(), kBufSize) : -1;
-      if (end_ == 0) {
-        eof_ = true;
-        break;
-      }
-      if (end_ < 0) {
-        eof_ = true;
-        err_ = true;
-        end_ = 0;
-        return -3;
-      }
+    if (begin_ >= end_ && !refill()) {
+      if (err_) return -3;
+      break;
     }
-    long i = begin_;
-    if (mode == kLine) {
-      while (i < end_ && buf_[i] != '\n') i++;
+    const char *b = buf_.data() + begin_, *e = buf_.data() + end_;
+    const char *p;
+    if (line) {
+      p = static_cast<const char *>(memchr(b, '\n', e - b));
+      if (!p) p = e;
     } else {
-      while (i < end_ && !isspace((unsigned char)buf_[i])) i++;
+      p = b;
+      while (p < e && !is_space((unsigned char)*p)) p++;
     }
     got = true;
-    s.append(buf_.data() + begin_, i - begin_);
-    begin_ = i + 1;
-    if (i < end_) {
-      if (delim) *delim = (unsigned char)buf_[i];
+    dst.insert(dst.end(), b, p);
+    begin_ = (size_t)(p - buf_.data()) + 1;
+    if (p < e) {
+      if (delim) *delim = (unsigned char)*p;
       break;
     }
   }
-  if (!got && eof_ && begin_ >= end_) return -1;
-  if (mode == kLine && s.size() > 1 && s.back() == '\r') s.pop_back();
-  return (int)s.size();
+  if (!got && eof_) return -1;
+  if (line && dst.size() - field > 1 && dst.back() == '\r') dst.pop_back();
+  return (int)(dst.size() - field);
 }
 
-int SeqReader::read(Record &r) {
+int SeqReader::read(RecordSet &s) {
   int c;
   if (last_char_ == 0) {   // find the next header
     while ((c = getc()) >= 0 && c != '>' && c != '@') {
@@ -92,51 +128,64 @@ int SeqReader::read(Record &r) {
     if (c < 0) return c;
     last_char_ = c;
   }
-  r.comment.clear();
-  r.seq.clear();
-  r.qual.clear();
-  int rc = read_until(kSpace, r.name, false, &c);
-  if (rc < 0) return rc;
-  if (c != '\n') read_until(kLine, r.comment, false, nullptr);
+  const size_t t0 = s.text.size(), q0 = s.seq.size();
+  auto undo = [&]() {
+    s.text.resize(t0);
+    s.seq.resize(q0);
+  };
+  int delim;
+  const int r = read_until(false, s.text, t0, &delim);
+  if (r < 0) {
+    undo();
+    return r;
+  }
+  const size_t name_len = s.text.size() - t0;
+  if (delim != '\n') read_until(true, s.text, t0 + name_len, nullptr);
+  const size_t comment_len = s.text.size() - t0 - name_len;
   while ((c = getc()) >= 0 && c != '>' && c != '+' && c != '@') {
     if (c == '\n') continue;
-    r.seq.push_back((char)c);
-    read_until(kLine, r.seq, true, nullptr);
+    s.seq.push_back((char)c);
+    read_until(true, s.seq, q0, nullptr);
   }
   if (c == '>' || c == '@') last_char_ = c;
-  r.fastq = false;
-  if (c != '+') return (int)r.seq.size();   // FASTA
-  while ((c = getc()) >= 0 && c != '\n') {   // rest of the '+' line
+  const size_t seq_len = s.seq.size() - q0;
+  bool fastq = false;
+  if (c == '+') {
+    while ((c = getc()) >= 0 && c != '\n') {   // rest of the '+' line
+    }
+    if (c == -1) {
+      undo();
+      return -2;
+    }
+    const size_t q = s.text.size();
+    while (read_until(true, s.text, q, nullptr) >= 0 && s.text.size() - q < seq_len) {
+    }
+    last_char_ = 0;
+    if (s.text.size() - q != seq_len) {
+      undo();
+      return -2;
+    }
+    fastq = seq_len > 0;
   }
-  if (c == -1) return -2;
-  while (read_until(kLine, r.qual, true, nullptr) >= 0 && r.qual.size() < r.seq.size()) {
-  }
-  last_char_ = 0;
-  if (r.seq.size() != r.qual.size()) return -2;
-  r.fastq = !r.qual.empty();
-  return (int)r.seq.size();
+  s.recs.push_back(RecordRef{t0, (uint32_t)name_len, (uint32_t)comment_len, fastq});
+  s.seq_off.push_back(s.seq.size());
+  return (int)seq_len;
 }
 
-bool SeqReader::load_block(std::vector<Record> &out, size_t &n, size_t block_bytes) {
-  size_t total = 0;
-  n = 0;
+size_t SeqReader::load_block(RecordSet &s, size_t block_bytes) {
+  size_t total = 0, n = 0;
   while (total < block_bytes) {
-    if (n == out.size()) out.emplace_back();
-    if (read(out[n]) < 0) break;
-    total += out[n].seq.size();
+    if (read(s) < 0) break;
+    total += s.seq_len(s.size() - 1);
     n++;
   }
-  return n > 0;
+  return n;
 }
 
-bool SeqReader::load_batch(std::vector<Record> &out, size_t &n, size_t count) {
-  n = 0;
-  while (n < count) {
-    if (n == out.size()) out.emplace_back();
-    if (read(out[n]) < 0) break;
-    n++;
-  }
-  return n > 0;
+size_t SeqReader::load_batch(RecordSet &s, size_t count) {
+  size_t n = 0;
+  while (n < count && read(s) >= 0) n++;
+  return n;
 }
 
 }  // namespace k2host

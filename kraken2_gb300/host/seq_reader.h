@@ -1,8 +1,9 @@
 // FASTA/FASTQ reader with the record semantics of the reference's reader
-// (klib kseq, src/kseq.h:183-222, wrapped by src/seqreader.h:56-178):
+// (klib kseq, src/kseq.h:99-150 and :183-222, wrapped by src/seqreader.h:101-188):
 //   * a record starts at the next '>' or '@' byte, wherever it is;
 //   * the name runs to the first whitespace byte, the comment to the end of
-//     that line (a trailing '\r' is dropped from lines longer than one byte);
+//     that line (a trailing '\r' is dropped from a line field longer than
+//     one byte, counted over everything the field holds so far);
 //   * sequence lines follow until a line starts with '>', '+' or '@';
 //     empty lines are skipped;
 //   * after '+', quality lines are read until they are as long as the
@@ -12,17 +13,49 @@
 //   * a record is FASTQ when it has qualities.
 // Blocks are formed the way the reference's reader threads take them:
 // LoadBlock (sequence bytes up to 3 MiB) and LoadBatch (a record count).
+//
+// Records are appended to a RecordSet: every field of every record goes into
+// two shared arenas (sequences back to back, ready to be handed to the GPU
+// call as one array; names, comments and qualities in the other), so reading
+// allocates nothing per record.  Lines are found with memchr over a 4 MiB
+// input buffer.
 #pragma once
 
 #include <cstdint>
-#include <string>
 #include <vector>
 
 namespace k2host {
 
-struct Record {
-  std::string name, comment, seq, qual;
-  bool fastq = false;
+// Where one record's fields sit in its RecordSet.
+struct RecordRef {
+  uint64_t text;                  // name, then comment, then qualities
+  uint32_t name_len, comment_len;
+  bool fastq;                     // has qualities, as many as sequence bytes
+};
+
+// Records parsed back to back into shared arenas.
+struct RecordSet {
+  std::vector<char> text;             // names, comments, qualities
+  std::vector<char> seq;              // sequences back to back
+  std::vector<uint64_t> seq_off{0};   // record i: seq[seq_off[i], seq_off[i + 1])
+  std::vector<RecordRef> recs;
+
+  size_t size() const { return recs.size(); }
+  void clear();
+  void truncate(size_t n);            // keeps the first n records
+  void reserve(size_t seq_bytes, size_t text_bytes, size_t records);
+
+  const char *name(size_t i) const { return text.data() + recs[i].text; }
+  const char *comment(size_t i) const { return name(i) + recs[i].name_len; }
+  const char *qual(size_t i) const { return comment(i) + recs[i].comment_len; }
+  char *seq_at(size_t i) { return seq.data() + seq_off[i]; }
+  const char *seq_at(size_t i) const { return seq.data() + seq_off[i]; }
+  uint64_t seq_len(size_t i) const { return seq_off[i + 1] - seq_off[i]; }
+
+  // MaskLowQualityBases (src/classify.cc:1061-1071) on records [first, size):
+  // a FASTQ base whose quality byte minus '!' is below min_quality becomes
+  // 'x'.  The byte is taken as signed, as the reference's x86 builds do.
+  void mask_low_quality(size_t first, int min_quality);
 };
 
 class SeqReader {
@@ -32,29 +65,32 @@ class SeqReader {
   SeqReader(const SeqReader &) = delete;
   SeqReader &operator=(const SeqReader &) = delete;
 
-  // >= 0: sequence length; -1: end of input; -2: truncated or mismatched
-  // qualities; -3: read error.
-  int read(Record &r);
+  // Appends the next record to `set`.  >= 0: its sequence length; -1: end of
+  // input; -2: truncated or mismatched qualities; -3: read error.  Nothing is
+  // appended unless the result is >= 0.
+  int read(RecordSet &set);
 
-  // Records until their sequence bytes reach block_bytes (or the input ends).
-  bool load_block(std::vector<Record> &out, size_t &n, size_t block_bytes);
-  // Up to count records.
-  bool load_batch(std::vector<Record> &out, size_t &n, size_t count);
+  // Appends records until their sequence bytes reach block_bytes (or the
+  // input ends); returns how many were appended.
+  size_t load_block(RecordSet &set, size_t block_bytes);
+  // Appends up to count records; returns how many were appended.
+  size_t load_batch(RecordSet &set, size_t count);
 
  private:
-  enum Until { kSpace, kLine };
+  bool refill();
   int getc();
-  int read_until(Until mode, std::string &s, bool append, int *delim);
+  int read_until(bool line, std::vector<char> &dst, size_t field, int *delim);
 
   int fd_;
   bool own_fd_;
   std::vector<char> buf_;
-  long begin_ = 0, end_ = 0;
+  size_t begin_ = 0, end_ = 0;
   bool eof_ = false, err_ = false;
   int last_char_ = 0;
 };
 
-// Opens a file (nullptr: standard input); exits with a message on failure.
+// Opens a file (nullptr: standard input).  Like the reference reader, a file
+// that cannot be opened reads as empty.
 int open_input(const char *path);
 
 }  // namespace k2host

@@ -396,9 +396,12 @@ static void ws_reserve(ko_ws *w, size_t n) {
   w->m2 = (char *)realloc(w->m2, n);
 }
 
+/* MaskLowQualityBases (src/classify.cc:1061-1071).  The reference subtracts
+ * from a std::string char, signed on the x86 builds it ships for, so quality
+ * bytes >= 0x80 count as negative; the cast keeps that on every platform. */
 static const char *mask_into(const char *seq, const char *qual, size_t len, int minq, char *buf) {
   if (minq <= 0 || !qual) return seq;
-  for (size_t i = 0; i < len; i++) buf[i] = ((qual[i] - '!') < minq) ? 'x' : seq[i];
+  for (size_t i = 0; i < len; i++) buf[i] = (((signed char)qual[i] - '!') < minq) ? 'x' : seq[i];
   return buf;
 }
 
