@@ -114,34 +114,55 @@ __device__ __forceinline__ int64_t seg_index(const EventView &ev, uint64_t j) {
 }
 
 // Kept events: one count per (taxon, block) and one (encoding, preorder)
-// key appended to the run's accumulator.
+// key appended to the run's accumulator.  A block takes tiles of
+// kCountRounds x blockDim events and reserves the tile's accumulator range
+// with one global atomic (per-warp reservations on one counter serialise);
+// the accumulator is sorted afterwards, so the order within it is free.
+constexpr int kCountRounds = 8;
+
 __global__ void count_kernel(EventView ev, uint32_t *seg, const uint32_t *pre, int tbits,
                              uint64_t *acc, unsigned long long *acc_used) {
+  __shared__ uint32_t s_n;
+  __shared__ unsigned long long s_base;
   const unsigned lane = threadIdx.x & 31;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  // the loop bound is uniform per warp (i0 is the warp's first event)
-  for (uint64_t i0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; i0 < ev.n;
-       i0 += stride) {
-    const uint64_t j = i0 + lane;
-    bool keep = false;
-    uint64_t key = 0;
-    int64_t si = -1;
-    if (j < ev.n) {
-      si = seg_index(ev, j);
-      if (si >= 0) {
-        keep = true;
-        key = ((uint64_t)hll_encode(hll_hash(ev.keys[j])) << tbits) | pre[ev.taxa[j]];
+  const uint64_t tile = (uint64_t)blockDim.x * kCountRounds;
+  // the loop bound is uniform per block
+  for (uint64_t t0 = blockIdx.x * tile; t0 < ev.n; t0 += (uint64_t)gridDim.x * tile) {
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    uint64_t key[kCountRounds];
+    uint32_t at[kCountRounds];   // slot within the tile's range, or ~0
+#pragma unroll
+    for (int r = 0; r < kCountRounds; r++) {
+      const uint64_t j = t0 + (uint64_t)r * blockDim.x + threadIdx.x;
+      bool keep = false;
+      int64_t si = -1;
+      key[r] = 0;
+      if (j < ev.n) {
+        si = seg_index(ev, j);
+        if (si >= 0) {
+          keep = true;
+          key[r] = ((uint64_t)hll_encode(hll_hash(ev.keys[j])) << tbits) | pre[ev.taxa[j]];
+        }
       }
+      // one atomic per distinct (taxon, block) in the warp: a read's hits
+      // mostly fall on one taxon, and a warp holds a few reads' events
+      const unsigned same = __match_any_sync(0xffffffffu, (unsigned long long)si);
+      if (si >= 0 && (__ffs(same) - 1) == (int)lane) atomicAdd(&seg[si], (unsigned)__popc(same));
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      uint32_t wbase = 0;
+      if (lane == 0 && m) wbase = atomicAdd(&s_n, (uint32_t)__popc(m));
+      wbase = __shfl_sync(0xffffffffu, wbase, 0);
+      at[r] = keep ? wbase + __popc(m & ((1u << lane) - 1)) : 0xFFFFFFFFu;
     }
-    // one atomic per distinct (taxon, block) in the warp: a read's hits
-    // mostly fall on one taxon, and a warp holds a few reads' events
-    const unsigned same = __match_any_sync(0xffffffffu, (unsigned long long)si);
-    if (si >= 0 && (__ffs(same) - 1) == (int)lane) atomicAdd(&seg[si], (unsigned)__popc(same));
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    unsigned long long base = 0;
-    if (lane == 0 && m) base = atomicAdd(acc_used, (unsigned long long)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) acc[base + __popc(m & ((1u << lane) - 1))] = key;
+    __syncthreads();
+    if (threadIdx.x == 0) s_base = s_n ? atomicAdd(acc_used, (unsigned long long)s_n) : 0ull;
+    __syncthreads();
+    const uint64_t base = s_base;
+#pragma unroll
+    for (int r = 0; r < kCountRounds; r++)
+      if (at[r] != 0xFFFFFFFFu) acc[base + at[r]] = key[r];
+    __syncthreads();
   }
 }
 
@@ -260,38 +281,46 @@ __global__ void run_count_kernel(const uint64_t *k, uint64_t n, uint32_t *tile_c
   if (threadIdx.x == 0) tile_cnt[blockIdx.x] = c;
 }
 
+// Round r of a tile covers keys t0 + r*kThreads .. +kThreads-1 (coalesced);
+// warps write their first-of-run keys in order after a per-round count.
 __global__ void run_write_kernel(const uint64_t *k, uint64_t n, const uint32_t *tile_off,
                                  uint64_t *out) {
-  __shared__ uint32_t s_cnt[rsort::kThreads];
+  __shared__ uint32_t s_wcnt[rsort::kWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t t0 = (uint64_t)blockIdx.x * rsort::kTile;
-  // thread j owns keys t0 + j*16 .. +15, so order is kept by a block scan
-  uint32_t mine = 0;
-  const uint64_t b0 = t0 + (uint64_t)threadIdx.x * rsort::kPerThread;
+  uint64_t w = tile_off[blockIdx.x];
   for (int r = 0; r < rsort::kPerThread; r++) {
-    const uint64_t i = b0 + r;
-    if (i < n && (i == 0 || k[i] != k[i - 1])) mine++;
-  }
-  s_cnt[threadIdx.x] = mine;
-  __syncthreads();
-  for (int o = 1; o < rsort::kThreads; o <<= 1) {
-    const uint32_t add = threadIdx.x >= (unsigned)o ? s_cnt[threadIdx.x - o] : 0;
+    const uint64_t i = t0 + (uint64_t)r * rsort::kThreads + threadIdx.x;
+    const uint64_t key = i < n ? k[i] : 0;
+    const bool first = i < n && (i == 0 || key != k[i - 1]);
+    const unsigned m = __ballot_sync(0xffffffffu, first);
+    if (lane == 0) s_wcnt[warp] = __popc(m);
     __syncthreads();
-    s_cnt[threadIdx.x] += add;
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int q = 0; q < rsort::kWarps; q++) {
+      const uint32_t c = s_wcnt[q];
+      before += q < warp ? c : 0;
+      total += c;
+    }
+    if (first) out[w + before + __popc(m & ((1u << lane) - 1))] = key;
+    w += total;
     __syncthreads();
-  }
-  uint64_t w = tile_off[blockIdx.x] + s_cnt[threadIdx.x] - mine;
-  for (int r = 0; r < rsort::kPerThread; r++) {
-    const uint64_t i = b0 + r;
-    if (i < n && (i == 0 || k[i] != k[i - 1])) out[w++] = k[i];
   }
 }
 
+// Per taxonomy node, packed so a walk step is one 16-byte load: preorder
+// number, one past the last preorder of its subtree, parent, and where its
+// sketch lives: a dense clade's register block (< kHotTag), kHotTag | h for
+// one of the kHot sparse clades with the most events (histogram kept in
+// shared memory by each block, flushed once), or ~0 for other sparse clades.
+constexpr int kHot = 64;
+constexpr uint32_t kHotTag = 0x40000000u;
+
 struct CladeView {
   const uint32_t *node_of;   // preorder -> taxon
-  const uint32_t *pre;       // taxon -> preorder
-  const uint32_t *end;       // taxon -> one past the last preorder of its subtree
-  const uint32_t *parent;
-  const uint32_t *slot;      // taxon -> register block of a dense clade, or ~0
+  const uint4 *node;         // taxon -> {pre, end, parent, sketch}
+  const uint32_t *hot;       // [kHot] taxon of each shared-memory histogram
   uint32_t *regs;            // [dense clades][4096]
   uint32_t *hist;            // [node][kHist] rank counts of sparse clades (their
                              // sum is the number of distinct encodings)
@@ -300,25 +329,39 @@ struct CladeView {
 // Keys are (encoding << tbits | preorder), sorted and unique.  Within one
 // encoding, taxa come in preorder, so the union of their root paths is the
 // disjoint union, over each taxon, of its path up to (not including) the
-// lowest ancestor it shares with the previous taxon of that encoding.
+// lowest ancestor it shares with the previous taxon of that encoding.  Every
+// distinct encoding reaches the root, so the upper clades' histogram bins
+// take most of the increments: those clades count in shared memory.
 __global__ void clade_walk_kernel(const uint64_t *k, uint64_t n, int tbits, CladeView cv) {
+  __shared__ uint32_t s_hot[kHot * kHist];
+  for (int i = threadIdx.x; i < kHot * kHist; i += blockDim.x) s_hot[i] = 0;
+  __syncthreads();
   const uint64_t pmask = (1ull << tbits) - 1;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t e = (uint32_t)(k[i] >> tbits);
-    const uint32_t x = cv.node_of[k[i] & pmask];
+    const uint64_t key = k[i];
+    const uint32_t e = (uint32_t)(key >> tbits);
     uint32_t prev_pre = 0xFFFFFFFFu;
-    if (i > 0 && (uint32_t)(k[i - 1] >> tbits) == e) prev_pre = (uint32_t)(k[i - 1] & pmask);
-    const uint32_t r = hll_rank(e), idx = e >> (32 - kHllP);
-    for (uint32_t a = x; a; a = cv.parent[a]) {
-      if (prev_pre != 0xFFFFFFFFu && cv.pre[a] <= prev_pre && prev_pre < cv.end[a]) break;
-      const uint32_t sl = cv.slot[a];
-      if (sl != 0xFFFFFFFFu) {
-        atomicMax(&cv.regs[(uint64_t)sl * (1u << kHllP) + idx], r);
-      } else {
-        atomicAdd(&cv.hist[(uint64_t)a * kHist + (r < kHist ? r : kHist - 1)], 1u);
-      }
+    if (i > 0) {
+      const uint64_t pk = k[i - 1];
+      if ((uint32_t)(pk >> tbits) == e) prev_pre = (uint32_t)(pk & pmask);
     }
+    const uint32_t r = hll_rank(e), idx = e >> (32 - kHllP);
+    const uint32_t bin = r < kHist ? r : kHist - 1;
+    for (uint32_t a = cv.node_of[key & pmask]; a;) {
+      const uint4 nd = cv.node[a];
+      if (prev_pre != 0xFFFFFFFFu && nd.x <= prev_pre && prev_pre < nd.y) break;
+      const uint32_t sk = nd.w;
+      if (sk == 0xFFFFFFFFu) atomicAdd(&cv.hist[(uint64_t)a * kHist + bin], 1u);
+      else if (sk & kHotTag) atomicAdd(&s_hot[(sk & (kHot - 1)) * kHist + bin], 1u);
+      else atomicMax(&cv.regs[(uint64_t)sk * (1u << kHllP) + idx], r);
+      a = nd.z;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kHot * kHist; i += blockDim.x) {
+    const uint32_t v = s_hot[i];
+    if (v) atomicAdd(&cv.hist[(uint64_t)cv.hot[i / kHist] * kHist + i % kHist], v);
   }
 }
 
@@ -351,6 +394,7 @@ struct k2g_counters {
   uint64_t node_count = 0;
   int tbits = 0;                       // bits of a preorder number
   std::vector<uint32_t> parent;        // host copy of the taxonomy
+  std::vector<uint32_t> pre, end;      // DFS preorder numbers and subtree ends
   uint32_t *d_pre = nullptr, *d_end = nullptr, *d_node_of = nullptr;
   uint64_t *d_nobs = nullptr;          // add_kmer calls per taxon
   uint8_t *d_dense = nullptr;          // some block's sketch of the taxon went dense
@@ -564,6 +608,8 @@ extern "C" k2g_status k2g_counters_create(const k2g_db *db, k2g_counters **out) 
       }
     }
   }
+  c->pre = pre;
+  c->end = end;
   uint64_t dummy = 0;
   if ((e = cudaMalloc(&c->d_pre, n * 4)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_end, n * 4)) != cudaSuccess ||
@@ -722,23 +768,40 @@ extern "C" k2g_status k2g_counters_finish(k2g_counters *c, uint64_t *taxon_kmers
       clade_of_slot.push_back((uint32_t)t);
     }
   const uint64_t nd = clade_of_slot.size();
-  uint32_t *d_slot = nullptr, *d_cos = nullptr, *d_regs = nullptr, *d_hist = nullptr;
+  if (nd >= kHotTag) return fail(K2G_ERR_BUDGET, "too many dense clades");
+  // the sparse clades with the most events count in shared memory
+  std::vector<uint32_t> hot;
+  for (uint64_t t = 1; t < n; t++)
+    if (!dense_clade[t] && clade_kmers[t]) hot.push_back((uint32_t)t);
+  const size_t n_hot = std::min<size_t>(hot.size(), kHot);
+  std::partial_sort(hot.begin(), hot.begin() + n_hot, hot.end(), [&](uint32_t x, uint32_t y) {
+    return clade_kmers[x] != clade_kmers[y] ? clade_kmers[x] > clade_kmers[y] : x < y;
+  });
+  hot.resize(n_hot);
+  std::vector<uint4> node(n);
+  for (uint64_t t = 0; t < n; t++) node[t] = make_uint4(c->pre[t], c->end[t], c->parent[t], slot[t]);
+  for (size_t h = 0; h < n_hot; h++) node[hot[h]].w = kHotTag | (uint32_t)h;
+  hot.resize(kHot, 0);
+  uint4 *d_node = nullptr;
+  uint32_t *d_hot = nullptr, *d_cos = nullptr, *d_regs = nullptr, *d_hist = nullptr;
   auto release = [&]() {
-    for (void *p : {(void *)d_slot, (void *)d_cos, (void *)d_regs, (void *)d_hist})
+    for (void *p : {(void *)d_node, (void *)d_hot, (void *)d_cos, (void *)d_regs, (void *)d_hist})
       if (p) cudaFree(p);
   };
   std::vector<uint32_t> hist(n * kHist);
   cudaError_t e = cudaSuccess;
   do {
-    if ((e = cudaMalloc(&d_slot, n * 4)) != cudaSuccess) break;
+    if ((e = cudaMalloc(&d_node, n * sizeof(uint4))) != cudaSuccess) break;
+    if ((e = cudaMalloc(&d_hot, kHot * 4)) != cudaSuccess) break;
     if ((e = cudaMalloc(&d_cos, std::max<uint64_t>(nd, 1) * 4)) != cudaSuccess) break;
     if ((e = cudaMalloc(&d_regs, std::max<uint64_t>(nd, 1) * (4ull << kHllP))) != cudaSuccess) break;
     if ((e = cudaMalloc(&d_hist, n * kHist * 4)) != cudaSuccess) break;
-    if ((e = cudaMemcpyAsync(d_slot, slot.data(), n * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(d_node, node.data(), n * sizeof(uint4), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(d_hot, hot.data(), kHot * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
     if (nd && (e = cudaMemcpyAsync(d_cos, clade_of_slot.data(), nd * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(d_regs, 0, std::max<uint64_t>(nd, 1) * (4ull << kHllP), st)) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(d_hist, 0, n * kHist * 4, st)) != cudaSuccess) break;
-    CladeView cv{c->d_node_of, c->d_pre, c->d_end, c->db->d_parent, d_slot, d_regs, d_hist};
+    CladeView cv{c->d_node_of, d_node, d_hot, d_regs, d_hist};
     if (c->acc_used) {
       clade_walk_kernel<<<grid_for(c->device, c->acc_used), 256, 0, st>>>(c->d_acc, c->acc_used,
                                                                           c->tbits, cv);
