@@ -177,7 +177,11 @@ typedef enum {
                                  fragment runs it as K2G_MODE_PERSISTENT   */
 } k2g_mode;
 
-/* Classifies a batch of fragments held in device memory. */
+/* Classifies a batch of fragments held in device memory.  Calls on one
+ * stream run in order; calls on different streams may run at the same time
+ * (up to eight streams per device get scratch of their own, further streams
+ * share it and are serialised with their sharers), so a caller with several
+ * batches in flight overlaps one batch's tail with the next batch's work. */
 k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
                         const k2g_classify_params *params, k2g_results *out,
                         int mode, void *stream);

@@ -339,7 +339,10 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
       rs.hits_cap = s.cap_hits;
       rs.d_hits_used = s.hits_used;
     }
-    status = k2g_classify(db, &rd, params, &rs, K2G_MODE_PIPELINED, s.st);
+    // short-read chunks share one execution state (in order, as overlapping
+    // them only adds interference); long-read chunks overlap their tails
+    const void *key = long_batch(nb, nf) ? (const void *)s.st : (const void *)&hc;
+    status = classify_keyed(db, &rd, params, &rs, K2G_MODE_PIPELINED, s.st, key);
     if (status != K2G_OK) { settle(); return status; }
     if (counters) {
       status = k2g_counters_add(counters, &rd, &rs, s.st);

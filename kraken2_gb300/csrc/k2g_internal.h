@@ -89,6 +89,24 @@ void note_launches(uint64_t n = 1);
 // One round (< 2^30 pairs) of the order-exact build insert (build_ordered.cu).
 k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
                                 uint64_t n, cudaStream_t st);
+
+// A batch averaging more than this many bases per fragment (mates together)
+// is mostly long fragments: the pipelined mode runs it on the fused
+// persistent kernel, whose tail is the longest fragment walked by one lane.
+constexpr double kLongBatchAvg = 512.0;
+inline bool long_batch(uint64_t total_bases, uint64_t n_frags) {
+  return (double)total_bases > kLongBatchAvg * (double)n_frags;
+}
+
+// k2g_classify with the execution state chosen by `state_key` instead of
+// the stream: calls with one key run in order on that state's internal
+// stream, calls with different keys may overlap.  The host-buffer paths
+// keep short-read batches on one key (overlapping them only adds
+// interference) and give long-read batches a key per stream (one batch's
+// tail then overlaps the next batch).
+k2g_status classify_keyed(const k2g_db *db, const k2g_reads *reads,
+                          const k2g_classify_params *params, k2g_results *out, int mode,
+                          void *stream, const void *state_key);
 }  // namespace k2g
 
 #define K2G_CUDA_TRY(call)                                        \

@@ -226,12 +226,18 @@ static void launch_scan(const ScanView &sv, const uint8_t *bases, const uint64_t
   note_launches();
 }
 
-// Classification runs on one internal stream per device, joined to the
-// caller's stream through events (calls stay asynchronous and capturable,
-// and concurrent callers never share scratch in flight).  Each sub-batch in
-// flight owns an execution context: every piece of device scratch its
-// kernels use (work counter, deferred-fragment list, slow-path scratch,
-// pipeline buffers).  The pipelined mode keeps three sub-batches in flight.
+// Classification runs on an internal stream joined to the caller's stream
+// through events (calls stay asynchronous and capturable).  Each device has
+// a few execution states, each with its own internal stream and scratch,
+// chosen by a key: k2g_classify uses the caller's stream, so calls from one
+// stream run in order and calls from different streams can run at the same
+// time (one call's tail -- a few long fragments on a few lanes -- then
+// overlaps the next call's work).  Once every state is taken, further keys
+// share them and are serialised with their sharers; scratch is never shared
+// in flight.  Each sub-batch in flight owns an execution context: every
+// piece of device scratch its kernels use (work counter, deferred-fragment
+// list, slow-path scratch, pipeline buffers).  The pipelined mode keeps three
+// sub-batches in flight.
 struct ExecCtx {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
@@ -264,7 +270,29 @@ struct DeviceState {
   uint64_t defer_cap = 0, defer2_cap = 0;
   unsigned long long *counters = nullptr;
 };
-static DeviceState g_state[64];
+constexpr int kStatesPerDevice = 8;   // state_for picks among them with the top three hash bits
+struct DeviceStates {
+  std::mutex mu;
+  DeviceState state[kStatesPerDevice];
+  const void *owner[kStatesPerDevice] = {};
+  int used = 0;
+};
+static DeviceStates g_states[64];
+
+// The execution state of calls with `key` (the caller's stream for
+// k2g_classify).
+static DeviceState &state_for(int dev, const void *key) {
+  DeviceStates &d = g_states[dev & 63];
+  std::lock_guard<std::mutex> lock(d.mu);
+  for (int i = 0; i < d.used; i++)
+    if (d.owner[i] == key) return d.state[i];
+  if (d.used < kStatesPerDevice) {
+    d.owner[d.used] = key;
+    return d.state[d.used++];
+  }
+  // keys are aligned pointers: mix the bits before picking
+  return d.state[((uint64_t)(uintptr_t)key * 0x9E3779B97F4A7C15ull) >> 61];
+}
 
 template <class T>
 static cudaError_t grow(T *&p, uint64_t &cap, uint64_t want) {
@@ -435,9 +463,10 @@ static PipeArgs pipe_view(const ClassifyArgs &a, const ExecCtx &c) {
 }
 
 static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mode,
-                               uint64_t max_len, uint64_t total_bases, cudaStream_t caller) {
+                               uint64_t max_len, uint64_t total_bases, cudaStream_t caller,
+                               const void *state_key) {
   const int dev = db->device;
-  DeviceState &ds = g_state[dev & 63];
+  DeviceState &ds = state_for(dev, state_key);
   std::lock_guard<std::mutex> lock(ds.mu);
   if (!ds.init) {
     K2G_CUDA_TRY(cudaStreamCreateWithFlags(&ds.st, cudaStreamNonBlocking));
@@ -447,12 +476,10 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
   }
   const int per = a0.cls.paired ? 2 : 1;
   // The pipeline is fastest on short fragments.  A batch whose fragments
-  // average more than kPipeMaxAvg bases (mates together) is mostly long
+  // average more than kLongBatchAvg bases (mates together) is mostly long
   // fragments, which the fused persistent kernel walks in segments with work
   // stealing; the pipeline would defer most of them to it anyway.
-  constexpr double kPipeMaxAvg = 512.0;
-  const bool pipeline = mode == K2G_MODE_PIPELINED &&
-                        (double)total_bases <= kPipeMaxAvg * (double)a0.n_frags;
+  const bool pipeline = mode == K2G_MODE_PIPELINED && !long_batch(total_bases, a0.n_frags);
   if (mode == K2G_MODE_PIPELINED && !pipeline) mode = K2G_MODE_PERSISTENT;
   uint64_t sb = a0.n_frags, cap_slots = 0;
   if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, sb, cap_slots);
@@ -642,6 +669,12 @@ extern "C" k2g_status k2g_scan(const k2g_db *db, const char *d_bases, const uint
 extern "C" k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
                                    const k2g_classify_params *params, k2g_results *out,
                                    int mode, void *stream) {
+  return k2g::classify_keyed(db, reads, params, out, mode, stream, stream);
+}
+
+k2g_status k2g::classify_keyed(const k2g_db *db, const k2g_reads *reads,
+                               const k2g_classify_params *params, k2g_results *out, int mode,
+                               void *stream, const void *state_key) {
   if (!db || !reads || !params || !out) return fail(K2G_ERR_ARG, "null argument");
   if (!reads->n_frags) return K2G_OK;
   if (!reads->d_bases || !reads->d_seq_off || !out->d_call || !out->d_runs || !out->d_status)
@@ -694,7 +727,7 @@ extern "C" k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
     K2G_CUDA_TRY(cudaStreamSynchronize(st));
     total = ends[1] - ends[0];
   }
-  return run_classify(db, a, mode, reads->max_seq_len, total, st);
+  return run_classify(db, a, mode, reads->max_seq_len, total, st, state_key);
 }
 
 extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,

@@ -7,9 +7,12 @@
 // large one is split over several batches.  Each of two slots owns device
 // and pinned buffers sized from the HBM budget given at creation -- that
 // budget is the admission limit; requests wait in the queue until a slot is
-// free.  One slot's copies overlap the other slot's classification (the
-// classification kernels of a device run in submission order).  Results are
-// scattered back per request; a request is done when all of its pieces are.
+// free.  Each slot has its own stream, so one slot's copies overlap the
+// other's classification; batches of mostly long fragments may also run at
+// the same time as the other slot's (a batch's tail of long fragments on a
+// few lanes then overlaps the next batch).  Results
+// are scattered back per request; a request is done when all of its pieces
+// are.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -240,7 +243,11 @@ k2g_status launch(k2g_server *sv, Slot &s) {
   rs.d_runs = s.d_sparse;
   rs.runs_cap = sv->cap_bases + 2 * sv->cap_frags + 8;
   rs.d_status = s.d_status;
-  k2g_status st = k2g_classify(sv->db, &rd, &sv->params, &rs, K2G_MODE_PIPELINED, s.st);
+  // a batch of mostly long fragments may overlap the other slot's batch
+  // (its tail is a few long fragments on a few lanes); short-read batches
+  // run in order on one execution state
+  const void *key = long_batch(bb, fb) ? (const void *)s.st : (const void *)sv;
+  k2g_status st = classify_keyed(sv->db, &rd, &sv->params, &rs, K2G_MODE_PIPELINED, s.st, key);
   if (st != K2G_OK) return st;
   st = compact_runs(s.d_sparse, s.d_off, sv->per, s.d_hlen, fb, s.d_excl, s.d_sums, s.d_total,
                     s.d_dense, s.st);
@@ -345,7 +352,8 @@ void worker_loop(k2g_server *sv) {
     if (launched) continue;
     std::unique_lock<std::mutex> lock(sv->mu);
     if (sv->stop) return;
-    const bool busy = sv->slots[0].busy || sv->slots[1].busy;
+    bool busy = false;
+    for (const Slot &s : sv->slots) busy = busy || s.busy;
     if (sv->queue.empty() && !busy) sv->cv_work.wait(lock, [&] { return sv->stop || !sv->queue.empty(); });
     else sv->cv_work.wait_for(lock, std::chrono::microseconds(50));
   }
