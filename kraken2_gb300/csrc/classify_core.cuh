@@ -58,6 +58,23 @@ struct Window {
   }
 };
 
+// A piece of a long single-end fragment (classify_split.cu): the tokens of
+// the k-mers ending at positions [lo, hi).  A cut lies where the reference's
+// token stream starts afresh -- the k-mers ending at lo - 1 and lo are both
+// unambiguous and have different minimizers, so the token at lo is a new
+// lookup (or a min-hash skip) and no REPEAT carries a taxon over the cut.
+// The pieces' counts, hit groups and runs then simply add up.
+constexpr int kPieceMap = 16;
+struct SplitPiece {
+  uint64_t frag;          // fragment index in the view
+  uint64_t last_min;      // minimizer of the k-mer ending at lo - 1
+  uint32_t lo, hi;        // hi == 0: unused slot
+  uint32_t index;         // piece number within its fragment
+  // results
+  uint32_t hit_groups, tokens, n_runs, n_map, status;   // status 1: map overflow
+  uint32_t map_taxon[kPieceMap], map_count[kPieceMap];
+};
+
 // Everything a classify kernel needs, passed by value.
 struct ClassifyArgs {
   TableView table;
@@ -96,6 +113,10 @@ struct ClassifyArgs {
   // slow-path scratch (global memory per thread)
   uint64_t *scratch;
   uint64_t scratch_stride;         // 64-bit words per thread
+  // long fragments classified as pieces
+  const uint8_t *split_mark;       // per fragment of the view: 1 = its pieces carry it
+  SplitPiece *pieces;              // piece mode: lanes take pieces instead of fragments
+  const unsigned long long *n_pieces;
 };
 
 // Per-lane storage accessors.  Shared-memory flavour: interleaved by lane.
@@ -173,6 +194,8 @@ struct Lane {
   uint32_t distinct;
   bool quick_stop;
   uint64_t run_base;
+  int32_t emit_lo;        // first position that emits a token (k - 1, or a piece's lo)
+  uint64_t piece;         // piece being classified, ~0 = a whole fragment
 };
 
 __device__ __forceinline__ uint4 load_chunk(const uint8_t *ap, uint32_t i, uint32_t n) {
@@ -235,6 +258,37 @@ __device__ __forceinline__ void lane_begin(Lane<W> &s, const ClassifyArgs &a, ui
   s.distinct = 0;
   s.quick_stop = false;
   s.run_base = o0 + 2 * (f + a.frag_off);
+  s.emit_lo = a.scan.k - 1;
+  s.piece = ~0ull;
+}
+
+// A piece of a single-end fragment: the whole read as its mate, scanned from
+// k bases before the piece (the scanner state at lo then equals that of a
+// scan from the read's start: l-mer window, ambiguity and the previous
+// minimizer, given by the plan), tokens only for [lo, hi), and its runs at
+// the fragment's run region shifted by the tokens before lo.
+template <int W>
+__device__ __forceinline__ void lane_begin_piece(Lane<W> &s, const ClassifyArgs &a, uint64_t pi) {
+  const SplitPiece &pc = a.pieces[pi];
+  lane_begin(s, a, pc.frag);
+  s.piece = pi;
+  const uint32_t k = (uint32_t)a.scan.k;
+  s.len = pc.hi;
+  s.nchunks = (s.head + pc.hi + 15) / 16;
+  if (pc.lo > k - 1) {
+    const uint32_t ci0 = (s.head + pc.lo - k) / 16;
+    s.ci = ci0;
+    s.c0 = load_chunk(s.ap, ci0, s.nchunks);
+    s.c1 = load_chunk(s.ap, ci0 + 1, s.nchunks);
+    if (s.aq) {
+      s.q0 = load_chunk(s.aq, ci0, s.nchunks);
+      s.q1 = load_chunk(s.aq, ci0 + 1, s.nchunks);
+    }
+    s.emit_lo = (int32_t)pc.lo;
+    s.last_min = pc.last_min;
+  }
+  s.key_ordinal = pc.index << 16;   // key ordinals stay monotone over the pieces
+  s.run_base += pc.lo - (k - 1);
 }
 
 // ---- scan phase ----------------------------------------------------------
@@ -287,7 +341,7 @@ __device__ __forceinline__ void scan_base(Lane<W> &s, Store &st, const ScanConst
   uint64_t cand = ((s.fwd < rcv ? s.fwd : rcv) & c.smask) ^ c.toggle;
   cand = (s.run >= c.l) ? cand : ~0ull;
   s.win.push(cand);
-  const bool emit = (p >= c.k - 1) && (p < (int32_t)s.len);
+  const bool emit = (p >= s.emit_lo) && (p < (int32_t)s.len);
   const bool amb = (p - s.last_amb) <= c.amb_span;
   const uint64_t m = s.win.min(c.w) ^ c.toggle;
   const bool nonamb = emit && !amb;
@@ -564,6 +618,34 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
   if (call && a.taxon_reads) atomicAdd(a.taxon_reads + call, 1ull);
   // clear this lane's map for the next fragment
   for (int i = 0; i < cap; i++) st.map_key(i) = 0;
+}
+
+// The end of a piece: its runs are already in place (the last one is written
+// here); counts, hit groups and the taxon map go to the piece record for the
+// merge (classify_split.cu), and the lane's map is cleared.
+template <class L, class Store>
+__device__ __forceinline__ void finish_piece(L &s, Store &st, const ClassifyArgs &a) {
+  if (s.run_cnt) {
+    uint64_t at = s.run_base + s.n_runs;
+    if (at < a.runs_cap) a.runs[at] = ((uint64_t)s.run_code << 32) | s.run_cnt;
+    else atomicOr(a.status, STATUS_RUNS_OVERFLOW);
+    s.n_runs++;
+    s.run_cnt = 0;
+  }
+  SplitPiece &pc = a.pieces[s.piece];
+  pc.hit_groups = s.hit_groups;
+  pc.tokens = s.total_tokens;
+  pc.n_runs = s.n_runs;
+  uint32_t n = 0;
+  for (int i = 0; i < st.map_cap(); i++) {
+    const uint32_t t = st.map_key(i);
+    if (!t) continue;
+    pc.map_taxon[n] = t;
+    pc.map_count[n] = st.map_cnt(i);
+    n++;
+    st.map_key(i) = 0;
+  }
+  pc.n_map = n;
 }
 
 }  // namespace k2g

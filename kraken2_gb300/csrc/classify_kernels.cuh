@@ -18,38 +18,52 @@ using FastStore = SmemStore<kKCap, kGCap, kMCap>;
 constexpr int kSlowKCap = 256, kSlowGCap = 320;
 using SlowStore = GlobalStore<kSlowKCap, kSlowGCap>;
 
+static_assert(kMCap <= kPieceMap, "a piece record holds a lane's whole taxon map");
+
+// Gives idle lanes work; returns true when the lane holds a fragment (or a
+// piece) afterwards.  Persistent lanes take indices from a global counter
+// until every lane has work or the source is exhausted; a fragment carried
+// by pieces (split_mark) and an unused piece slot are passed over.
 template <int W>
 __device__ __forceinline__ bool lane_fetch(Lane<W> &s, const ClassifyArgs &a, bool persistent,
                                            bool &exhausted, uint64_t first) {
-  // Returns true when the lane holds a fragment afterwards.
   const unsigned lane = threadIdx.x & 31;
   if (!persistent) {
     if (s.frag == ~0ull && !exhausted) {
       exhausted = true;
-      if (first < a.n_frags) {
+      if (first < a.n_frags && !(a.split_mark && a.split_mark[first])) {
         lane_begin(s, a, first);
         return true;
       }
     }
     return s.frag != ~0ull;
   }
-  bool need = (s.frag == ~0ull) && !exhausted;
-  unsigned m = __ballot_sync(0xffffffffu, need);
-  if (m) {
-    int leader = __ffs(m) - 1;
+  while (true) {
+    const bool need = (s.frag == ~0ull) && !exhausted;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) break;
+    const int leader = __ffs(m) - 1;
     unsigned long long base = 0;
     if ((int)lane == leader) base = atomicAdd(a.next_frag, (unsigned long long)__popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
     if (need) {
-      uint64_t f = base + __popc(m & ((1u << lane) - 1));
-      if (a.in_list) {   // list mode: the fragments deferred by the pipeline
-        const uint64_t n = min((uint64_t)*a.in_count, a.in_cap);
-        if (f < n) lane_begin(s, a, a.in_list[f]);
-        else exhausted = true;
-      } else if (f < a.n_frags) {
-        lane_begin(s, a, f);
+      const uint64_t i = base + __popc(m & ((1u << lane) - 1));
+      if (a.pieces) {   // piece mode: n_frags is the piece buffer's capacity
+        if (i < min((uint64_t)*a.n_pieces, a.n_frags)) {
+          if (a.pieces[i].hi) lane_begin_piece(s, a, i);
+        } else {
+          exhausted = true;
+        }
       } else {
-        exhausted = true;
+        uint64_t f = ~0ull;
+        if (a.in_list) {   // list mode: the fragments deferred by the pipeline
+          const uint64_t n = min((uint64_t)*a.in_count, a.in_cap);
+          if (i < n) f = a.in_list[i];
+        } else if (i < a.n_frags) {
+          f = i;
+        }
+        if (f == ~0ull) exhausted = true;
+        else if (!(a.split_mark && a.split_mark[f])) lane_begin(s, a, f);
       }
     }
   }
@@ -88,11 +102,19 @@ classify_kernel(ClassifyArgs a, int persistent) {
       bool ok = replay_segment(s, st, a, ng);
       s.key_ordinal += nk;
       if (!ok) {
-        // taxon map overflow: hand the fragment to the slow path
-        unsigned long long at = atomicAdd(a.defer_count, 1ull);
-        if (at < a.defer_cap) a.defer_list[at] = s.frag;
-        else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
+        // taxon map overflow: hand the fragment to the slow path (a piece
+        // marks its record; the merge hands its fragment on)
+        if (s.piece != ~0ull) {
+          a.pieces[s.piece].status = 1;
+        } else {
+          unsigned long long at = atomicAdd(a.defer_count, 1ull);
+          if (at < a.defer_cap) a.defer_list[at] = s.frag;
+          else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
+        }
         for (int i = 0; i < kMCap; i++) st.map_key(i) = 0;
+        s.frag = ~0ull;
+      } else if (s.piece != ~0ull && s.scan_done) {
+        finish_piece(s, st, a);
         s.frag = ~0ull;
       } else if (s.quick_stop || s.scan_done) {
         finish_fragment(s, st, a);

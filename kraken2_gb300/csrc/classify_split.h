@@ -1,0 +1,52 @@
+// Long single-end fragments classified as pieces by several lanes, so that
+// no lane walks a whole long read alone (a 50 kb read walked by one lane
+// takes about 30 ms while the rest of the device idles).  A plan kernel
+// cuts each long fragment where the reference's token stream starts afresh
+// (see SplitPiece), the fused kernel classifies the pieces like fragments,
+// and a merge kernel adds up each fragment's pieces and resolves it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "classify_core.cuh"
+
+namespace k2g {
+
+constexpr uint32_t kSplitMinLen = 4096;   // fragments at least this long are cut
+constexpr uint32_t kPieceLen = 2048;      // nominal piece length
+constexpr uint32_t kCutSearch = 256;      // a cut is looked for within this many positions
+
+// The pieces of one split fragment: pieces[first, first + n).
+struct SplitFrag {
+  uint64_t frag;
+  uint64_t first;
+  uint32_t n;             // 0: the fragment was left whole
+};
+
+struct SplitBufs {
+  uint8_t *mark;                // per fragment of the view
+  SplitPiece *pieces;
+  uint64_t pieces_cap;
+  SplitFrag *frags;
+  uint64_t frags_cap;
+  uint32_t *map_key, *map_cnt;  // merge maps, 64 entries per piece slot
+  unsigned long long *ctr;      // [0] piece slots taken, [1] split fragments, [2] work counter
+};
+
+// Slot capacities for a call of total_bases bases.
+inline uint64_t split_pieces_cap(uint64_t total_bases) {
+  return total_bases / kPieceLen + total_bases / kSplitMinLen + 16;
+}
+inline uint64_t split_frags_cap(uint64_t total_bases) { return total_bases / kSplitMinLen + 16; }
+
+// Plans the pieces of the view's long fragments (b.ctr and b.pieces must be
+// zeroed first); marks them in b.mark.
+cudaError_t split_plan(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st);
+// Merges the pieces of every split fragment and writes its outputs; a
+// fragment one of whose pieces overflowed its taxon map goes to the view's
+// slow-path list instead.
+cudaError_t split_merge(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st);
+
+}  // namespace k2g

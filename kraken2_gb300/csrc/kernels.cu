@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "classify_kernels.cuh"
+#include "classify_split.h"
 #include "k2g_internal.h"
 #include "pipeline.cuh"
 
@@ -269,6 +270,16 @@ struct DeviceState {
   uint64_t *defer = nullptr, *defer2 = nullptr;
   uint64_t defer_cap = 0, defer2_cap = 0;
   unsigned long long *counters = nullptr;
+  // persistent mode: long single-end fragments classified as pieces
+  uint8_t *split_mark = nullptr;
+  uint64_t split_mark_cap = 0;
+  SplitPiece *pieces = nullptr;
+  uint64_t pieces_cap = 0;
+  SplitFrag *split_frags = nullptr;
+  uint64_t split_frags_cap = 0;
+  uint32_t *merge_map = nullptr;
+  uint64_t merge_map_cap = 0;
+  unsigned long long *split_ctr = nullptr;
 };
 constexpr int kStatesPerDevice = 8;   // state_for picks among them with the top three hash bits
 struct DeviceStates {
@@ -551,12 +562,41 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     }
     K2G_CUDA_TRY(deferred());
   } else {
+    // Persistent mode cuts long single-end fragments into pieces first, so
+    // no lane walks a long read alone; quick mode stops inside a fragment
+    // and pairs carry a mate border, so those stay whole.
+    const bool split = mode == K2G_MODE_PERSISTENT && !a0.cls.paired && !a0.cls.quick &&
+                       max_len >= kSplitMinLen;
+    SplitBufs spl{};
+    if (split) {
+      const uint64_t pc = split_pieces_cap(total_bases), fc = split_frags_cap(total_bases);
+      K2G_CUDA_TRY(grow(ds.split_mark, ds.split_mark_cap, std::max<uint64_t>(sb, 1)));
+      K2G_CUDA_TRY(grow(ds.pieces, ds.pieces_cap, pc));
+      K2G_CUDA_TRY(grow(ds.split_frags, ds.split_frags_cap, fc));
+      K2G_CUDA_TRY(grow(ds.merge_map, ds.merge_map_cap, 128 * pc));
+      if (!ds.split_ctr) K2G_CUDA_TRY(cudaMalloc(&ds.split_ctr, 3 * sizeof(unsigned long long)));
+      spl = SplitBufs{ds.split_mark, ds.pieces, pc, ds.split_frags, fc,
+                      ds.merge_map, ds.merge_map + 64 * pc, ds.split_ctr};
+    }
     for (uint64_t i = 0; i < S; i++) {
       const ExecCtx &c = ds.ctx[0];
       const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+      ClassifyArgs v = sub_view(a0, f0, n, c, sp);
       K2G_CUDA_TRY(cudaMemsetAsync(c.counters, 0, 2 * sizeof(unsigned long long), st));
-      K2G_CUDA_TRY(dispatch_fast(sub_view(a0, f0, n, c, sp), mode == K2G_MODE_PERSISTENT ? 1 : 0,
-                                 sm_count(dev), st));
+      if (split) {
+        K2G_CUDA_TRY(cudaMemsetAsync(spl.ctr, 0, 3 * sizeof(unsigned long long), st));
+        K2G_CUDA_TRY(cudaMemsetAsync(spl.pieces, 0, spl.pieces_cap * sizeof(SplitPiece), st));
+        K2G_CUDA_TRY(split_plan(v, spl, sm_count(dev), st));
+        ClassifyArgs pv = v;
+        pv.pieces = spl.pieces;
+        pv.n_pieces = spl.ctr;
+        pv.next_frag = spl.ctr + 2;
+        pv.n_frags = spl.pieces_cap;   // bounds the piece indices and sizes the launch
+        K2G_CUDA_TRY(dispatch_fast(pv, 1, sm_count(dev), st));
+        v.split_mark = spl.mark;
+      }
+      K2G_CUDA_TRY(dispatch_fast(v, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), st));
+      if (split) K2G_CUDA_TRY(split_merge(v, spl, sm_count(dev), st));
       K2G_CUDA_TRY(slow(i));
     }
   }

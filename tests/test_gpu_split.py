@@ -1,0 +1,123 @@
+"""Long single-end fragments cut into pieces (persistent mode) must classify
+exactly as when one lane walks each whole fragment (plain mode never cuts)
+and as the oracle does: calls, hit groups, hit-list runs, taxon counts.
+
+The reads are built to stress the cuts: ambiguous runs and low-complexity
+stretches around the nominal cut positions, lower-case bases, reads with no
+usable cut, quality masking, and hit events (-K)."""
+import os
+
+import numpy as np
+import pytest
+
+import kraken2_gb300 as k2g
+import oracle
+from gpu_util import classify_batch
+from kraken_io import GOLDEN, Batch, batch_of, golden_db
+
+pytestmark = pytest.mark.gpu
+
+K = 35
+PIECE = 2048
+
+
+def long_reads(seed: int, n: int = 60, quals: bool = False) -> Batch:
+    rng = np.random.default_rng(seed)
+    src = batch_of("se150")
+    pieces = [src.bases[int(src.seq_off[i]):int(src.seq_off[i + 1])] for i in range(src.n_frags)]
+    reads = []
+    for r in range(n):
+        target = int(rng.integers(4096, 30_000)) if r % 7 else int(rng.integers(150, 4096))
+        buf = bytearray()
+        while len(buf) < target:
+            buf += pieces[int(rng.integers(0, len(pieces)))]
+        buf = buf[:target]
+        kind = r % 5
+        for j in range(1, target // PIECE + 1):
+            c = K - 1 + j * PIECE
+            if c >= target:
+                break
+            at = min(c + int(rng.integers(-60, 300)), target - 2)
+            if kind == 1:      # ambiguous runs across the cut
+                ln = int(rng.integers(1, 80))
+                buf[max(0, at):max(0, at) + ln] = b"N" * len(buf[max(0, at):max(0, at) + ln])
+            elif kind == 2:    # low complexity: one minimizer repeated past the search window
+                ln = int(rng.integers(200, 700))
+                buf[max(0, at - 100):max(0, at - 100) + ln] = b"A" * len(buf[max(0, at - 100):max(0, at - 100) + ln])
+            elif kind == 3:    # lower case and scattered N
+                s0 = max(0, at - 50)
+                buf[s0:s0 + 120] = bytes(buf[s0:s0 + 120]).lower()
+                for _ in range(3):
+                    p = int(rng.integers(max(0, at - 40), min(target, at + 40)))
+                    buf[p] = ord("N")
+        if r % 11 == 4:        # no usable cut at all: N every 30 bases
+            for p in range(0, target, 30):
+                buf[p] = ord("N")
+        reads.append(bytes(buf))
+    bases = b"".join(reads)
+    off = np.concatenate([[0], np.cumsum([len(x) for x in reads])]).astype(np.uint64)
+    q = None
+    if quals:
+        qa = rng.integers(33, 74, len(bases)).astype(np.uint8)
+        q = qa.tobytes()
+    return Batch(bases, q, off, n, False, [f"r{i}" for i in range(n)],
+                 [(len(x),) for x in reads], np.zeros(n, np.uint32))
+
+
+def same(a, b, n):
+    assert a.status == 0 and b.status == 0
+    assert np.array_equal(a.call[:n], b.call[:n])
+    assert np.array_equal(a.hit_groups[:n], b.hit_groups[:n])
+    assert np.array_equal(a.hitlist_len[:n], b.hitlist_len[:n])
+    assert np.array_equal(a.taxon_reads, b.taxon_reads)
+    for i in range(n):
+        assert a.runs_of(i) == b.runs_of(i), i
+
+
+@pytest.mark.parametrize("seed,params", [
+    (1, dict(confidence=0.0, min_hit_groups=0)),
+    (2, dict(confidence=0.3, min_hit_groups=2)),
+    (3, dict(confidence=0.1, min_hit_groups=2, min_quality=15)),
+])
+def test_pieces_equal_whole_fragments_and_oracle(seed, params):
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    b = long_reads(seed, quals="min_quality" in params)
+    split = classify_batch(db, b, params, mode=k2g.MODE_PERSISTENT)
+    whole = classify_batch(db, b, params, mode=k2g.MODE_PLAIN)
+    same(split, whole, b.n_frags)
+    g = golden_db("db_a")
+    o = oracle.Oracle(g.hash.cells, g.hash.capacity, g.hash.key_bits, g.hash.value_bits,
+                      g.taxo.parent, oracle.index_opts(g.opts.k, g.opts.l, g.opts.spaced_seed_mask,
+                                                       g.opts.toggle_mask))
+    calls, hg, nr, runs, base = o.classify(b.bases, b.quals, b.seq_off, b.n_frags, threads=4,
+                                           **params)
+    assert np.array_equal(split.call[:b.n_frags], calls.astype(np.uint32))
+    assert np.array_equal(split.hit_groups[:b.n_frags], hg.astype(np.uint32))
+    for i in range(b.n_frags):
+        want = [(int(r["code"]), int(r["count"])) for r in runs[int(base[i]):int(base[i]) + int(nr[i])]]
+        assert split.runs_of(i) == want, i
+    # the batch did go through the pieces: most reads are long enough
+    assert sum(1 for L in b.lens if L[0] >= 4096) > b.n_frags // 2
+    db.close()
+
+
+def test_long_batch_events_give_the_same_counters():
+    """Persistent mode with add_kmer events: the -K counters built from the
+    pieces' events equal those built from whole fragments."""
+    from test_gpu_counters import classify_with_events
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    b = long_reads(9, n=40)
+    b.blocks = (np.arange(b.n_frags) // 7).astype(np.uint32)
+    params = dict(confidence=0.0, min_hit_groups=0, quick=False, paired=False, min_quality=0)
+    outs = []
+    for mode in (k2g.MODE_PERSISTENT, k2g.MODE_PLAIN):
+        c = k2g.Counters(db)
+        reads, res, tr, keep = classify_with_events(db, b, params, mode)
+        c.add(reads, res)
+        outs.append((tr, c.finish()))
+        c.close()
+        del keep
+    assert np.array_equal(outs[0][0], outs[1][0])
+    for x, y in zip(outs[0][1], outs[1][1]):
+        assert np.array_equal(x, y)
+    db.close()
