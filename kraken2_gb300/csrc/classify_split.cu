@@ -86,14 +86,19 @@ __global__ void split_plan_kernel(ClassifyArgs a, SplitBufs b) {
     if (sid >= b.frags_cap) continue;
     const uint8_t *seq = a.bases + o0;
     const uint8_t *qs = qual ? a.quals + o0 : nullptr;
+    // with hit events a piece's key ordinals are index << 16 | local: keep
+    // the pieces below 2^15 and each below 2^16 bases (so below 2^16 keys)
+    const bool events = a.hit_keys != nullptr;
+    bool whole = events && n_cuts + 1 >= (1u << 15);
     uint32_t lo = k - 1, idx = 0;
     uint64_t lm = 0;
-    for (uint32_t j = 1; j <= n_cuts; j++) {
+    for (uint32_t j = 1; j <= n_cuts && !whole; j++) {
       const uint32_t c = k - 1 + j * kPieceLen;
       const uint32_t end = (uint32_t)min((uint64_t)c + kCutSearch, len);
       uint64_t mp = 0;
       const uint32_t p = find_cut(sc, rc1, seq, qs, thr, qall, c, end, mp);
       if (!p) continue;
+      if (events && p - lo >= kMaxEventPiece) whole = true;
       SplitPiece &pc = b.pieces[base + idx];
       pc.frag = f;
       pc.last_min = lm;
@@ -104,7 +109,12 @@ __global__ void split_plan_kernel(ClassifyArgs a, SplitBufs b) {
       lo = p;
       lm = mp;
     }
+    if (events && len - lo >= kMaxEventPiece) whole = true;
     SplitFrag sf{f, base, 0};
+    if (whole) {   // slots already written are voided
+      for (uint32_t j = 0; j < idx; j++) b.pieces[base + j].hi = 0;
+      idx = 0;
+    }
     if (idx) {
       SplitPiece &pc = b.pieces[base + idx];
       pc.frag = f;
@@ -155,9 +165,13 @@ __global__ void split_merge_kernel(ClassifyArgs a, SplitBufs b) {
       else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
       continue;
     }
-    // at least twice the most distinct taxa the pieces can hold (12 each)
-    int cap = 64;
-    while ((uint64_t)cap * 2 <= 64ull * sf.n) cap *= 2;
+    // at least twice the taxon entries of all pieces (ResolveTree walks the
+    // whole map, so it is no larger than that); at most 32 per piece, which
+    // fits the fragment's 64 entries per piece of the merge buffer
+    uint32_t entries = 0;
+    for (uint32_t j = 0; j < sf.n; j++) entries += b.pieces[sf.first + j].n_map;
+    int cap = 16;
+    while ((uint32_t)cap < 2 * entries) cap *= 2;
     MergeMap st{b.map_key + sf.first * 64, b.map_cnt + sf.first * 64, cap};
     for (int i = 0; i < cap; i++) st.mkey[i] = 0;
     MergeLane s{};
@@ -175,18 +189,28 @@ __global__ void split_merge_kernel(ClassifyArgs a, SplitBufs b) {
       s.hit_groups += pc.hit_groups;
       for (uint32_t e = 0; e < pc.n_map; e++) map_add(st, distinct, pc.map_taxon[e], pc.map_count[e]);
       const uint64_t r0 = s.run_base + (pc.lo - (k - 1));
-      for (uint32_t r = 0; r < pc.n_runs; r++) {
-        if (r0 + r >= a.runs_cap) break;
-        const uint64_t x = a.runs[r0 + r];
-        const uint32_t code = (uint32_t)(x >> 32), cnt = (uint32_t)x;
-        if (have && code == lc) {
-          ln += cnt;
-        } else {
-          if (have && s.run_base + w < a.runs_cap) a.runs[s.run_base + w] = ((uint64_t)lc << 32) | ln;
-          w += have ? 1 : 0;
-          lc = code;
-          ln = cnt;
-          have = true;
+      const uint32_t nr =
+          r0 >= a.runs_cap ? 0u : (uint32_t)min((uint64_t)pc.n_runs, a.runs_cap - r0);
+      // runs are read kBatch at a time before any is written back: the loads
+      // overlap, and the writes land at or before positions already read
+      constexpr uint32_t kBatch = 16;
+      for (uint32_t r = 0; r < nr; r += kBatch) {
+        uint64_t x[kBatch];
+#pragma unroll
+        for (uint32_t i = 0; i < kBatch; i++) x[i] = r + i < nr ? a.runs[r0 + r + i] : 0;
+#pragma unroll
+        for (uint32_t i = 0; i < kBatch; i++) {
+          if (r + i >= nr) break;
+          const uint32_t code = (uint32_t)(x[i] >> 32), cnt = (uint32_t)x[i];
+          if (have && code == lc) {
+            ln += cnt;
+          } else {
+            if (have && s.run_base + w < a.runs_cap) a.runs[s.run_base + w] = ((uint64_t)lc << 32) | ln;
+            w += have ? 1 : 0;
+            lc = code;
+            ln = cnt;
+            have = true;
+          }
         }
       }
     }

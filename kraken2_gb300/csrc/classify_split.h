@@ -14,9 +14,10 @@
 
 namespace k2g {
 
-constexpr uint32_t kSplitMinLen = 4096;   // fragments at least this long are cut
-constexpr uint32_t kPieceLen = 2048;      // nominal piece length
+constexpr uint32_t kSplitMinLen = 2048;   // fragments at least this long are cut
+constexpr uint32_t kPieceLen = 1024;      // nominal piece length
 constexpr uint32_t kCutSearch = 256;      // a cut is looked for within this many positions
+constexpr uint32_t kMaxEventPiece = 60000; // longest piece when hit events are requested
 
 // The pieces of one split fragment: pieces[first, first + n).
 struct SplitFrag {

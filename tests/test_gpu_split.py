@@ -18,7 +18,7 @@ from kraken_io import GOLDEN, Batch, batch_of, golden_db
 pytestmark = pytest.mark.gpu
 
 K = 35
-PIECE = 2048
+PIECE = 1024
 
 
 def long_reads(seed: int, n: int = 60, quals: bool = False) -> Batch:
@@ -97,7 +97,7 @@ def test_pieces_equal_whole_fragments_and_oracle(seed, params):
         want = [(int(r["code"]), int(r["count"])) for r in runs[int(base[i]):int(base[i]) + int(nr[i])]]
         assert split.runs_of(i) == want, i
     # the batch did go through the pieces: most reads are long enough
-    assert sum(1 for L in b.lens if L[0] >= 4096) > b.n_frags // 2
+    assert sum(1 for L in b.lens if L[0] >= 2048) > b.n_frags // 2
     db.close()
 
 
