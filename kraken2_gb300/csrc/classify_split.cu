@@ -61,71 +61,88 @@ __device__ uint32_t find_cut(const ScanConst &sc, bool rc1, const uint8_t *seq,
   return 0;
 }
 
-// One thread per fragment: a long single-end fragment gets a contiguous
-// range of piece slots (one per nominal cut, plus one) and is cut near
-// every kPieceLen positions.  A fragment without room, or without a single
-// usable cut, is left whole.
-__global__ void split_plan_kernel(ClassifyArgs a, SplitBufs b) {
-  const ScanConst sc = scan_const(a);
+// A long single-end fragment gets a contiguous range of piece slots (one
+// per nominal cut, plus one) and is cut near every kPieceLen positions.  A
+// fragment without room, or without a single usable cut, is left whole.
+__device__ void plan_fragment(const ClassifyArgs &a, const SplitBufs &b, const ScanConst &sc,
+                              uint64_t f) {
   const bool rc1 = a.scan.revcom_version != 0;
   const bool qual = a.quals != nullptr && a.cls.min_quality > 0;
   const int thr = 33 + a.cls.min_quality;
   const bool qall = thr > 127;
   const uint32_t k = (uint32_t)sc.k;
+  const uint64_t o0 = a.seq_off[f], len = a.seq_off[f + 1] - o0;
+  if (len < kSplitMinLen) return;
+  // nominal cuts at k - 1 + j * kPieceLen, the last piece keeping half that
+  const uint32_t n_cuts = (uint32_t)((len - (k - 1) - kPieceLen / 2) / kPieceLen);
+  if (!n_cuts) return;
+  const unsigned long long base = atomicAdd(b.ctr, (unsigned long long)n_cuts + 1);
+  if (base + n_cuts + 1 > b.pieces_cap) return;
+  const unsigned long long sid = atomicAdd(b.ctr + 1, 1ull);
+  if (sid >= b.frags_cap) return;
+  const uint8_t *seq = a.bases + o0;
+  const uint8_t *qs = qual ? a.quals + o0 : nullptr;
+  // with hit events a piece's key ordinals are index << 16 | local: keep
+  // the pieces below 2^15 and each below 2^16 bases (so below 2^16 keys)
+  const bool events = a.hit_keys != nullptr;
+  bool whole = events && n_cuts + 1 >= (1u << 15);
+  uint32_t lo = k - 1, idx = 0;
+  uint64_t lm = 0;
+  for (uint32_t j = 1; j <= n_cuts && !whole; j++) {
+    const uint32_t c = k - 1 + j * kPieceLen;
+    const uint32_t end = (uint32_t)min((uint64_t)c + kCutSearch, len);
+    uint64_t mp = 0;
+    const uint32_t p = find_cut(sc, rc1, seq, qs, thr, qall, c, end, mp);
+    if (!p) continue;
+    if (events && p - lo >= kMaxEventPiece) whole = true;
+    SplitPiece &pc = b.pieces[base + idx];
+    pc.frag = f;
+    pc.last_min = lm;
+    pc.lo = lo;
+    pc.hi = p;
+    pc.index = idx;
+    idx++;
+    lo = p;
+    lm = mp;
+  }
+  if (events && len - lo >= kMaxEventPiece) whole = true;
+  SplitFrag sf{f, base, 0};
+  if (whole) {   // slots already written are voided
+    for (uint32_t j = 0; j < idx; j++) b.pieces[base + j].hi = 0;
+    idx = 0;
+  }
+  if (idx) {
+    SplitPiece &pc = b.pieces[base + idx];
+    pc.frag = f;
+    pc.last_min = lm;
+    pc.lo = lo;
+    pc.hi = (uint32_t)len;
+    pc.index = idx;
+    sf.n = idx + 1;
+    b.mark[f] = 1;
+  }
+  b.frags[sid] = sf;
+}
+
+// One thread per fragment of the view (marks are cleared here).
+__global__ void split_plan_kernel(ClassifyArgs a, SplitBufs b) {
+  const ScanConst sc = scan_const(a);
   for (uint64_t f = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; f < a.n_frags;
        f += (uint64_t)gridDim.x * blockDim.x) {
     b.mark[f] = 0;
-    const uint64_t o0 = a.seq_off[f], len = a.seq_off[f + 1] - o0;
-    if (len < kSplitMinLen) continue;
-    // nominal cuts at k - 1 + j * kPieceLen, the last piece keeping half that
-    const uint32_t n_cuts = (uint32_t)((len - (k - 1) - kPieceLen / 2) / kPieceLen);
-    if (!n_cuts) continue;
-    const unsigned long long base = atomicAdd(b.ctr, (unsigned long long)n_cuts + 1);
-    if (base + n_cuts + 1 > b.pieces_cap) continue;
-    const unsigned long long sid = atomicAdd(b.ctr + 1, 1ull);
-    if (sid >= b.frags_cap) continue;
-    const uint8_t *seq = a.bases + o0;
-    const uint8_t *qs = qual ? a.quals + o0 : nullptr;
-    // with hit events a piece's key ordinals are index << 16 | local: keep
-    // the pieces below 2^15 and each below 2^16 bases (so below 2^16 keys)
-    const bool events = a.hit_keys != nullptr;
-    bool whole = events && n_cuts + 1 >= (1u << 15);
-    uint32_t lo = k - 1, idx = 0;
-    uint64_t lm = 0;
-    for (uint32_t j = 1; j <= n_cuts && !whole; j++) {
-      const uint32_t c = k - 1 + j * kPieceLen;
-      const uint32_t end = (uint32_t)min((uint64_t)c + kCutSearch, len);
-      uint64_t mp = 0;
-      const uint32_t p = find_cut(sc, rc1, seq, qs, thr, qall, c, end, mp);
-      if (!p) continue;
-      if (events && p - lo >= kMaxEventPiece) whole = true;
-      SplitPiece &pc = b.pieces[base + idx];
-      pc.frag = f;
-      pc.last_min = lm;
-      pc.lo = lo;
-      pc.hi = p;
-      pc.index = idx;
-      idx++;
-      lo = p;
-      lm = mp;
-    }
-    if (events && len - lo >= kMaxEventPiece) whole = true;
-    SplitFrag sf{f, base, 0};
-    if (whole) {   // slots already written are voided
-      for (uint32_t j = 0; j < idx; j++) b.pieces[base + j].hi = 0;
-      idx = 0;
-    }
-    if (idx) {
-      SplitPiece &pc = b.pieces[base + idx];
-      pc.frag = f;
-      pc.last_min = lm;
-      pc.lo = lo;
-      pc.hi = (uint32_t)len;
-      pc.index = idx;
-      sf.n = idx + 1;
-      b.mark[f] = 1;
-    }
-    b.frags[sid] = sf;
+    plan_fragment(a, b, sc, f);
+  }
+}
+
+// One thread per entry of the view's in_list (the fragments the pipeline
+// deferred); marks must be cleared before.
+__global__ void split_plan_list_kernel(ClassifyArgs a, SplitBufs b) {
+  const ScanConst sc = scan_const(a);
+  const uint64_t n = min((uint64_t)*a.in_count, a.in_cap);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t f = a.in_list[i];
+    if (f < a.n_frags) plan_fragment(a, b, sc, f);
   }
 }
 
@@ -233,6 +250,13 @@ unsigned grid_of(uint64_t n, int sms) {
 
 cudaError_t split_plan(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st) {
   split_plan_kernel<<<grid_of(v.n_frags, sms), 128, 0, st>>>(v, b);
+  note_launches();
+  return cudaGetLastError();
+}
+
+cudaError_t split_plan_list(const ClassifyArgs &v, const SplitBufs &b, uint64_t list_cap, int sms,
+                           cudaStream_t st) {
+  split_plan_list_kernel<<<grid_of(list_cap, sms), 128, 0, st>>>(v, b);
   note_launches();
   return cudaGetLastError();
 }

@@ -45,6 +45,9 @@ inline uint64_t split_frags_cap(uint64_t total_bases) { return total_bases / kSp
 // Plans the pieces of the view's long fragments (b.ctr and b.pieces must be
 // zeroed first); marks them in b.mark.
 cudaError_t split_plan(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st);
+// The same for the fragments of the view's in_list (b.mark must be zeroed).
+cudaError_t split_plan_list(const ClassifyArgs &v, const SplitBufs &b, uint64_t list_cap, int sms,
+                           cudaStream_t st);
 // Merges the pieces of every split fragment and writes its outputs; a
 // fragment one of whose pieces overflowed its taxon map goes to the view's
 // slow-path list instead.

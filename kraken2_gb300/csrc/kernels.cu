@@ -514,6 +514,21 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
   // one list after the last beat, so its work stealing spreads the long
   // ones over the whole device; what that kernel defers goes to the slow
   // kernel.
+  // Long single-end fragments of that list are cut into pieces first (see
+  // classify_split.h); the fused kernel then skips them, and the merge hands
+  // a fragment whose piece overflowed its taxon map to the slow kernel.
+  const bool split_deferred = pipeline && !a0.cls.paired && !a0.cls.quick && max_len >= kSplitMinLen;
+  SplitBufs dspl{};
+  if (split_deferred) {
+    const uint64_t pc = split_pieces_cap(total_bases), fc = split_frags_cap(total_bases);
+    K2G_CUDA_TRY(grow(ds.split_mark, ds.split_mark_cap, std::max<uint64_t>(a0.n_frags, 1)));
+    K2G_CUDA_TRY(grow(ds.pieces, ds.pieces_cap, pc));
+    K2G_CUDA_TRY(grow(ds.split_frags, ds.split_frags_cap, fc));
+    K2G_CUDA_TRY(grow(ds.merge_map, ds.merge_map_cap, 128 * pc));
+    if (!ds.split_ctr) K2G_CUDA_TRY(cudaMalloc(&ds.split_ctr, 3 * sizeof(unsigned long long)));
+    dspl = SplitBufs{ds.split_mark, ds.pieces, pc, ds.split_frags, fc,
+                     ds.merge_map, ds.merge_map + 64 * pc, ds.split_ctr};
+  }
   auto deferred = [&]() -> cudaError_t {
     ClassifyArgs a = a0;
     a.in_list = ds.defer;
@@ -526,9 +541,26 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     a.frag_list = ds.defer2;
     a.scratch = ds.ctx[0].slow;
     a.scratch_stride = sp.stride;
-    cudaError_t e = dispatch_fast(a, 1, sm_count(dev), st);
-    if (e != cudaSuccess) return e;
+    cudaError_t e;
+    if (split_deferred) {
+      if ((e = cudaMemsetAsync(dspl.mark, 0, a0.n_frags, st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(dspl.ctr, 0, 3 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(dspl.pieces, 0, dspl.pieces_cap * sizeof(SplitPiece), st)) != cudaSuccess)
+        return e;
+      if ((e = split_plan_list(a, dspl, ds.defer_cap, sm_count(dev), st)) != cudaSuccess) return e;
+      ClassifyArgs pv = a;
+      pv.in_list = nullptr;
+      pv.pieces = dspl.pieces;
+      pv.n_pieces = dspl.ctr;
+      pv.next_frag = dspl.ctr + 2;
+      pv.n_frags = dspl.pieces_cap;   // bounds the piece indices and sizes the launch
+      if ((e = dispatch_fast(pv, 1, sm_count(dev), st)) != cudaSuccess) return e;
+      a.split_mark = dspl.mark;
+    }
+    if ((e = dispatch_fast(a, 1, sm_count(dev), st)) != cudaSuccess) return e;
+    if (split_deferred && (e = split_merge(a, dspl, sm_count(dev), st)) != cudaSuccess) return e;
     a.in_list = nullptr;
+    a.split_mark = nullptr;
     return dispatch_slow(a, sp.mcap, (unsigned)(sp.threads / 128), 128, st);
   };
 

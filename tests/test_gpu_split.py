@@ -121,3 +121,38 @@ def test_long_batch_events_give_the_same_counters():
     for x, y in zip(outs[0][1], outs[1][1]):
         assert np.array_equal(x, y)
     db.close()
+
+
+@pytest.mark.parametrize("seed,minq", [(4, 0), (5, 15)])
+def test_long_reads_deferred_from_a_short_batch(seed, minq):
+    """A batch of mostly short reads stays in the pipeline; its long reads
+    are deferred there and cut into pieces before the fused kernel runs."""
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    long_b = long_reads(seed, n=15, quals=minq > 0)
+    short = batch_of("se150")
+    rng = np.random.default_rng(seed)
+    n_short = 900
+    pick = rng.integers(0, short.n_frags, n_short)
+    reads = [short.bases[int(short.seq_off[i]):int(short.seq_off[i + 1])] for i in pick]
+    longs = [long_b.bases[int(long_b.seq_off[i]):int(long_b.seq_off[i + 1])] for i in range(long_b.n_frags)]
+    order = list(range(n_short + len(longs)))
+    rng.shuffle(order)
+    seqs = [(reads + longs)[i] for i in order]
+    bases = b"".join(seqs)
+    off = np.concatenate([[0], np.cumsum([len(x) for x in seqs])]).astype(np.uint64)
+    quals = rng.integers(33, 74, len(bases)).astype(np.uint8).tobytes() if minq else None
+    b = Batch(bases, quals, off, len(seqs), False, [f"m{i}" for i in range(len(seqs))],
+              [(len(x),) for x in seqs], np.zeros(len(seqs), np.uint32))
+    assert len(bases) / len(seqs) < 512            # stays a pipelined batch
+    params = dict(confidence=0.2, min_hit_groups=2, min_quality=minq)
+    piped = classify_batch(db, b, params, mode=k2g.MODE_PIPELINED)
+    whole = classify_batch(db, b, params, mode=k2g.MODE_PLAIN)
+    same(piped, whole, b.n_frags)
+    g = golden_db("db_a")
+    o = oracle.Oracle(g.hash.cells, g.hash.capacity, g.hash.key_bits, g.hash.value_bits,
+                      g.taxo.parent, oracle.index_opts(g.opts.k, g.opts.l, g.opts.spaced_seed_mask,
+                                                       g.opts.toggle_mask))
+    calls, hg, nr, runs, base = o.classify(b.bases, b.quals, b.seq_off, b.n_frags, threads=4,
+                                           **params)
+    assert np.array_equal(piped.call[:b.n_frags], calls.astype(np.uint32))
+    db.close()
