@@ -1,6 +1,8 @@
 #include "seq_reader.h"
 
 #include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
 #include <unistd.h>
 
 #include <cstdio>
@@ -56,9 +58,32 @@ void RecordSet::mask_low_quality(size_t first, int min_quality) {
   }
 }
 
-SeqReader::SeqReader(int fd) : fd_(fd), own_fd_(fd > 2), buf_(kBufSize) {}
+SeqReader::SeqReader(int fd) : fd_(fd), own_fd_(fd > 2) {
+  // a regular file is parsed in place from where its offset stands (an
+  // inherited standard input may have been read from already)
+  struct stat st;
+  const off_t at = fd >= 0 ? lseek(fd, 0, SEEK_CUR) : (off_t)-1;
+  if (at >= 0 && fstat(fd, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > at) {
+    const off_t page = (off_t)sysconf(_SC_PAGESIZE);
+    const off_t base = at / page * page;
+    const size_t len = (size_t)(st.st_size - base);
+    void *p = mmap(nullptr, len, PROT_READ, MAP_PRIVATE, fd, base);
+    if (p != MAP_FAILED) {
+      madvise(p, len, MADV_SEQUENTIAL);
+      map_ = p;
+      map_len_ = len;
+      data_ = static_cast<const char *>(p);
+      begin_ = (size_t)(at - base);
+      end_ = len;   // the rest of the file is one buffer; refill() then ends it
+      return;
+    }
+  }
+  buf_.resize(kBufSize);
+  data_ = buf_.data();
+}
 
 SeqReader::~SeqReader() {
+  if (map_) munmap(map_, map_len_);
   if (own_fd_) close(fd_);
 }
 
@@ -68,6 +93,10 @@ bool SeqReader::refill() {
   if (eof_ || err_) return false;
   begin_ = 0;
   end_ = 0;
+  if (map_) {   // the mapped file has been read to its end
+    eof_ = true;
+    return false;
+  }
   const ssize_t got = fd_ >= 0 ? ::read(fd_, buf_.data(), buf_.size()) : -1;
   if (got <= 0) {
     eof_ = true;
@@ -81,7 +110,7 @@ bool SeqReader::refill() {
 // Next byte; -1 at the end of input, -3 after a read error.
 inline int SeqReader::getc() {
   if (begin_ >= end_ && !refill()) return err_ ? -3 : -1;
-  return (unsigned char)buf_[begin_++];
+  return (unsigned char)data_[begin_++];
 }
 
 // Appends the bytes up to the delimiter to dst and consumes the delimiter:
@@ -98,7 +127,7 @@ int SeqReader::read_until(bool line, std::vector<char> &dst, size_t field, int *
       if (err_) return -3;
       break;
     }
-    const char *b = buf_.data() + begin_, *e = buf_.data() + end_;
+    const char *b = data_ + begin_, *e = data_ + end_;
     const char *p;
     if (line) {
       p = static_cast<const char *>(memchr(b, '\n', e - b));
@@ -109,7 +138,7 @@ int SeqReader::read_until(bool line, std::vector<char> &dst, size_t field, int *
     }
     got = true;
     dst.insert(dst.end(), b, p);
-    begin_ = (size_t)(p - buf_.data()) + 1;
+    begin_ = (size_t)(p - data_) + 1;
     if (p < e) {
       if (delim) *delim = (unsigned char)*p;
       break;

@@ -17,8 +17,9 @@
 // Records are appended to a RecordSet: every field of every record goes into
 // two shared arenas (sequences back to back, ready to be handed to the GPU
 // call as one array; names, comments and qualities in the other), so reading
-// allocates nothing per record.  Lines are found with memchr over a 4 MiB
-// input buffer.
+// allocates nothing per record.  Lines are found with memchr over the input:
+// a regular file is mapped into memory and parsed in place; other inputs
+// (pipes, standard input) are read into a 4 MiB buffer.
 #pragma once
 
 #include <cstdint>
@@ -84,6 +85,9 @@ class SeqReader {
   int fd_;
   bool own_fd_;
   std::vector<char> buf_;
+  const char *data_ = nullptr;    // buf_, or the mapped file
+  void *map_ = nullptr;
+  size_t map_len_ = 0;
   size_t begin_ = 0, end_ = 0;
   bool eof_ = false, err_ = false;
   int last_char_ = 0;

@@ -3,6 +3,7 @@
 //
 //   seq_dump <file> block <bytes> [min_quality]
 //   seq_dump <file> batch <count> [min_quality]
+// (<file> "-": standard input)
 //
 // Output, per block: "B <records>\n", then per record
 // "<fastq> <name len> <comment len> <seq len>\n" followed by the name,
@@ -19,7 +20,7 @@ int main(int argc, char **argv) {
   const bool by_bytes = strcmp(argv[2], "block") == 0;
   const size_t arg = strtoull(argv[3], nullptr, 10);
   const int minq = argc > 4 ? atoi(argv[4]) : 0;
-  k2host::SeqReader reader(k2host::open_input(argv[1]));
+  k2host::SeqReader reader(k2host::open_input(strcmp(argv[1], "-") ? argv[1] : nullptr));
   k2host::RecordSet set;
   for (;;) {
     // append after what earlier blocks left, as the drop-in's batches do

@@ -60,11 +60,17 @@ def expected(data: bytes, mode: str, arg: int, minq: int):
     return [[(r.name, r.comment, ks.mask_low_quality(r, minq), r.qual) for r in b] for b in blks]
 
 
-def check(dumper, tmp_path, data: bytes, mode="block", arg=1 << 20, minq=0):
-    path = tmp_path / "in.txt"
-    path.write_bytes(data)
-    r = subprocess.run([dumper, str(path), mode, str(arg), str(minq)], capture_output=True,
-                       check=True)
+def check(dumper, tmp_path, data: bytes, mode="block", arg=1 << 20, minq=0, pipe=False):
+    """A regular file is parsed in place (mapped); pipe=True feeds the same
+    bytes through standard input, read in buffer-sized pieces."""
+    if pipe:
+        r = subprocess.run([dumper, "-", mode, str(arg), str(minq)], input=data,
+                           capture_output=True, check=True)
+    else:
+        path = tmp_path / "in.txt"
+        path.write_bytes(data)
+        r = subprocess.run([dumper, str(path), mode, str(arg), str(minq)], capture_output=True,
+                           check=True)
     got = parse_dump(r.stdout)
     want = expected(data, mode, arg, minq)
     assert got == want, (data[:200], got[:2], want[:2])
@@ -99,6 +105,7 @@ CASES = [
 def test_edge_cases(dumper, tmp_path, data, mode, arg):
     check(dumper, tmp_path, data, mode, arg)
     check(dumper, tmp_path, data, mode, arg, minq=20)
+    check(dumper, tmp_path, data, mode, arg, pipe=True)
 
 
 def _fuzz_input(rng) -> bytes:
@@ -133,7 +140,7 @@ def test_fuzz_against_restatement(dumper, tmp_path, seed):
     data = _fuzz_input(rng)
     mode, arg = [("block", 1 << 20), ("block", int(rng.integers(1, 30))),
                  ("batch", int(rng.integers(1, 5)))][seed % 3]
-    check(dumper, tmp_path, data, mode, arg, minq=int(rng.integers(0, 2)) * 15)
+    check(dumper, tmp_path, data, mode, arg, minq=int(rng.integers(0, 2)) * 15, pipe=seed % 2 == 1)
 
 
 def test_records_spanning_input_buffers(dumper, tmp_path):
@@ -144,3 +151,4 @@ def test_records_spanning_input_buffers(dumper, tmp_path):
     data = b"@big x\n" + big[:3_000_000] + b"\n" + big[3_000_000:] + b"\n+\n" + b"I" * 5_000_000
     data += b"\n" + b"".join(b">s%d\n%s\n" % (i, big[i:i + 97]) for i in range(60_000))
     check(dumper, tmp_path, data, "block", 3 << 20)
+    check(dumper, tmp_path, data, "block", 3 << 20, pipe=True)
