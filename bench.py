@@ -952,6 +952,17 @@ def run_ours(args, log):
     if args.long_reads:
         # the long-read mix alone (for ncu captures of the persistent kernel)
         return {"metric": "long_reads", **long_reads_run(wl, log)}
+    if args.kmer_only:
+        # the -K pass alone, once warm and once timed (for ncu captures)
+        kr = KmerRunner(wl, wl.k2g.MODE_PIPELINED)
+        kr.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kr.run()
+        torch.cuda.synchronize()
+        kdt = time.perf_counter() - t0
+        return {"metric": "minimizer_data", "reads": cfg.n_reads, "s_per_pass": round(kdt, 3),
+                "mreads_min": round(cfg.n_reads / kdt * 60 / 1e6, 1)}
     mode = {"plain": wl.k2g.MODE_PLAIN, "persistent": wl.k2g.MODE_PERSISTENT,
             "pipelined": wl.k2g.MODE_PIPELINED}[args.mode]
     runner = DeviceRunner(wl, mode)
@@ -1188,6 +1199,8 @@ def main():
                     help="setup plus two classification steps only (for ncu captures)")
     ap.add_argument("--long-reads", action="store_true",
                     help="setup plus the long-read mix in HBM only (for ncu captures)")
+    ap.add_argument("--kmer-only", action="store_true",
+                    help="setup plus two -K passes only (for ncu captures)")
     args = ap.parse_args()
     log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
     out = run_reference(args, log) if args.impl == "reference" else run_ours(args, log)
