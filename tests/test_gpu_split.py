@@ -156,3 +156,70 @@ def test_long_reads_deferred_from_a_short_batch(seed, minq):
                                            **params)
     assert np.array_equal(piped.call[:b.n_frags], calls.astype(np.uint32))
     db.close()
+
+
+SEED_MASK = 0x3FFFFFFFF3333333
+
+
+@pytest.mark.parametrize("k,l,mask,revcom,min_hash", [
+    (35, 31, SEED_MASK, 0, 0),                     # legacy reverse complement, spaced seed
+    (25, 19, 0, 1, 7378697629483821056),           # w = 7, min-hash subsampling (SKIP tokens)
+    (31, 31, 0, 0, 0),                             # k == l, legacy reverse complement
+])
+def test_pieces_under_other_scanner_options(k, l, mask, revcom, min_hash):
+    """Cuts found with the scanner options of the database: a table built on
+    the GPU from random genomes, long reads from them, pieces against whole
+    fragments and the oracle."""
+    from gpu_util import to_dev, torch
+    t = torch()
+    rng = np.random.default_rng(k * 7 + revcom)
+    toggle = 0xE37E28C4271B5A2D & ((1 << (2 * l)) - 1) if l < 32 else 0xE37E28C4271B5A2D
+    node_count = 400
+    parent = np.zeros(node_count, np.uint64)
+    for i in range(2, node_count):
+        parent[i] = rng.integers(1, i)
+    opts = k2g.IndexOptions(k, l, mask, toggle, 1, revcom, min_hash)
+    db = k2g.Database.create(opts, 3_000_017, 20, 12, parent)
+    oopts = oracle.index_opts(k, l, mask, toggle, revcom=revcom, min_hash=min_hash)
+    sources = [rng.choice(np.frombuffer(b"ACGT", np.uint8), 20_000).tobytes() for _ in range(30)]
+    keys, taxa = [], []
+    for s in sources:
+        m, amb = oracle.scan(oopts, s)
+        m = m[amb == 0]
+        keys.append(m)
+        taxa.append(np.full(len(m), rng.integers(node_count // 2, node_count), np.uint32))
+    keys, taxa = np.concatenate(keys), np.concatenate(taxa)
+    dk, dt = to_dev(keys), to_dev(taxa)
+    db.build_insert(dk.data_ptr(), dt.data_ptr(), len(keys), False, t.cuda.current_stream().cuda_stream)
+    t.cuda.synchronize()
+    reads = []
+    for r in range(24):
+        s = sources[int(rng.integers(0, len(sources)))]
+        ln = int(rng.integers(2500, 15_000))
+        a = int(rng.integers(0, len(s) - ln))
+        buf = bytearray(s[a:a + ln])
+        for p in rng.integers(0, ln, ln // 50):          # substitutions
+            buf[p] = b"ACGT"[int(rng.integers(0, 4))]
+        if r % 3 == 1:
+            for c in range(PIECE, ln - 100, PIECE):       # ambiguity near the nominal cuts
+                at = c + int(rng.integers(-30, 200))
+                buf[at:at + 20] = b"N" * len(buf[at:at + 20])
+        reads.append(bytes(buf))
+    bases = b"".join(reads)
+    off = np.concatenate([[0], np.cumsum([len(x) for x in reads])]).astype(np.uint64)
+    b = Batch(bases, None, off, len(reads), False, [f"q{i}" for i in range(len(reads))],
+              [(len(x),) for x in reads], np.zeros(len(reads), np.uint32))
+    params = dict(confidence=0.0, min_hit_groups=0)
+    split = classify_batch(db, b, params, mode=k2g.MODE_PERSISTENT)
+    whole = classify_batch(db, b, params, mode=k2g.MODE_PLAIN)
+    same(split, whole, b.n_frags)
+    cells, _ = db.download()
+    info = db.info()
+    o = oracle.Oracle(cells, info.capacity, info.key_bits, info.value_bits, parent, oopts)
+    calls, hg, nr, runs, base = o.classify(b.bases, None, b.seq_off, b.n_frags, threads=4, **params)
+    assert np.array_equal(split.call[:b.n_frags], calls.astype(np.uint32))
+    for i in range(b.n_frags):
+        want = [(int(x["code"]), int(x["count"])) for x in runs[int(base[i]):int(base[i]) + int(nr[i])]]
+        assert split.runs_of(i) == want, i
+    assert (calls > 0).mean() > 0.5
+    db.close()

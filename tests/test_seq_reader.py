@@ -112,13 +112,13 @@ def _fuzz_input(rng) -> bytes:
     pieces = []
     for _ in range(int(rng.integers(1, 40))):
         kind = rng.integers(0, 10)
-        name = bytes(rng.choice(list(b"ab1/ \t\r:"), int(rng.integers(0, 8))))
+        name = rng.choice(np.frombuffer(b"ab1/ \t\r:", np.uint8), int(rng.integers(0, 8))).tobytes()
         seq_len = int(rng.integers(0, 12))
-        seq = bytes(rng.choice(list(b"ACGTN"), seq_len))
+        seq = rng.choice(np.frombuffer(b"ACGTN", np.uint8), seq_len).tobytes()
         nl = b"\r\n" if rng.random() < 0.2 else b"\n"
         if kind < 5:                                    # FASTQ, sometimes broken
             q_len = seq_len if rng.random() < 0.8 else int(rng.integers(0, 14))
-            qual = bytes(rng.choice(list(b"!#5I@+>\x90"), q_len))
+            qual = rng.choice(np.frombuffer(b"!#5I@+>\x90", np.uint8), q_len).tobytes()
             split = int(rng.integers(0, q_len + 1))
             qlines = qual[:split] + nl + qual[split:] if rng.random() < 0.3 else qual
             pieces.append(b"@" + name + nl + seq + nl + b"+" + name[:2] + nl + qlines + nl)
@@ -127,7 +127,7 @@ def _fuzz_input(rng) -> bytes:
             extra = nl if rng.random() < 0.3 else b""
             pieces.append(b">" + name + nl + seq[:cut] + nl + extra + seq[cut:] + nl)
         else:                                           # stray bytes
-            pieces.append(bytes(rng.choice(list(b"@>+\n\r A"), int(rng.integers(1, 6)))))
+            pieces.append(rng.choice(np.frombuffer(b"@>+\n\r A", np.uint8), int(rng.integers(1, 6))).tobytes())
     data = b"".join(pieces)
     if rng.random() < 0.3:
         data = data[:int(rng.integers(0, len(data) + 1))]
@@ -147,7 +147,7 @@ def test_records_spanning_input_buffers(dumper, tmp_path):
     """Records longer than the reader's 4 MiB buffer, and many short ones
     straddling buffer boundaries."""
     rng = np.random.default_rng(7)
-    big = bytes(rng.choice(list(b"ACGT"), 5_000_000))
+    big = rng.choice(np.frombuffer(b"ACGT", np.uint8), 5_000_000).tobytes()
     data = b"@big x\n" + big[:3_000_000] + b"\n" + big[3_000_000:] + b"\n+\n" + b"I" * 5_000_000
     data += b"\n" + b"".join(b">s%d\n%s\n" % (i, big[i:i + 97]) for i in range(60_000))
     check(dumper, tmp_path, data, "block", 3 << 20)
