@@ -2,9 +2,8 @@
 // counters to group hit events.  Each pass: a per-tile digit histogram, an
 // exclusive scan of the (digit, tile) counts in digit-major order, and a
 // stable scatter that ranks each tile's keys in shared memory (warp match
-// and warp-private counters over each warp's contiguous sub-tile, then one
-// prefix over the warps) and writes them out digit run by digit run, so
-// global writes are contiguous.
+// for ranks within a warp, per-warp counts for ranks across warps) and then
+// writes them out digit run by digit run, so global writes are contiguous.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -94,70 +93,68 @@ __global__ void scan_add_kernel(uint32_t *v, uint64_t n, const uint32_t *sums) {
     if (base + i < n) v[base + i] += add;
 }
 
-// Each warp ranks its own contiguous sub-tile of kTile / kWarps keys, 32 at a
-// time, with warp-private digit counters (no block barrier per round); one
-// prefix over the warps per digit then places every key, keeping the input
-// order among equal digits (the sort is stable).
 __global__ void scatter_kernel(const uint64_t *in, uint64_t *out, uint64_t n, int shift,
                                const uint32_t *offs, uint32_t ntiles) {
-  constexpr int kPerWarp = kTile / kWarps;      // 512 keys, kPerThread per lane
   __shared__ uint64_t s_keys[kTile];
   __shared__ uint32_t s_warp[kWarps][kRadix];   // per-warp counts, then exclusive offsets
-  __shared__ uint32_t s_tot[kRadix];            // keys of each digit in the tile
+  __shared__ uint32_t s_run[kRadix];            // keys of each digit ranked so far
   __shared__ uint32_t s_start[kRadix];          // first local position of each digit
   __shared__ uint32_t s_glob[kRadix];           // global position of each digit's run
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t t0 = (uint64_t)blockIdx.x * kTile;
   const uint32_t cnt = (uint32_t)(n > t0 ? (n - t0 < kTile ? n - t0 : kTile) : 0);
-  for (int d = lane; d < kRadix; d += 32) s_warp[warp][d] = 0;
-  __syncwarp();
+  s_run[threadIdx.x] = 0;
   uint64_t key[kPerThread];
   uint32_t rank[kPerThread];
-  const unsigned below_mask = (1u << lane) - 1;
-#pragma unroll
   for (int r = 0; r < kPerThread; r++) {
-    const uint32_t li = (uint32_t)(warp * kPerWarp + r * 32 + lane);
-    const bool valid = li < cnt;
-    key[r] = valid ? in[t0 + li] : ~0ull;
-    const uint32_t dig = valid ? (uint32_t)((key[r] >> shift) & 0xFF) : (uint32_t)kRadix;
-    const unsigned peers = __match_any_sync(0xffffffffu, dig);
-    const uint32_t below = __popc(peers & below_mask);
-    const uint32_t seen = valid ? s_warp[warp][dig] : 0;
-    __syncwarp();
-    if (valid && below == 0) s_warp[warp][dig] = seen + __popc(peers);
-    __syncwarp();
-    rank[r] = seen + below;
+    const uint32_t li = (uint32_t)r * kThreads + threadIdx.x;
+    key[r] = li < cnt ? in[t0 + li] : ~0ull;
   }
-  __syncthreads();
+  // Local ranks, round by round (round r holds keys r*256 .. r*256+255 in
+  // thread order, which is their order in the input).
+  for (int r = 0; r < kPerThread; r++) {
+    for (int d = lane; d < kRadix; d += 32) s_warp[warp][d] = 0;
+    __syncthreads();
+    const uint32_t li = (uint32_t)r * kThreads + threadIdx.x;
+    const bool valid = li < cnt;
+    const uint32_t dig = valid ? (uint32_t)((key[r] >> shift) & 0xFF) : 0;
+    const unsigned peers = __match_any_sync(0xffffffffu, valid ? dig : 0x100u);
+    const uint32_t below = __popc(peers & ((1u << lane) - 1));
+    if (valid && below == 0) s_warp[warp][dig] = __popc(peers);
+    __syncthreads();
+    // exclusive prefix over warps per digit, plus the digit's running count
+    {
+      const int d = threadIdx.x;
+      uint32_t acc = s_run[d];
+      for (int w = 0; w < kWarps; w++) {
+        const uint32_t c = s_warp[w][d];
+        s_warp[w][d] = acc;
+        acc += c;
+      }
+      s_run[d] = acc;
+    }
+    __syncthreads();
+    rank[r] = valid ? s_warp[warp][dig] + below : 0;
+    __syncthreads();
+  }
+  // digit starts within the tile (exclusive scan of s_run), global offsets
   {
     const int d = threadIdx.x;
-    uint32_t acc = 0;
-#pragma unroll
-    for (int w = 0; w < kWarps; w++) {
-      const uint32_t c = s_warp[w][d];
-      s_warp[w][d] = acc;
-      acc += c;
+    s_start[d] = s_run[d];
+    __syncthreads();
+    for (int o = 1; o < kRadix; o <<= 1) {
+      uint32_t add = d >= o ? s_start[d - o] : 0;
+      __syncthreads();
+      s_start[d] += add;
+      __syncthreads();
     }
-    s_tot[d] = acc;
-    s_start[d] = acc;
+    s_start[d] -= s_run[d];
     s_glob[d] = offs[(uint64_t)d * ntiles + blockIdx.x];
   }
   __syncthreads();
-  for (int o = 1; o < kRadix; o <<= 1) {
-    const uint32_t add = threadIdx.x >= (unsigned)o ? s_start[threadIdx.x - o] : 0;
-    __syncthreads();
-    s_start[threadIdx.x] += add;
-    __syncthreads();
-  }
-  s_start[threadIdx.x] -= s_tot[threadIdx.x];
-  __syncthreads();
-#pragma unroll
   for (int r = 0; r < kPerThread; r++) {
-    const uint32_t li = (uint32_t)(warp * kPerWarp + r * 32 + lane);
-    if (li < cnt) {
-      const uint32_t d = (uint32_t)((key[r] >> shift) & 0xFF);
-      s_keys[s_start[d] + s_warp[warp][d] + rank[r]] = key[r];
-    }
+    const uint32_t li = (uint32_t)r * kThreads + threadIdx.x;
+    if (li < cnt) s_keys[s_start[(key[r] >> shift) & 0xFF] + rank[r]] = key[r];
   }
   __syncthreads();
   for (uint32_t p = threadIdx.x; p < cnt; p += kThreads) {
