@@ -895,6 +895,25 @@ def profiled_dram_bytes_per_read() -> float | None:
     return None
 
 
+def value_counts_run(wl: Workload, reps: int = 5) -> dict:
+    """Cells per taxon of the resident table (k2g_db_value_counts, what
+    dump_table / kraken2-inspect report): one streaming pass over the table,
+    host clock around the whole call (allocation, kernels, copy-back)."""
+    counts, outside = wl.db.value_counts()
+    table_bytes = wl.cfg.capacity * 4
+    best = float("inf")
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        wl.db.value_counts()
+        best = min(best, time.perf_counter() - t0)
+    peak, source = hbm_peak()
+    gbs = table_bytes / best / 1e9
+    return {"table_gb": round(table_bytes / 1e9, 1), "s": round(best, 5),
+            "gb_per_s": round(gbs, 1), "frac_of_copy_peak": round(gbs / peak, 3),
+            "peak_source": source, "cells_counted": int(counts.sum()), "outside": outside,
+            "equals_table_size": int(counts.sum()) + outside == int(wl.db.info().size)}
+
+
 def long_reads_run(wl: Workload, log, call_bases: int = 200_000_000, n_pool: int = 1_500_000,
                    reps: int = 2) -> dict:
     """The serving mix (5 in 6 reads of 150 bp, 1 in 6 log-normal, mean
@@ -1082,6 +1101,7 @@ def run_ours(args, log):
     e2e_t, h2d, d2h, e2e_calls = e2e_run(wl, cfg.e2e_reads, max(2, min(args.steps, 5)))
     serving = None if args.skip_serving else serving_run(wl, log)
     long_reads = None if args.skip_serving else long_reads_run(wl, log)
+    value_counts = value_counts_run(wl)
     configs = None
     if not args.skip_configs:
         del runner
@@ -1136,6 +1156,7 @@ def run_ours(args, log):
         "minimizer_data": kmer,
         "serving": serving,
         "long_reads": long_reads,
+        "value_counts": value_counts,
         "configs": configs,
         "gpu_launches": launches,
         "clocks": clk.summary(),

@@ -101,6 +101,13 @@ k2g_status k2g_db_info_get(const k2g_db *db, k2g_db_info *out);
 k2g_status k2g_db_write_hash(const k2g_db *db, const char *hash_k2d);
 /* Copies the table (capacity cells) into host memory. */
 k2g_status k2g_db_download(const k2g_db *db, uint32_t *cells, uint64_t *size);
+/* Cells per taxon -- CompactHashTable::GetValueCounts (src/compact_hash.h:503-519),
+ * what dump_table / kraken2-inspect report (src/dump_table.cc:59-101):
+ * counts[t] (host, node_count entries) = cells whose value is taxon t
+ * (counts[0] = 0); *outside (may be NULL) = cells whose value is not a node
+ * of the taxonomy.  One streaming pass over the table; synchronises `stream`. */
+k2g_status k2g_db_value_counts(const k2g_db *db, uint64_t *counts, uint64_t *outside,
+                               void *stream);
 
 /* Batched lookup -- KeyValueStore::GetBatch (src/kv_store.h:29,
  * src/compact_hash.h:380-392): vals[i] = Get(keys[i]), 0 when absent. */

@@ -34,7 +34,8 @@ HIT_SLOW = 0x80000000       # K2G_HIT_SLOW
 
 # Every symbol include/k2g.h declares.
 EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g_db_close",
-           "k2g_db_info_get", "k2g_db_write_hash", "k2g_db_download", "k2g_lookup",
+           "k2g_db_info_get", "k2g_db_write_hash", "k2g_db_download", "k2g_db_value_counts",
+           "k2g_lookup",
            "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
            "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_sector_gather",
            "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
@@ -106,6 +107,7 @@ def lib():
             "k2g_db_info_get": [vp, C.POINTER(DbInfo)],
             "k2g_db_write_hash": [vp, C.c_char_p],
             "k2g_db_download": [vp, vp, C.POINTER(u64)],
+            "k2g_db_value_counts": [vp, vp, vp, vp],
             "k2g_lookup": [vp, vp, vp, u64, vp],
             "k2g_lookup_host": [vp, vp, vp, u64],
             "k2g_scan": [vp, vp, vp, u64, vp, vp, vp],
@@ -202,6 +204,14 @@ class Database:
         size = C.c_uint64()
         check(lib().k2g_db_download(self.h, cells.ctypes.data, C.byref(size)))
         return cells, size.value
+
+    def value_counts(self, stream: int = 0):
+        """Cells per taxon (uint64, node_count entries) and the number of
+        cells whose value is not a taxonomy node."""
+        counts = np.zeros(self.info().node_count, np.uint64)
+        outside = C.c_uint64()
+        check(lib().k2g_db_value_counts(self.h, counts.ctypes.data, C.byref(outside), stream))
+        return counts, outside.value
 
     def write_hash(self, path: str):
         check(lib().k2g_db_write_hash(self.h, path.encode()))

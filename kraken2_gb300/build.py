@@ -26,10 +26,11 @@ HOST_FLAGS = "-fPIC,-O3,-ffp-contract=off,-Wall"
 
 CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc.cu",
               "classify_static.cu", "counters.cu", "build_ordered.cu",
-              "server.cu", "classify_split.cu"]
+              "server.cu", "classify_split.cu", "inspect.cu"]
 CC_SOURCES = ["db.cc"]
-# the classify drop-in (host C++ over the C ABI)
+# the drop-in executables (host C++ over the C ABI)
 HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "report.cc"]
+DUMP_SOURCES = ["dump_table_main.cc", "report.cc"]
 
 
 def nvcc() -> str:
@@ -66,15 +67,19 @@ def classify_path() -> str:
     return os.path.join(OUT, "classify")
 
 
+def dump_table_path() -> str:
+    return os.path.join(OUT, "dump_table")
+
+
 def _build_classify(lib: str):
-    """g++ for the drop-in; it finds libk2g.so next to itself ($ORIGIN)."""
+    """g++ for the drop-ins; they find libk2g.so next to themselves ($ORIGIN)."""
     gxx = shutil.which("g++") or "g++"
-    exe = classify_path()
-    tmp = exe + ".tmp"
-    _run([gxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I", INCLUDE,
-          *[os.path.join(HOST, s) for s in HOST_SOURCES],
-          "-L", OUT, "-lk2g", "-Wl,-rpath,$ORIGIN", "-o", tmp])
-    os.replace(tmp, exe)
+    for exe, sources in ((classify_path(), HOST_SOURCES), (dump_table_path(), DUMP_SOURCES)):
+        tmp = exe + ".tmp"
+        _run([gxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I", INCLUDE,
+              *[os.path.join(HOST, s) for s in sources],
+              "-L", OUT, "-lk2g", "-Wl,-rpath,$ORIGIN", "-o", tmp])
+        os.replace(tmp, exe)
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
@@ -82,7 +87,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     lib = os.path.join(OUT, "libk2g.so")
     deps = _deps()
-    if not force and _newer(lib, deps + [__file__]) and _newer(classify_path(), deps + [lib]):
+    if (not force and _newer(lib, deps + [__file__]) and _newer(classify_path(), deps + [lib])
+            and _newer(dump_table_path(), deps + [lib])):
         return lib
     if not force and _newer(lib, deps + [__file__]):
         _build_classify(lib)
