@@ -33,13 +33,25 @@ value_hist_kernel(const uint4 *cells, uint64_t n_vec, uint32_t value_mask, uint3
     if (v - lo < bins) atomicAdd(&h[v - lo], 1u);
     else if (count_outside && v >= node_count) mine_outside++;
   };
+  // kUnroll loads in flight per thread before any is counted (one block of
+  // 1024 threads per SM needs them to keep enough bytes in flight)
+  constexpr int kUnroll = 8;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_vec;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint4 c = __ldcs(cells + i);   // streamed once: no reuse in cache
-    add(c.x & value_mask);
-    add(c.y & value_mask);
-    add(c.z & value_mask);
-    add(c.w & value_mask);
+       i += kUnroll * stride) {
+    uint4 c[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const uint64_t j = i + u * stride;
+      c[u] = j < n_vec ? __ldcs(cells + j) : make_uint4(0, 0, 0, 0);   // streamed once
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      add(c[u].x & value_mask);
+      add(c[u].y & value_mask);
+      add(c[u].z & value_mask);
+      add(c[u].w & value_mask);
+    }
   }
   if (count_outside && mine_outside) atomicAdd(outside, (unsigned long long)mine_outside);
   __syncthreads();
