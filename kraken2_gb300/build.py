@@ -29,7 +29,7 @@ CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc
               "server.cu", "classify_split.cu", "inspect.cu"]
 CC_SOURCES = ["db.cc"]
 # the drop-in executables (host C++ over the C ABI)
-HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "report.cc"]
+HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "block_reader.cc", "report.cc"]
 DUMP_SOURCES = ["dump_table_main.cc", "report.cc"]
 
 

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "k2g.h"
+#include "block_reader.h"
 #include "report.h"
 #include "seq_reader.h"
 
@@ -225,12 +226,14 @@ struct Batch {
   std::unique_ptr<uint64_t[]> runs;   // hit-list runs, uninitialised until written
   uint64_t runs_cap = 0;
   std::vector<uint64_t> run_start;    // first run of each fragment
+  uint64_t silent_from = UINT64_MAX;  // fragments from here on are counted, not written
 
   uint64_t frags() const { return block.size(); }
   void clear() {
     m1.clear();
     m2.clear();
     block.clear();
+    silent_from = UINT64_MAX;
   }
 };
 
@@ -398,6 +401,7 @@ class Pipeline {
       pc.stats.total_sequences++;
       pc.stats.total_bases += len1 + len2;
       if (c) pc.stats.total_classified++;
+      if (i >= b.silent_from) continue;
       if (out_.kraken) {
         // kraken line (src/classify.cc:908-945)
         ko += c ? "C\t" : "U\t";
@@ -480,36 +484,82 @@ class Pipeline {
 };
 
 // ProcessFiles (src/classify.cc:481-690): one input (or pair of inputs),
-// read block by block into batches of whole blocks.
+// read in the reference's blocks, whole blocks to a batch.  A regular file is
+// parsed on the pool's threads; the blocks are the same either way.
+//
+// A block load that comes back empty (src/classify.cc:521-545: the input
+// has ended, or a record whose qualities were dropped came first) ends the
+// reading thread that made it, but the other -p - 1 threads read on.  Their
+// blocks are classified and counted (stats, report, -K counters) but never
+// written: the output queue waits for the empty block's id
+// (src/classify.cc:647-673).  So reading ends at the -p-th empty load, and
+// the fragments read after the first are silent.
 void process_files(const char *f1, const char *f2, const Options &o, Pipeline &pl,
-                   Outputs &out, uint32_t &block_id) {
-  k2host::SeqReader reader1(k2host::open_input(f1));
-  k2host::SeqReader reader2(f2 ? k2host::open_input(f2) : -1);
+                   Outputs &out, uint32_t &block_id, k2host::WorkerPool &pool) {
+  k2host::BlockReader reader1(k2host::open_input(f1), &pool);
+  k2host::BlockReader reader2(f2 ? k2host::open_input(f2) : -1, &pool);
+  const bool two_files = o.paired_end_processing && !o.single_file_pairs;
+  const bool interleaved = o.paired_end_processing && o.single_file_pairs;
+  k2host::BlockReader::Cut cut;
+  if (!o.paired_end_processing) cut.bytes = kBlockBytes;
+  else cut.records = two_files ? kFragmentsPerBatch : kFragmentsPerBatch * 2;
+  const int minq = o.minimum_quality_score;
+  const uint64_t max_empty = (uint64_t)o.num_threads;
+  uint64_t empty = 0;
+  std::vector<uint32_t> c1, c2;
+  std::vector<std::pair<uint64_t, uint64_t>> drop1, drop2;   // records a block leaves out
   Batch *b = pl.take();
-  while (true) {
-    const size_t s1 = b->m1.size(), s2 = b->m2.size();
-    size_t frags;
-    if (!o.paired_end_processing) {
-      frags = reader1.load_block(b->m1, kBlockBytes);
-      if (!frags) break;
-    } else if (!o.single_file_pairs) {
-      // a fragment needs both mates; the rest of a longer block is dropped
-      const size_t n1 = reader1.load_batch(b->m1, kFragmentsPerBatch);
-      const size_t n2 = n1 ? reader2.load_batch(b->m2, kFragmentsPerBatch) : 0;
-      frags = std::min(n1, n2);
-      b->m1.truncate(s1 + frags);
-      b->m2.truncate(s2 + frags);
-      if (!frags) break;
-    } else {
-      const size_t n1 = reader1.load_batch(b->m1, kFragmentsPerBatch * 2);
-      frags = n1 / 2;
-      b->m1.truncate(s1 + 2 * frags);
-      if (!n1) break;
+  while (empty < max_empty) {
+    c1.clear();
+    c2.clear();
+    const uint64_t s1 = b->m1.size(), s2 = b->m2.size(), q1 = b->m1.seq.size();
+    const uint64_t room = kGpuBatchBases - std::min(kGpuBatchBases, q1 + b->m2.seq.size());
+    reader1.load_blocks(b->m1, c1, cut, q1 + std::max<uint64_t>(two_files ? room / 2 : room, 1),
+                        SIZE_MAX, max_empty - empty, 0, minq);
+    if (two_files) {   // one second-file load per non-empty first-file block
+      const size_t loads = (size_t)std::count_if(c1.begin(), c1.end(), [](uint32_t c) { return c; });
+      if (loads)
+        reader2.load_blocks(b->m2, c2, cut, UINT64_MAX, loads, max_empty - empty,
+                            b->m1.seq.size() - q1, minq);
     }
-    b->m1.mask_low_quality(s1, o.minimum_quality_score);
-    b->m2.mask_low_quality(s2, o.minimum_quality_score);
-    b->block.insert(b->block.end(), frags, block_id++);
-    initialize_outputs(o, out);
+    drop1.clear();
+    drop2.clear();
+    uint64_t a1 = s1, a2 = s2;   // the current block's first record in m1 / m2
+    size_t j = 0;                // the current block's load from the second file
+    for (size_t i = 0; i < c1.size() && empty < max_empty; i++) {
+      const uint64_t n1 = c1[i];
+      uint64_t n2 = 0, frags;
+      bool ok = n1 > 0;
+      if (ok && two_files) {
+        // no load left means the second file ended: the load comes back empty
+        n2 = j < c2.size() ? c2[j] : 0;
+        j += j < c2.size();
+        ok = n2 > 0;
+      }
+      if (!ok) {   // this thread's empty load: its block (any first mates) is lost
+        drop1.emplace_back(a1, a1 + n1);
+        a1 += n1;
+        empty++;
+        block_id++;
+        continue;
+      }
+      // fragments: pairs while both mates last (src/classify.cc:553-565)
+      frags = two_files ? std::min(n1, n2) : interleaved ? n1 / 2 : n1;
+      drop1.emplace_back(a1 + (interleaved ? 2 * frags : frags), a1 + n1);
+      if (two_files) drop2.emplace_back(a2 + frags, a2 + n2);
+      a1 += n1;
+      a2 += n2;
+      if (empty && b->silent_from == UINT64_MAX) b->silent_from = b->frags();
+      b->block.insert(b->block.end(), frags, block_id++);
+      initialize_outputs(o, out);
+    }
+    // reading ended inside the loads: what was read after the last load is unused
+    b->m1.truncate(a1);
+    b->m2.truncate(a2);
+    for (size_t k = drop1.size(); k-- > 0;) b->m1.erase(drop1[k].first, drop1[k].second);
+    for (size_t k = drop2.size(); k-- > 0;) b->m2.erase(drop2[k].first, drop2[k].second);
+    // an ended input makes every later load come back empty
+    if (reader1.done() || (two_files && reader2.done())) empty = max_empty;
     if (b->m1.seq.size() + b->m2.seq.size() >= kGpuBatchBases) {
       pl.submit(b);
       b = pl.take();
@@ -566,6 +616,7 @@ int main(int argc, char **argv) {
   rc.taxon_reads.assign(tax.nodes.size(), 0);
   Outputs out;
   Pipeline pl(o, db, tax, counters, rc, out);
+  k2host::WorkerPool pool(o.num_threads);
   uint32_t block_id = 0;
 
   timeval tv1, tv2;
@@ -573,7 +624,7 @@ int main(int argc, char **argv) {
   if (o.filenames.empty()) {
     if (o.paired_end_processing && !o.single_file_pairs)
       errx(EX_USAGE, "paired end processing used with no files specified");
-    process_files(nullptr, nullptr, o, pl, out, block_id);
+    process_files(nullptr, nullptr, o, pl, out, block_id, pool);
   } else {
     for (size_t i = 0; i < o.filenames.size(); i++) {
       if (o.paired_end_processing && !o.single_file_pairs) {
@@ -581,10 +632,11 @@ int main(int argc, char **argv) {
           pl.finish();   // the earlier inputs' output is written first
           errx(EX_USAGE, "paired end processing used with unpaired file");
         }
-        process_files(o.filenames[i].c_str(), o.filenames[i + 1].c_str(), o, pl, out, block_id);
+        process_files(o.filenames[i].c_str(), o.filenames[i + 1].c_str(), o, pl, out, block_id,
+                      pool);
         i++;
       } else {
-        process_files(o.filenames[i].c_str(), nullptr, o, pl, out, block_id);
+        process_files(o.filenames[i].c_str(), nullptr, o, pl, out, block_id, pool);
       }
     }
   }

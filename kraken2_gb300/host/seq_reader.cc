@@ -5,6 +5,8 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 
@@ -16,8 +18,8 @@ constexpr size_t kBufSize = 4u << 20;
 // isspace() in the C locale: '\t', '\n', '\v', '\f', '\r' and ' '.
 inline bool is_space(unsigned char c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
 
-template <class T>
-void grow_to(std::vector<T> &v, size_t n) {
+template <class V>
+void grow_to(V &v, size_t n) {
   if (v.capacity() < n) v.reserve(n);
 }
 }  // namespace
@@ -39,6 +41,19 @@ void RecordSet::truncate(size_t n) {
   recs.resize(n);
 }
 
+void RecordSet::erase(size_t first, size_t last) {
+  last = std::min(last, recs.size());
+  if (first >= last) return;
+  const uint64_t t0 = recs[first].text, t1 = text_end(last);
+  const uint64_t q0 = seq_off[first], q1 = seq_off[last];
+  text.erase(text.begin() + t0, text.begin() + t1);
+  seq.erase(seq.begin() + q0, seq.begin() + q1);
+  for (size_t i = last; i < recs.size(); i++) recs[i].text -= t1 - t0;
+  for (size_t i = last + 1; i < seq_off.size(); i++) seq_off[i] -= q1 - q0;
+  recs.erase(recs.begin() + first, recs.begin() + last);
+  seq_off.erase(seq_off.begin() + first + 1, seq_off.begin() + last + 1);
+}
+
 void RecordSet::reserve(size_t seq_bytes, size_t text_bytes, size_t records) {
   grow_to(seq, seq_bytes);
   grow_to(text, text_bytes);
@@ -46,9 +61,9 @@ void RecordSet::reserve(size_t seq_bytes, size_t text_bytes, size_t records) {
   grow_to(recs, records);
 }
 
-void RecordSet::mask_low_quality(size_t first, int min_quality) {
+void RecordSet::mask_low_quality(size_t first, size_t last, int min_quality) {
   if (min_quality <= 0) return;
-  for (size_t i = first; i < recs.size(); i++) {
+  for (size_t i = first; i < last; i++) {
     if (!recs[i].fastq) continue;
     const signed char *q = reinterpret_cast<const signed char *>(qual(i));
     char *s = seq_at(i);
@@ -74,12 +89,24 @@ SeqReader::SeqReader(int fd) : fd_(fd), own_fd_(fd > 2) {
       map_len_ = len;
       data_ = static_cast<const char *>(p);
       begin_ = (size_t)(at - base);
+      map_start_ = begin_;
       end_ = len;   // the rest of the file is one buffer; refill() then ends it
       return;
     }
   }
   buf_.resize(kBufSize);
   data_ = buf_.data();
+}
+
+SeqReader::SeqReader(const char *data, size_t begin, size_t end)
+    : fd_(-1), own_fd_(false), data_(data), span_(true), begin_(begin), end_(end) {}
+
+size_t SeqReader::next_header() const {
+  if (eof_ || err_) return SIZE_MAX;
+  if (last_char_) return begin_ - 1;   // the header byte has been consumed
+  for (size_t i = begin_; i < end_; i++)
+    if (data_[i] == '>' || data_[i] == '@') return i;
+  return SIZE_MAX;
 }
 
 SeqReader::~SeqReader() {
@@ -93,7 +120,7 @@ bool SeqReader::refill() {
   if (eof_ || err_) return false;
   begin_ = 0;
   end_ = 0;
-  if (map_) {   // the mapped file has been read to its end
+  if (map_ || span_) {   // the mapped file or the span has been read to its end
     eof_ = true;
     return false;
   }
@@ -118,7 +145,7 @@ inline int SeqReader::getc() {
 // starts in dst (a line field may continue earlier lines).  Returns the
 // field's length, -1 when the input had ended before anything was read, -3
 // on a read error.
-int SeqReader::read_until(bool line, std::vector<char> &dst, size_t field, int *delim) {
+int SeqReader::read_until(bool line, Arena<char> &dst, size_t field, int *delim) {
   if (delim) *delim = 0;
   bool got = false;
   for (;;) {
@@ -149,7 +176,7 @@ int SeqReader::read_until(bool line, std::vector<char> &dst, size_t field, int *
   return (int)(dst.size() - field);
 }
 
-int SeqReader::read(RecordSet &s) {
+int SeqReader::read_record(RecordSet &s) {
   int c;
   if (last_char_ == 0) {   // find the next header
     while ((c = getc()) >= 0 && c != '>' && c != '@') {

@@ -112,21 +112,36 @@ class Stream:
         return len(seq), Rec(bytes(name), bytes(comment), bytes(seq), bytes(qual) or None)
 
 
-def blocks(data: bytes, block_bytes: int | None = None, count: int | None = None) -> list:
-    """The blocks a reader thread would load until the input is exhausted:
-    LoadBlock(block_bytes) or LoadBatch(count) repeated while it succeeds."""
+def block_attempts(data: bytes, block_bytes: int | None = None, count: int | None = None):
+    """Successive LoadBlock(block_bytes) / LoadBatch(count) calls on one stream
+    (src/seqreader.h:101-159): yields (records, ended) forever, records
+    possibly empty; ended is true once the stream has ended (every later
+    call comes back empty)."""
     s = Stream(data)
-    out = []
     while True:
-        recs, total = [], 0
+        recs, total, last = [], 0, 0
         while (total < block_bytes) if block_bytes is not None else (len(recs) < count):
             r, rec = s.read()
             if r < 0:
+                last = r
                 break
             recs.append(rec)
             total += len(rec.seq)
-        if not recs:
+        yield recs, (not recs and last in (-1, -3))
+
+
+def blocks(data: bytes, block_bytes: int | None = None, count: int | None = None,
+           empties: int = 1) -> list:
+    """The blocks loaded until `empties` loads have come back empty or the
+    stream has ended; empty blocks before the last are kept (as [])."""
+    out, seen = [], 0
+    for recs, ended in block_attempts(data, block_bytes, count):
+        if ended:
             return out
+        if not recs:
+            seen += 1
+            if seen == empties:
+                return out
         out.append(recs)
 
 

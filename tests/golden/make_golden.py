@@ -228,9 +228,31 @@ def hll_vectors():
         f.write(r.stdout.decode())
 
 
+def runs_only(tags):
+    """Re-runs only the named classify runs against the committed databases
+    (python tests/golden/make_golden.py --runs TAG ...), updating the
+    manifest's entries for them and their read sets."""
+    work = tempfile.mkdtemp(prefix="k2golden_")
+    with open(os.path.join(HERE, "manifest.json")) as f:
+        manifest = json.load(f)
+    for tag in tags:
+        db, args, key = readsets.RUNS[tag]
+        paths = readsets.write_set(key, work)
+        manifest["reads"][key] = [hashlib.sha256(open(p, "rb").read()).hexdigest() for p in paths]
+        manifest["runs"][tag] = {"db": db, "args": args, "reads": key,
+                                 "sha256": classify(db, args, paths, work, tag)}
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+    shutil.rmtree(work)
+    print("runs written:", " ".join(tags))
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "classify")):
         sys.exit("build the reference first: make -C oracle ref")
+    if len(sys.argv) > 2 and sys.argv[1] == "--runs":
+        runs_only(sys.argv[2:])
+        return
     work = tempfile.mkdtemp(prefix="k2golden_")
     manifest = {"dbs": {}, "runs": {}, "reads": {}}
     dbs = {

@@ -101,11 +101,84 @@ def build(key):
     raise KeyError(key)
 
 
+def _fastq_bytes(r, damage=None, stop=None) -> bytes:
+    """FASTQ text of a Reads object; damage maps a record index to how it is
+    written: "short" (one quality missing: the quality reader takes the next
+    record's header line as qualities, drops the record and ends its block,
+    and the header search resumes inside the next record), "long" (one
+    quality too many: the record is dropped and ends its block, and the next
+    header is intact), "junk" (a stray line without '@' or '>' before it),
+    "multiline" (sequence and qualities over two lines each), "crlf"."""
+    damage = damage or {}
+    out = []
+    for i, (n, s, q) in enumerate(zip(r.names, r.seqs, r.quals)):
+        if stop is not None and i == stop:
+            break
+        kind = damage.get(i)
+        if kind == "short":
+            out.append(b"@" + n + b"\n" + s + b"\n+\n" + q[:-1] + b"\n")
+        elif kind == "long":
+            out.append(b"@" + n + b"\n" + s + b"\n+\n" + q + b"I\n")
+        elif kind == "junk":
+            out.append(b"some stray text\n\n" + b"@" + n + b"\n" + s + b"\n+\n" + q + b"\n")
+        elif kind == "multiline":
+            h = len(s) // 2
+            out.append(b"@" + n + b"\n" + s[:h] + b"\n" + s[h:] + b"\n+\n" + q[:h] + b"\n"
+                       + q[h:] + b"\n")
+        elif kind == "crlf":
+            out.append(b"@" + n + b"\r\n" + s + b"\r\n+\r\n" + q + b"\r\n")
+        else:
+            out.append(b"@" + n + b"\n" + s + b"\n+\n" + q + b"\n")
+    return b"".join(out)
+
+
+def _damaged(key, p):
+    """Inputs with broken records.  dmg_se: single reads; a broken record
+    ends a block, and two clean drops in a row make a load come back empty.
+    dmg_pe: mate files where the second has broken records that end blocks
+    early and leave one of its loads empty while the first file reads on,
+    and ends first (the reference drops the unpaired rest of each block and
+    pairs what follows as it comes).  dmg_il: interleaved pairs where a
+    broken record leaves a block with an odd record count."""
+    if key == "dmg_se":
+        r = synth.sample_reads(synth.Rng(108), genomes_of("db_a"), 8000, 100, 0.01, 0.10,
+                               n_frac=0.03)
+        dmg = {500: "short", 1200: "junk", 2000: "multiline", 3000: "crlf", 5500: "long",
+               7000: "long", 7001: "long"}
+        with open(p(key + ".fq"), "wb") as f:
+            f.write(_fastq_bytes(r, dmg))
+        return [p(key + ".fq")]
+    if key == "dmg_pe":
+        m1, m2 = synth.sample_reads(synth.Rng(109), genomes_of("db_a"), 30600, 50, 0.01, 0.10,
+                                    mates=2, insert=(130, 20))
+        with open(p(key + "_1.fq"), "wb") as f:
+            f.write(_fastq_bytes(m1, {4000: "junk"}))
+        with open(p(key + "_2.fq"), "wb") as f:
+            f.write(_fastq_bytes(m2, {3000: "short", 6000: "crlf", 12500: "long", 12501: "long"},
+                                 stop=14000))
+        return [p(key + "_1.fq"), p(key + "_2.fq")]
+    if key == "dmg_il":
+        m1, m2 = synth.sample_reads(synth.Rng(110), genomes_of("db_a"), 10300, 60, 0.01, 0.10,
+                                    mates=2, insert=(150, 20))
+        inter = synth.Reads([], [], [])
+        for i in range(len(m1.names)):
+            for m in (m1, m2):
+                inter.names.append(m.names[i])
+                inter.seqs.append(m.seqs[i])
+                inter.quals.append(m.quals[i])
+        with open(p(key + ".fq"), "wb") as f:
+            f.write(_fastq_bytes(inter, {1001: "short", 9000: "multiline"}))
+        return [p(key + ".fq")]
+    raise KeyError(key)
+
+
 def write_set(key, directory):
     """Writes read set ``key`` into directory; returns the input file list the
     reference classify was given."""
     os.makedirs(directory, exist_ok=True)
     p = lambda name: os.path.join(directory, name)  # noqa: E731
+    if key.startswith("dmg_"):
+        return _damaged(key, p)
     if key in ("pe100", "blk_pe"):
         m1, m2 = build(key)
         m1.write_fastq(p(key + "_1.fq"))
@@ -131,7 +204,7 @@ def write_set(key, directory):
 
 
 READ_SETS = ["se150", "pe100", "pe100_interleaved", "se150_fasta", "long", "edge",
-             "blk_se", "blk_pe", "se_b", "se_c"]
+             "blk_se", "blk_pe", "se_b", "se_c", "dmg_se", "dmg_pe", "dmg_il"]
 
 
 def write_all(directory):
@@ -160,4 +233,7 @@ RUNS = {
     "blk_pe": ("db_a", ["-P", "-g", "2", "-R", "x", "-K"], "blk_pe"),
     "db_b_default": ("db_b", ["-T", "0", "-g", "2", "-R", "x", "-K"], "se_b"),
     "db_c_default": ("db_c", ["-T", "0.1", "-g", "2", "-R", "x", "-K"], "se_c"),
+    "dmg_se": ("db_a", ["-T", "0", "-g", "2", "-Q", "10", "-R", "x", "-K", "-U", "u.fq"], "dmg_se"),
+    "dmg_pe": ("db_a", ["-P", "-T", "0.1", "-g", "2", "-R", "x", "-K"], "dmg_pe"),
+    "dmg_il": ("db_a", ["-S", "-g", "2", "-R", "x", "-K"], "dmg_il"),
 }

@@ -84,6 +84,11 @@ class Batch:
     headers: list            # per fragment, mate-1 header
     lens: list               # per fragment, (len1,) or (len1, len2)
     blocks: np.ndarray       # uint32 reader block of each fragment
+    written: int = -1        # fragments the reference writes out (-1: all)
+
+    def __post_init__(self):
+        if self.written < 0:
+            self.written = self.n_frags
 
 
 def _blocks_se(lens):
@@ -97,15 +102,70 @@ def _blocks_se(lens):
     return np.array(out, np.uint32)
 
 
-def batch_of(key: str) -> Batch:
+DAMAGED_SETS = {"dmg_se": "single", "dmg_pe": "two_files", "dmg_il": "interleaved"}
+GOLDEN_THREADS = 4   # -p of every golden run
+
+
+def _batch_from_files(key: str, datas: list, min_quality: int,
+                      threads: int = GOLDEN_THREADS) -> Batch:
+    """The fragments ProcessFiles (src/classify.cc:481-690) forms from the
+    input files with `threads` reader threads, read with the kseq
+    restatement.  Loads are single reads in blocks of 3 MiB of sequence; two
+    mate files in blocks of 10,000 records each (the second file is loaded
+    only after the first gave records; a pair block keeps pairs while both
+    mates last); interleaved pairs in blocks of 20,000 records (an odd
+    block's last record is left out).  A load that comes back empty ends one
+    thread, so reading ends at the threads-th empty load, and the fragments
+    read after the first empty load are classified and counted but not
+    written (Batch.written).  Bases are masked for -Q here (records without
+    qualities are not)."""
+    from oracle import kseq_records as ks
+    mode = DAMAGED_SETS[key]
+    cut = dict(block_bytes=SE_BLOCK_BYTES) if mode == "single" else dict(
+        count=PE_BLOCK_FRAGS if mode == "two_files" else 2 * PE_BLOCK_FRAGS)
+    g1 = ks.block_attempts(datas[0], **cut)
+    g2 = ks.block_attempts(datas[1], **cut) if mode == "two_files" else None
+    frags, blocks, empty, written, block_id = [], [], 0, None, 0
+    while empty < threads:
+        blk1, _ = next(g1)
+        blk2 = next(g2)[0] if (g2 is not None and blk1) else None
+        if not blk1 or (g2 is not None and not blk2):
+            empty += 1
+            block_id += 1
+            continue
+        if empty and written is None:
+            written = len(frags)
+        if mode == "single":
+            new = [(r,) for r in blk1]
+        elif mode == "two_files":
+            new = list(zip(blk1, blk2))
+        else:
+            new = [(blk1[2 * j], blk1[2 * j + 1]) for j in range(len(blk1) // 2)]
+        frags += new
+        blocks += [block_id] * len(new)
+        block_id += 1
+    seqs = [ks.mask_low_quality(r, min_quality) for f in frags for r in f]
+    off = np.zeros(len(seqs) + 1, np.uint64)
+    off[1:] = np.cumsum([len(x) for x in seqs])
+    return Batch(b"".join(seqs), None, off, len(frags), mode != "single",
+                 [f[0].name for f in frags], [tuple(len(r.seq) for r in f) for f in frags],
+                 np.array(blocks, np.uint32), len(frags) if written is None else written)
+
+
+def batch_of(key: str, min_quality: int = 0) -> Batch:
     """Regenerates read set ``key`` and lays it out as a Batch, checking the
-    generator against the manifest digest of the files the reference read."""
+    generator against the manifest digest of the files the reference read.
+    Damaged read sets are laid out from their files (masked for -Q there);
+    the others from the generator's records (the oracle masks them)."""
     import tempfile
     with tempfile.TemporaryDirectory() as d:
         files = readsets.write_set(key, d)
         want = manifest()["reads"][key]
-        got = [hashlib.sha256(open(p, "rb").read()).hexdigest() for p in files]
+        datas = [open(p, "rb").read() for p in files]
+        got = [hashlib.sha256(x).hexdigest() for x in datas]
         assert got == want, f"read generator drifted for {key}"
+    if key in DAMAGED_SETS:
+        return _batch_from_files(key, datas, min_quality)
     paired = key in ("pe100", "blk_pe", "pe100_interleaved")
     if key == "pe100_interleaved":
         m1, m2 = readsets.build("pe100")

@@ -87,7 +87,7 @@ def check_report(tag, db_name, taxon_reads, clade_kmers, distinct):
 def test_counters_match_golden_report(tag, run, mode):
     params, flags = parse_args(run["args"])
     db = k2g.Database.open(os.path.join(GOLDEN, run["db"]))
-    b = batch_of(run["reads"])
+    b = batch_of(run["reads"], params["min_quality"])
     reads, res, tr, keep = classify_with_events(db, b, params, MODES[mode])
     c = k2g.Counters(db)
     c.add(reads, res, torch().cuda.current_stream().cuda_stream)

@@ -100,7 +100,7 @@ def test_classify_runs(tag, run):
     """Per-read kraken lines and report counters of every golden run."""
     params, flags = parse_args(run["args"])
     o = _oracle_for(run["db"])
-    b = batch_of(run["reads"])
+    b = batch_of(run["reads"], params["min_quality"])
     calls, hg, nr, runs, base = o.classify(b.bases, b.quals, b.seq_off, b.n_frags, threads=4,
                                            **params)
     taxo = golden_db(run["db"]).taxo
@@ -108,6 +108,7 @@ def test_classify_runs(tag, run):
                          taxo, b.paired, names=flags["names"], quick=params["quick"])
              for i in range(b.n_frags)]
     want = golden_output(tag)
+    lines = lines[:b.written]   # read after an empty load: counted, not written
     assert len(lines) == len(want)
     bad = [i for i in range(len(want)) if lines[i] != want[i]]
     assert not bad, f"{len(bad)} lines differ, first: {lines[bad[0]]!r} vs {want[bad[0]]!r}"

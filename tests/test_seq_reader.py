@@ -1,7 +1,10 @@
-"""The drop-in's FASTA/FASTQ reader (kraken2_gb300/host/seq_reader.cc) against
-the byte-by-byte restatement of the reference's kseq reader: hand-written
-edge cases and seeded fuzz inputs, in both block modes, with quality
-masking.  CPU only (g++ builds a small dumper around the reader)."""
+"""The drop-in's FASTA/FASTQ reader (kraken2_gb300/host/seq_reader.cc, and
+the parallel BlockReader of block_reader.cc) against the byte-by-byte
+restatement of the reference's kseq reader: hand-written edge cases and
+seeded fuzz inputs, in both block modes, with quality masking.  The parallel
+reader runs with windows and segments of a few bytes, so that nearly every
+record boundary is a segment boundary and wrong guesses at record starts are
+common.  CPU only (g++ builds a small dumper around the readers)."""
 import os
 import shutil
 import subprocess
@@ -21,14 +24,20 @@ def dumper(tmp_path_factory):
     if not gxx:
         pytest.skip("g++ not available")
     exe = str(tmp_path_factory.mktemp("seqdump") / "seq_dump")
-    subprocess.run([gxx, "-O1", "-std=c++17", "-I", HOST, os.path.join(HERE, "seq_dump.cc"),
-                    os.path.join(HOST, "seq_reader.cc"), "-o", exe], check=True)
+    subprocess.run([gxx, "-O1", "-std=c++17", "-pthread", "-I", HOST,
+                    os.path.join(HERE, "seq_dump.cc"), os.path.join(HOST, "seq_reader.cc"),
+                    os.path.join(HOST, "block_reader.cc"), "-o", exe], check=True)
     return exe
 
 
 def parse_dump(raw: bytes):
-    out, pos = [], 0
+    """Blocks of a dump, and the parallel reader's "W <windows> <re-parsed>"
+    line when there is one."""
+    out, pos, stats = [], 0, None
     while pos < len(raw):
+        if raw.startswith(b"W ", pos):
+            stats = tuple(int(x) for x in raw[pos + 2:].split())
+            break
         nl = raw.index(b"\n", pos)
         tag, n = raw[pos:nl].split()
         assert tag == b"B"
@@ -52,28 +61,35 @@ def parse_dump(raw: bytes):
             pos += 1
             blk.append((name, comment, seq, qual))
         out.append(blk)
-    return out
+    return out, stats
 
 
-def expected(data: bytes, mode: str, arg: int, minq: int):
-    blks = ks.blocks(data, block_bytes=arg) if mode == "block" else ks.blocks(data, count=arg)
+def expected(data: bytes, mode: str, arg: int, minq: int, empties: int = 1):
+    blks = (ks.blocks(data, block_bytes=arg, empties=empties) if mode == "block"
+            else ks.blocks(data, count=arg, empties=empties))
     return [[(r.name, r.comment, ks.mask_low_quality(r, minq), r.qual) for r in b] for b in blks]
 
 
-def check(dumper, tmp_path, data: bytes, mode="block", arg=1 << 20, minq=0, pipe=False):
+def check(dumper, tmp_path, data: bytes, mode="block", arg=1 << 20, minq=0, pipe=False,
+          par=None, want=None):
     """A regular file is parsed in place (mapped); pipe=True feeds the same
-    bytes through standard input, read in buffer-sized pieces."""
+    bytes through standard input, read in buffer-sized pieces.  par =
+    (threads, window bytes, segment bytes) reads through BlockReader.
+    Returns the parallel reader's (windows, segments parsed again)."""
+    extra = [str(x) for x in par] if par else []
     if pipe:
-        r = subprocess.run([dumper, "-", mode, str(arg), str(minq)], input=data,
+        r = subprocess.run([dumper, "-", mode, str(arg), str(minq), *extra], input=data,
                            capture_output=True, check=True)
     else:
         path = tmp_path / "in.txt"
         path.write_bytes(data)
-        r = subprocess.run([dumper, str(path), mode, str(arg), str(minq)], capture_output=True,
-                           check=True)
-    got = parse_dump(r.stdout)
-    want = expected(data, mode, arg, minq)
-    assert got == want, (data[:200], got[:2], want[:2])
+        r = subprocess.run([dumper, str(path), mode, str(arg), str(minq), *extra],
+                           capture_output=True, check=True)
+    got, stats = parse_dump(r.stdout)
+    if want is None:
+        want = expected(data, mode, arg, minq)
+    assert got == want, (data[:200], par, got[:2], want[:2])
+    return stats
 
 
 CASES = [
@@ -106,6 +122,9 @@ def test_edge_cases(dumper, tmp_path, data, mode, arg):
     check(dumper, tmp_path, data, mode, arg)
     check(dumper, tmp_path, data, mode, arg, minq=20)
     check(dumper, tmp_path, data, mode, arg, pipe=True)
+    for par in [(1, 0, 0), (3, 4, 1), (4, 9, 2), (2, 1, 1)]:
+        check(dumper, tmp_path, data, mode, arg, minq=20 * (par[1] % 2), par=par)
+    check(dumper, tmp_path, data, mode, arg, pipe=True, par=(3, 4, 1))
 
 
 def _fuzz_input(rng) -> bytes:
@@ -140,7 +159,83 @@ def test_fuzz_against_restatement(dumper, tmp_path, seed):
     data = _fuzz_input(rng)
     mode, arg = [("block", 1 << 20), ("block", int(rng.integers(1, 30))),
                  ("batch", int(rng.integers(1, 5)))][seed % 3]
-    check(dumper, tmp_path, data, mode, arg, minq=int(rng.integers(0, 2)) * 15, pipe=seed % 2 == 1)
+    minq = int(rng.integers(0, 2)) * 15
+    check(dumper, tmp_path, data, mode, arg, minq=minq, pipe=seed % 2 == 1)
+    want = expected(data, mode, arg, minq)
+    for threads, window, segment in [(4, 1, 1), (3, 7, 2), (8, 64, 3), (2, 1 << 20, 16)]:
+        check(dumper, tmp_path, data, mode, arg, minq=minq, par=(threads, window, segment),
+              want=want)
+
+
+def _fastq(rng, n, lo=1, hi=300, crlf=False) -> bytes:
+    nl = b"\r\n" if crlf else b"\n"
+    out = []
+    for i in range(n):
+        L = int(rng.integers(lo, hi))
+        seq = rng.choice(np.frombuffer(b"ACGTN", np.uint8), L).tobytes()
+        qual = rng.choice(np.frombuffer(b"!#5I@>+", np.uint8), L).tobytes()
+        out.append(b"@read%d x" % i + nl + seq + nl + b"+" + nl + qual + nl)
+    return b"".join(out)
+
+
+@pytest.mark.parametrize("mode,arg", [("block", 3000), ("block", 1 << 16), ("batch", 37),
+                                      ("batch", 2000)])
+def test_parallel_reader_clean_inputs(dumper, tmp_path, mode, arg):
+    """Well-formed FASTQ (qualities that start with '@', '>' and '+') and
+    multi-line FASTA over many windows: the records match, and the guesses at
+    record starts are right."""
+    rng = np.random.default_rng(arg)
+    fq = _fastq(rng, 4000)
+    windows, reparsed = check(dumper, tmp_path, fq, mode, arg, minq=10, par=(4, 40_000, 2_000))
+    assert windows > 5 and reparsed == 0
+    fa = b"".join(b">chr%d desc\n" % i + b"\n".join(
+        rng.choice(np.frombuffer(b"ACGT", np.uint8), 60).tobytes() for _ in range(int(rng.integers(1, 30))))
+        + b"\n" for i in range(3000))
+    windows, reparsed = check(dumper, tmp_path, fa, mode, arg, par=(4, 40_000, 2_000))
+    assert windows > 5 and reparsed == 0
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_parallel_reader_damaged_fastq(dumper, tmp_path, seed):
+    """FASTQ with broken records, stray bytes, multi-line and CRLF records
+    spliced in: wrong guesses at record starts are parsed again, and the
+    blocks still match."""
+    rng = np.random.default_rng(100 + seed)
+    parts = []
+    for _ in range(40):
+        parts.append(_fastq(rng, int(rng.integers(1, 30)), 0, 40, crlf=rng.random() < 0.2))
+        parts.append(_fuzz_input(rng))
+    data = b"".join(parts)
+    mode, arg = [("block", 500), ("batch", 7), ("block", 1 << 20)][seed % 3]
+    minq = 15 * (seed % 2)
+    want = expected(data, mode, arg, minq)
+    for par in [(4, 300, 20), (6, 2_000, 50), (2, 64, 8)]:
+        check(dumper, tmp_path, data, mode, arg, minq=minq, par=par, want=want)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_parallel_reader_reads_past_empty_blocks(dumper, tmp_path, seed):
+    """Loads go on after one comes back empty (a record with dropped
+    qualities first in its block), until a given number have, as the
+    reference's reader threads do; two clean drops in a row make an empty
+    block."""
+    rng = np.random.default_rng(300 + seed)
+    parts = []
+    for _ in range(30):
+        parts.append(_fastq(rng, int(rng.integers(0, 12)), 0, 30))
+        if rng.random() < 0.5:
+            parts.append(b"@bad1\nACGT\n+\nIIIII\n@bad2\nAC\n+\nIII\n")
+        else:
+            parts.append(_fuzz_input(rng))
+    data = b"".join(parts)
+    mode, arg = [("block", 60), ("batch", 3), ("block", 1 << 20), ("batch", 50)][seed % 4]
+    for empties in (1, 2, 5, 1000):
+        want = expected(data, mode, arg, 0, empties)
+        for par in [(4, 200, 16), (3, 1 << 20, 64), (2, 1, 1)]:
+            check(dumper, tmp_path, data, mode, arg, par=(*par, empties), want=want)
+        check(dumper, tmp_path, data, mode, arg, par=(2, 0, 0, empties), want=want, pipe=True)
+        if empties == 1000:
+            assert sum(1 for b in want if not b) >= 1
 
 
 def test_records_spanning_input_buffers(dumper, tmp_path):
@@ -152,3 +247,5 @@ def test_records_spanning_input_buffers(dumper, tmp_path):
     data += b"\n" + b"".join(b">s%d\n%s\n" % (i, big[i:i + 97]) for i in range(60_000))
     check(dumper, tmp_path, data, "block", 3 << 20)
     check(dumper, tmp_path, data, "block", 3 << 20, pipe=True)
+    check(dumper, tmp_path, data, "block", 3 << 20, par=(8, 1 << 20, 1 << 16))
+    check(dumper, tmp_path, data, "batch", 10_000, par=(8, 0, 0))
