@@ -318,6 +318,24 @@ uint64_t k2g_kernel_launches(void);
 k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
                             uint64_t n, int ordered, void *stream);
 
+/* ProcessSequence of the deterministic build (src/build_db.h:217-326) for a
+ * batch of sequences in host memory: sequence i is bases[seq_off[i],
+ * seq_off[i+1]) and taxids[i] its internal taxon (0: the sequence is
+ * skipped, as the reference skips sequences without a mapped ID).  Each
+ * sequence is cut into blocks of block_size k-mer starts (-B) scanned in
+ * subblocks of subblock_size (-b); each block's distinct minimizers -- of
+ * its unambiguous k-mers, plus the one the reference's scanner reports at
+ * the start of each subblock past position 0, above the table's subsampling
+ * threshold -- are inserted ordered by MurmurHash3 mod 256 and then by
+ * value, block after block, sequence after sequence.  With ordered != 0 the
+ * table is the one the reference's build leaves after the same sequences
+ * (ordered == 0: the fast unordered insert, -F).  Batches must hold fewer
+ * than 2^32 bases; *n_keys (may be NULL) receives the number of (block,
+ * minimizer) pairs inserted.  DNA tables only.  Synchronous. */
+k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const uint64_t *seq_off,
+                               const uint32_t *taxids, uint64_t n_seqs, uint64_t block_size,
+                               uint64_t subblock_size, int ordered, uint64_t *n_keys);
+
 #ifdef __cplusplus
 }
 #endif

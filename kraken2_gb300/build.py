@@ -26,11 +26,12 @@ HOST_FLAGS = "-fPIC,-O3,-ffp-contract=off,-Wall"
 
 CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc.cu",
               "classify_static.cu", "counters.cu", "build_ordered.cu",
-              "server.cu", "classify_split.cu", "inspect.cu"]
+              "server.cu", "classify_split.cu", "inspect.cu", "build_gather.cu"]
 CC_SOURCES = ["db.cc"]
 # the drop-in executables (host C++ over the C ABI)
 HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "block_reader.cc", "report.cc"]
 DUMP_SOURCES = ["dump_table_main.cc", "report.cc"]
+BUILD_DB_SOURCES = ["build_db_main.cc", "ncbi_taxonomy.cc", "seq_reader.cc", "block_reader.cc"]
 
 
 def nvcc() -> str:
@@ -71,15 +72,28 @@ def dump_table_path() -> str:
     return os.path.join(OUT, "dump_table")
 
 
+def build_db_path() -> str:
+    return os.path.join(OUT, "build_db")
+
+
+def _executables():
+    return ((classify_path(), HOST_SOURCES), (dump_table_path(), DUMP_SOURCES),
+            (build_db_path(), BUILD_DB_SOURCES))
+
+
 def _build_classify(lib: str):
-    """g++ for the drop-ins; they find libk2g.so next to themselves ($ORIGIN)."""
+    """g++ for the drop-ins, in parallel; they find libk2g.so next to
+    themselves ($ORIGIN)."""
     gxx = shutil.which("g++") or "g++"
-    for exe, sources in ((classify_path(), HOST_SOURCES), (dump_table_path(), DUMP_SOURCES)):
-        tmp = exe + ".tmp"
-        _run([gxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I", INCLUDE,
-              *[os.path.join(HOST, s) for s in sources],
-              "-L", OUT, "-lk2g", "-Wl,-rpath,$ORIGIN", "-o", tmp])
-        os.replace(tmp, exe)
+    jobs = []
+    for exe, sources in _executables():
+        jobs.append([gxx, "-O2", "-std=c++17", "-Wall", "-pthread", "-I", INCLUDE,
+                     *[os.path.join(HOST, s) for s in sources],
+                     "-L", OUT, "-lk2g", "-Wl,-rpath,$ORIGIN", "-o", exe + ".tmp"])
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(_run, jobs))
+    for exe, _ in _executables():
+        os.replace(exe + ".tmp", exe)
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
@@ -87,8 +101,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     lib = os.path.join(OUT, "libk2g.so")
     deps = _deps()
-    if (not force and _newer(lib, deps + [__file__]) and _newer(classify_path(), deps + [lib])
-            and _newer(dump_table_path(), deps + [lib])):
+    if (not force and _newer(lib, deps + [__file__])
+            and all(_newer(exe, deps + [lib]) for exe, _ in _executables())):
         return lib
     if not force and _newer(lib, deps + [__file__]):
         _build_classify(lib)

@@ -74,6 +74,9 @@ def lib():
         L.ko_lca.argtypes = [U64P, C.c_uint64, C.c_uint64]
         L.ko_scan.restype = C.c_size_t
         L.ko_scan.argtypes = [C.POINTER(IndexOpts), C.c_char_p, C.c_size_t, U64P, U8P]
+        L.ko_scan_range.restype = C.c_size_t
+        L.ko_scan_range.argtypes = [C.POINTER(IndexOpts), C.c_char_p, C.c_size_t, C.c_size_t,
+                                    C.c_size_t, U64P, U8P]
         L.ko_classify_many.restype = None
         L.ko_classify_many.argtypes = [C.POINTER(Ctx), C.c_char_p, C.c_char_p, U64P,
                                        C.c_uint64, C.c_int, U64P, I64P, U32P, C.c_void_p]
@@ -98,6 +101,15 @@ def murmur3(key: int) -> int:
 def index_opts(k, l, mask, toggle, revcom=1, min_hash=0):
     return IndexOpts(k, l, mask, toggle & ((1 << (2 * l)) - 1) if l < 32 else toggle,
                      revcom, min_hash)
+
+
+def scan_range(opts: IndexOpts, seq: bytes, start: int, finish: int):
+    """NextMinimizer / is_ambiguous after LoadSequence(seq, start, finish)."""
+    n = max(min(finish, len(seq)) - start, 1)
+    mins = np.zeros(n, np.uint64)
+    amb = np.zeros(n, np.uint8)
+    m = lib().ko_scan_range(C.byref(opts), seq, len(seq), start, finish, mins, amb)
+    return mins[:m], amb[:m]
 
 
 def scan(opts: IndexOpts, seq: bytes):

@@ -215,18 +215,26 @@ static void scanner_init(ko_scanner *s, const ko_index_opts *o) {
   s->revcom_version = o->revcom_version;
 }
 
-/* LoadSequence -- mmscanner.cc:98-112. */
-static void scanner_load(ko_scanner *s, const char *str, size_t len) {
+/* LoadSequence -- mmscanner.cc:98-112, over [start, finish) of str (len
+ * bytes).  NextMinimizer's "a k-mer has been read" test compares the
+ * absolute position with k (mmscanner.cc:185), so an interval that starts
+ * past 0 reports the minimizer of its first k - l l-mers as unambiguous. */
+static void scanner_load_range(ko_scanner *s, const char *str, size_t len, size_t start,
+                               size_t finish) {
   s->str = str;
-  s->start = 0;
-  s->finish = len;
-  s->pos = 0;
+  s->start = start;
+  s->finish = finish > len ? len : finish;
+  s->pos = start;
   if ((long)(s->finish - s->start) + 1 < s->l) s->pos = s->finish;
   s->qh = s->qn = 0;
   s->queue_pos = 0;
   s->loaded = 0;
   s->last_min = ~0ULL;
   s->last_ambig = 0;
+}
+
+static void scanner_load(ko_scanner *s, const char *str, size_t len) {
+  scanner_load_range(s, str, len, 0, len);
 }
 
 /* is_ambiguous -- mmscanner.h:47-49. */
@@ -303,6 +311,23 @@ size_t ko_scan(const ko_index_opts *o, const char *seq, size_t len,
   ko_scanner *s = (ko_scanner *)malloc(sizeof(ko_scanner));
   scanner_init(s, o);
   scanner_load(s, seq, len);
+  size_t n = 0;
+  uint64_t m;
+  int a;
+  while (scanner_next(s, &m, &a)) {
+    mins[n] = m;
+    ambig[n] = (uint8_t)a;
+    n++;
+  }
+  free(s);
+  return n;
+}
+
+size_t ko_scan_range(const ko_index_opts *o, const char *seq, size_t len, size_t start,
+                     size_t finish, uint64_t *mins, uint8_t *ambig) {
+  ko_scanner *s = (ko_scanner *)malloc(sizeof(ko_scanner));
+  scanner_init(s, o);
+  scanner_load_range(s, seq, len, start, finish);
   size_t n = 0;
   uint64_t m;
   int a;

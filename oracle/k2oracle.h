@@ -59,6 +59,10 @@ typedef struct {
  * returns the number of pairs (len-k+1, or 0). */
 size_t ko_scan(const ko_index_opts *o, const char *seq, size_t len,
                uint64_t *mins, uint8_t *ambig);
+/* The same over [start, finish) (MinimizerScanner::LoadSequence with an
+ * interval, as the build's subblocks use it). */
+size_t ko_scan_range(const ko_index_opts *o, const char *seq, size_t len, size_t start,
+                     size_t finish, uint64_t *mins, uint8_t *ambig);
 
 /* ---- classification of one fragment (src/classify.cc:710-991) */
 typedef struct {
