@@ -336,6 +336,18 @@ k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const uint64_t *se
                                const uint32_t *taxids, uint64_t n_seqs, uint64_t block_size,
                                uint64_t subblock_size, int ordered, uint64_t *n_keys);
 
+/* The capacity estimate's sample (src/estimate_capacity.cc:57-92,
+ * :180-203) for a batch of sequences in host memory: the distinct
+ * minimizers of every sequence's unambiguous k-mers (each sequence scanned
+ * whole) whose MurmurHash3 mod 1024 is below sample_below (-n, 1..1024),
+ * ascending, written to keys (host, keys_cap entries).  *n_keys receives
+ * their number; K2G_ERR_CAPACITY when it exceeds keys_cap (nothing
+ * written).  The table of `db` is not used, only its scanner options.  DNA
+ * only.  Synchronous. */
+k2g_status k2g_sample_minimizers(const k2g_db *db, const char *bases, const uint64_t *seq_off,
+                                 uint64_t n_seqs, uint32_t sample_below, uint64_t *keys,
+                                 uint64_t keys_cap, uint64_t *n_keys);
+
 #ifdef __cplusplus
 }
 #endif

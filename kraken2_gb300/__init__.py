@@ -38,6 +38,7 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_lookup",
            "k2g_lookup_host", "k2g_scan", "k2g_classify", "k2g_classify_host",
            "k2g_host_alloc", "k2g_host_free", "k2g_build_insert", "k2g_build_sequences",
+           "k2g_sample_minimizers",
            "k2g_sector_gather",
            "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
            "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
@@ -120,6 +121,7 @@ def lib():
             "k2g_host_free": [vp],
             "k2g_build_insert": [vp, vp, vp, u64, i32, vp],
             "k2g_build_sequences": [vp, vp, vp, vp, u64, u64, u64, i32, C.POINTER(u64)],
+            "k2g_sample_minimizers": [vp, vp, vp, u64, C.c_uint32, vp, u64, C.POINTER(u64)],
             "k2g_sector_gather": [vp, u64, vp, vp],
             "k2g_classify_static": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams),
                                     C.POINTER(Results), vp],

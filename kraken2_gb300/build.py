@@ -32,6 +32,7 @@ CC_SOURCES = ["db.cc"]
 HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "block_reader.cc", "report.cc"]
 DUMP_SOURCES = ["dump_table_main.cc", "report.cc"]
 BUILD_DB_SOURCES = ["build_db_main.cc", "ncbi_taxonomy.cc", "seq_reader.cc", "block_reader.cc"]
+ESTIMATE_SOURCES = ["estimate_capacity_main.cc", "seq_reader.cc", "block_reader.cc"]
 
 
 def nvcc() -> str:
@@ -76,9 +77,13 @@ def build_db_path() -> str:
     return os.path.join(OUT, "build_db")
 
 
+def estimate_capacity_path() -> str:
+    return os.path.join(OUT, "estimate_capacity")
+
+
 def _executables():
     return ((classify_path(), HOST_SOURCES), (dump_table_path(), DUMP_SOURCES),
-            (build_db_path(), BUILD_DB_SOURCES))
+            (build_db_path(), BUILD_DB_SOURCES), (estimate_capacity_path(), ESTIMATE_SOURCES))
 
 
 def _build_classify(lib: str):

@@ -60,9 +60,18 @@ struct Chunk {
 // the previous k-mer of its block) or at its first k-mer.  A subblock start
 // at i scans bases i .. i + k - 2 only: its window then holds the k - l
 // l-mers the reference's subblock scanner reports first.
+// Which minimizers a chunk keeps: those whose hash is not below the table's
+// subsampling threshold (a build), or whose hash mod 1024 is below
+// sample_below (a capacity estimate, src/estimate_capacity.cc:192-201).
+__device__ __forceinline__ bool keep(const ScanView &sv, uint32_t sample_below, uint64_t m) {
+  if (sample_below) return (murmur3(m) & 1023u) < sample_below;
+  return !sv.min_hash || murmur3(m) >= sv.min_hash;
+}
+
 template <int W>
 __global__ void chunk_kernel(ScanView sv, const uint8_t *bases, const Chunk *chunks,
-                             uint64_t n_chunks, uint64_t *cand, uint32_t *counts) {
+                             uint64_t n_chunks, uint64_t *cand, uint32_t *counts,
+                             uint32_t sample_below) {
   const uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (c >= n_chunks) return;
   const Chunk ch = chunks[c];
@@ -103,14 +112,13 @@ __global__ void chunk_kernel(ScanView sv, const uint8_t *bases, const Chunk *chu
     const bool amb = (int32_t)p - last_amb <= amb_span;
     const uint64_t m = win.min(sv.w) ^ sv.toggle;
     const bool own = start + p - (k - 1) >= ch.pos;   // not the previous block k-mer
-    if (own && !amb && !(prev_ok && prev_min == m) && (!sv.min_hash || murmur3(m) >= sv.min_hash))
-      out[cnt++] = m;
+    if (own && !amb && !(prev_ok && prev_min == m) && keep(sv, sample_below, m)) out[cnt++] = m;
     prev_ok = !amb;
     prev_min = m;
   }
   if (sub && last_amb < 0) {   // bases i .. i + k - 2 all A/C/G/T
     const uint64_t m = win.min(sv.w) ^ sv.toggle;
-    if (!sv.min_hash || murmur3(m) >= sv.min_hash) out[cnt++] = m;
+    if (keep(sv, sample_below, m)) out[cnt++] = m;
   }
   counts[c] = cnt;
 }
@@ -264,9 +272,22 @@ __global__ void unique_kernel(const uint64_t *keys, const uint32_t *blocks, uint
 
 template <int W>
 void launch_chunks(const ScanView &sv, const uint8_t *bases, const Chunk *chunks, uint64_t n,
-                   uint64_t *cand, uint32_t *counts, cudaStream_t st) {
-  chunk_kernel<W><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(sv, bases, chunks, n, cand, counts);
+                   uint64_t *cand, uint32_t *counts, uint32_t sample_below, cudaStream_t st) {
+  chunk_kernel<W><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(sv, bases, chunks, n, cand, counts,
+                                                                sample_below);
   note_launches();
+}
+
+// Keys-only: the first of each run of equal keys, and the compaction.
+__global__ void key_first_kernel(const uint64_t *keys, uint64_t n, uint32_t *flag) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void key_unique_kernel(const uint64_t *keys, uint64_t n, const uint32_t *pos,
+                                  uint64_t *out) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n && (i == 0 || keys[i] != keys[i - 1])) out[pos[i]] = keys[i];
 }
 
 // Device buffers of one call, freed together.
@@ -284,6 +305,93 @@ struct Scratch {
   }
 };
 
+struct StreamGuard {
+  cudaStream_t s = nullptr;
+  ~StreamGuard() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+// A batch's candidates, compacted on the device.
+struct Gathered {
+  uint64_t *keys = nullptr;      // n candidate minimizers
+  uint32_t *blocks = nullptr;    // the block of each
+  uint64_t n = 0;
+  std::vector<uint32_t> block_taxon;
+};
+
+// Chunks of every block of every sequence that has a taxon (taxids null:
+// every sequence) and a k-mer -- the block's k-mer starts and, for a build,
+// its subblock starts i >= 1 whose first k - 1 bases lie inside the block
+// (src/build_db.h:224-250) -- scanned, counted and compacted.
+k2g_status gather(const k2g_db *db, const char *bases, const uint64_t *seq_off,
+                  const uint32_t *taxids, uint64_t n_seqs, uint64_t block_size,
+                  uint64_t subblock_size, uint32_t sample_below, Scratch &s, cudaStream_t st,
+                  Gathered &g) {
+  const ScanView sv = db->scan_view();
+  const uint64_t k = (uint64_t)sv.k;
+  const uint64_t base0 = seq_off[0], total = seq_off[n_seqs] - base0;
+  std::vector<Chunk> chunks;
+  uint64_t extra_slot = total;
+  for (uint64_t i = 0; i < n_seqs; i++) {
+    const uint64_t len = seq_off[i + 1] - seq_off[i];
+    if ((taxids && !taxids[i]) || len < k) continue;
+    const uint64_t nk = len - k + 1, s0 = seq_off[i] - base0;
+    for (uint64_t j = 0; j < len; j += block_size) {
+      const uint64_t be = std::min(nk, j + block_size);
+      const uint64_t finish = std::min(j + block_size + k - 1, len);
+      const uint32_t blk = (uint32_t)g.block_taxon.size();
+      const size_t before = chunks.size();
+      for (uint64_t c = j; c < be; c += kChunk)
+        chunks.push_back(Chunk{s0 + c, s0 + c, (uint32_t)std::min<uint64_t>(kChunk, be - c), blk,
+                               c == j ? kOpensBlock : kContinues, 0u});
+      if (sv.k > sv.l)
+        for (uint64_t sb = j; sb < finish; sb += subblock_size)
+          if (sb >= 1 && sb + k - 1 <= finish)
+            chunks.push_back(Chunk{s0 + sb, extra_slot++, 1u, blk, kSubblockStart, 0u});
+      if (chunks.size() > before) g.block_taxon.push_back(taxids ? taxids[i] : 1u);
+      if (block_size > len) break;
+    }
+  }
+  if (chunks.empty()) return K2G_OK;
+  if (extra_slot >= (1ull << 32)) return fail(K2G_ERR_ARG, "a batch holds fewer than 2^32 bases");
+  const uint64_t nc = chunks.size();
+  uint8_t *d_bases;
+  Chunk *d_chunks;
+  uint64_t *d_cand;
+  uint32_t *d_counts, *d_offs, *d_sums;
+  K2G_CUDA_TRY(s.get(&d_bases, total + 8));
+  K2G_CUDA_TRY(s.get(&d_chunks, nc));
+  K2G_CUDA_TRY(s.get(&d_cand, extra_slot));
+  K2G_CUDA_TRY(s.get(&d_counts, nc));
+  K2G_CUDA_TRY(s.get(&d_offs, nc));
+  K2G_CUDA_TRY(s.get(&d_sums, nc / rsort::kScanChunk + 2));
+  K2G_CUDA_TRY(cudaMemcpyAsync(d_bases, bases + base0, total, cudaMemcpyHostToDevice, st));
+  K2G_CUDA_TRY(cudaMemcpyAsync(d_chunks, chunks.data(), nc * sizeof(Chunk), cudaMemcpyHostToDevice, st));
+  switch (sv.w) {
+    case 1: launch_chunks<1>(sv, d_bases, d_chunks, nc, d_cand, d_counts, sample_below, st); break;
+    case 5: launch_chunks<5>(sv, d_bases, d_chunks, nc, d_cand, d_counts, sample_below, st); break;
+    case 7: launch_chunks<7>(sv, d_bases, d_chunks, nc, d_cand, d_counts, sample_below, st); break;
+    default: launch_chunks<0>(sv, d_bases, d_chunks, nc, d_cand, d_counts, sample_below, st); break;
+  }
+  K2G_CUDA_TRY(cudaGetLastError());
+  K2G_CUDA_TRY(cudaMemcpyAsync(d_offs, d_counts, nc * 4, cudaMemcpyDeviceToDevice, st));
+  K2G_CUDA_TRY(rsort::exclusive_scan(d_offs, nc, d_sums, st));
+  uint32_t last[2] = {0, 0};
+  K2G_CUDA_TRY(cudaMemcpyAsync(&last[0], d_offs + nc - 1, 4, cudaMemcpyDeviceToHost, st));
+  K2G_CUDA_TRY(cudaMemcpyAsync(&last[1], d_counts + nc - 1, 4, cudaMemcpyDeviceToHost, st));
+  K2G_CUDA_TRY(cudaStreamSynchronize(st));
+  g.n = (uint64_t)last[0] + last[1];
+  if (!g.n) return K2G_OK;
+  K2G_CUDA_TRY(s.get(&g.keys, g.n));
+  K2G_CUDA_TRY(s.get(&g.blocks, g.n));
+  compact_kernel<<<(unsigned)((nc * 32 + 255) / 256), 256, 0, st>>>(d_chunks, nc, d_cand, d_counts,
+                                                                       d_offs, g.keys, g.blocks);
+  note_launches();
+  K2G_CUDA_TRY(cudaGetLastError());
+  return K2G_OK;
+}
+
 }  // namespace
 }  // namespace k2g
 
@@ -299,99 +407,34 @@ extern "C" k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const u
   if (!db->opts.dna_db) return fail(K2G_ERR_ARG, "protein databases are not supported");
   if (!n_seqs) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
-  const ScanView sv = db->scan_view();
-  const uint64_t k = (uint64_t)sv.k;
-  const uint64_t base0 = seq_off[0], total = seq_off[n_seqs] - base0;
-
-  // chunks of every block of every sequence that has a taxon and a k-mer:
-  // the block's k-mer starts, and its subblock starts i >= 1 whose first
-  // k - 1 bases lie inside the block (src/build_db.h:224-250)
-  std::vector<Chunk> chunks;
-  std::vector<uint32_t> block_taxon;
-  uint64_t extra_slot = total;
-  for (uint64_t i = 0; i < n_seqs; i++) {
-    const uint64_t len = seq_off[i + 1] - seq_off[i];
-    if (!taxids[i] || len < k) continue;
-    const uint64_t nk = len - k + 1, s0 = seq_off[i] - base0;
-    for (uint64_t j = 0; j < len; j += block_size) {
-      const uint64_t be = std::min(nk, j + block_size);
-      const uint64_t finish = std::min(j + block_size + k - 1, len);
-      const uint32_t blk = (uint32_t)block_taxon.size();
-      const size_t before = chunks.size();
-      for (uint64_t c = j; c < be; c += kChunk)
-        chunks.push_back(Chunk{s0 + c, s0 + c, (uint32_t)std::min<uint64_t>(kChunk, be - c), blk,
-                               c == j ? kOpensBlock : kContinues, 0u});
-      if (sv.k > sv.l)
-        for (uint64_t s = j; s < finish; s += subblock_size)
-          if (s >= 1 && s + k - 1 <= finish)
-            chunks.push_back(Chunk{s0 + s, extra_slot++, 1u, blk, kSubblockStart, 0u});
-      if (chunks.size() > before) block_taxon.push_back(taxids[i]);
-    }
-  }
-  if (chunks.empty()) return K2G_OK;
-  if (extra_slot >= (1ull << 32)) return fail(K2G_ERR_ARG, "a batch holds fewer than 2^32 bases");
-  const uint64_t nc = chunks.size(), nb = block_taxon.size();
-  cudaStream_t st = nullptr;
-  K2G_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  struct StreamGuard {
-    cudaStream_t s;
-    ~StreamGuard() { cudaStreamDestroy(s); }
-  } guard{st};
+  StreamGuard guard;
+  K2G_CUDA_TRY(cudaStreamCreateWithFlags(&guard.s, cudaStreamNonBlocking));
+  cudaStream_t st = guard.s;
   Scratch s;
-  uint8_t *d_bases;
-  Chunk *d_chunks;
-  uint64_t *d_cand;
-  uint32_t *d_counts, *d_offs, *d_sums, *d_btax;
-  K2G_CUDA_TRY(s.get(&d_bases, total + 8));
-  K2G_CUDA_TRY(s.get(&d_chunks, nc));
-  K2G_CUDA_TRY(s.get(&d_cand, extra_slot));
-  K2G_CUDA_TRY(s.get(&d_counts, nc));
-  K2G_CUDA_TRY(s.get(&d_offs, nc));
-  K2G_CUDA_TRY(s.get(&d_sums, nc / rsort::kScanChunk + 2));
-  K2G_CUDA_TRY(s.get(&d_btax, nb));
-  K2G_CUDA_TRY(cudaMemcpyAsync(d_bases, bases + base0, total, cudaMemcpyHostToDevice, st));
-  K2G_CUDA_TRY(cudaMemcpyAsync(d_chunks, chunks.data(), nc * sizeof(Chunk), cudaMemcpyHostToDevice, st));
-  K2G_CUDA_TRY(cudaMemcpyAsync(d_btax, block_taxon.data(), nb * 4, cudaMemcpyHostToDevice, st));
+  Gathered g;
+  k2g_status r = gather(db, bases, seq_off, taxids, n_seqs, block_size, subblock_size, 0, s, st, g);
+  if (r != K2G_OK || !g.n) return r;
+  const uint64_t n = g.n, nb = g.block_taxon.size();
+  const int l = db->scan_view().l;
 
-  switch (sv.w) {
-    case 1: launch_chunks<1>(sv, d_bases, d_chunks, nc, d_cand, d_counts, st); break;
-    case 5: launch_chunks<5>(sv, d_bases, d_chunks, nc, d_cand, d_counts, st); break;
-    case 7: launch_chunks<7>(sv, d_bases, d_chunks, nc, d_cand, d_counts, st); break;
-    default: launch_chunks<0>(sv, d_bases, d_chunks, nc, d_cand, d_counts, st); break;
-  }
-  K2G_CUDA_TRY(cudaGetLastError());
-  // candidate offsets and their number
-  K2G_CUDA_TRY(cudaMemcpyAsync(d_offs, d_counts, nc * 4, cudaMemcpyDeviceToDevice, st));
-  K2G_CUDA_TRY(rsort::exclusive_scan(d_offs, nc, d_sums, st));
-  uint32_t last[2] = {0, 0};
-  K2G_CUDA_TRY(cudaMemcpyAsync(&last[0], d_offs + nc - 1, 4, cudaMemcpyDeviceToHost, st));
-  K2G_CUDA_TRY(cudaMemcpyAsync(&last[1], d_counts + nc - 1, 4, cudaMemcpyDeviceToHost, st));
-  K2G_CUDA_TRY(cudaStreamSynchronize(st));
-  const uint64_t n = (uint64_t)last[0] + last[1];
-  if (!n) return K2G_OK;
-
-  uint64_t *d_k0, *d_k1;
-  uint32_t *d_v0, *d_v1, *d_hist, *d_hsums;
+  uint64_t *d_k1;
+  uint32_t *d_v1, *d_hist, *d_hsums, *d_btax;
   const uint32_t ntiles = (uint32_t)((n + kPTile - 1) / kPTile);
   const uint64_t hist_n = 256ull * ntiles;
-  K2G_CUDA_TRY(s.get(&d_k0, n));
   K2G_CUDA_TRY(s.get(&d_k1, n));
-  K2G_CUDA_TRY(s.get(&d_v0, n));
   K2G_CUDA_TRY(s.get(&d_v1, n));
   K2G_CUDA_TRY(s.get(&d_hist, hist_n));
   K2G_CUDA_TRY(s.get(&d_hsums, (hist_n + rsort::kScanChunk - 1) / rsort::kScanChunk + 1));
-  compact_kernel<<<(unsigned)((nc * 32 + 255) / 256), 256, 0, st>>>(d_chunks, nc, d_cand, d_counts,
-                                                                       d_offs, d_k0, d_v0);
-  note_launches();
-  K2G_CUDA_TRY(cudaGetLastError());
+  K2G_CUDA_TRY(s.get(&d_btax, nb));
+  K2G_CUDA_TRY(cudaMemcpyAsync(d_btax, g.block_taxon.data(), nb * 4, cudaMemcpyHostToDevice, st));
 
   // passes: minimizer bytes (2l bits), zone, block bytes
   std::vector<Digit> passes;
-  for (int sh = 0; sh < 2 * sv.l; sh += 8) passes.push_back(Digit{0, sh});
+  for (int sh = 0; sh < 2 * l; sh += 8) passes.push_back(Digit{0, sh});
   passes.push_back(Digit{1, 0});
   for (int sh = 0; sh < 32 && (nb - 1) >> sh; sh += 8) passes.push_back(Digit{2, sh});
-  uint64_t *ka = d_k0, *kb = d_k1;
-  uint32_t *va = d_v0, *vb = d_v1;
+  uint64_t *ka = g.keys, *kb = d_k1;
+  uint32_t *va = g.blocks, *vb = d_v1;
   for (const Digit &dg : passes) {
     pair_hist_kernel<<<ntiles, kPThreads, 0, st>>>(ka, va, n, dg, d_hist, ntiles);
     note_launches();
@@ -404,25 +447,75 @@ extern "C" k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const u
   }
 
   // unique (block, minimizer) pairs, in order, with their taxa
-  uint32_t *d_flag = reinterpret_cast<uint32_t *>(vb);   // the free value buffer
-  uint64_t *d_out_keys = kb;                               // the free key buffer
+  uint32_t *d_flag = vb;          // the free value buffer
+  uint64_t *d_out_keys = kb;      // the free key buffer
   uint32_t *d_out_taxa, *d_fsums;
   K2G_CUDA_TRY(s.get(&d_out_taxa, n));
   K2G_CUDA_TRY(s.get(&d_fsums, (n + rsort::kScanChunk - 1) / rsort::kScanChunk + 1));
-  const unsigned g = (unsigned)((n + 255) / 256);
-  first_kernel<<<g, 256, 0, st>>>(ka, va, n, d_flag);
+  const unsigned gr = (unsigned)((n + 255) / 256);
+  first_kernel<<<gr, 256, 0, st>>>(ka, va, n, d_flag);
   note_launches();
   uint32_t last_flag = 0, last_pos = 0;
   K2G_CUDA_TRY(cudaMemcpyAsync(&last_flag, d_flag + n - 1, 4, cudaMemcpyDeviceToHost, st));
   K2G_CUDA_TRY(rsort::exclusive_scan(d_flag, n, d_fsums, st));
   K2G_CUDA_TRY(cudaMemcpyAsync(&last_pos, d_flag + n - 1, 4, cudaMemcpyDeviceToHost, st));
-  unique_kernel<<<g, 256, 0, st>>>(ka, va, n, d_flag, d_btax, d_out_keys, d_out_taxa);
+  unique_kernel<<<gr, 256, 0, st>>>(ka, va, n, d_flag, d_btax, d_out_keys, d_out_taxa);
   note_launches();
   K2G_CUDA_TRY(cudaGetLastError());
   K2G_CUDA_TRY(cudaStreamSynchronize(st));
   const uint64_t n_unique = (uint64_t)last_pos + last_flag;
-  k2g_status r = k2g_build_insert(db, d_out_keys, d_out_taxa, n_unique, ordered, st);
+  r = k2g_build_insert(db, d_out_keys, d_out_taxa, n_unique, ordered, st);
   if (r != K2G_OK) return r;
   if (n_keys) *n_keys = n_unique;
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_sample_minimizers(const k2g_db *db, const char *bases,
+                                            const uint64_t *seq_off, uint64_t n_seqs,
+                                            uint32_t sample_below, uint64_t *keys, uint64_t keys_cap,
+                                            uint64_t *n_keys) {
+  if (!db || !n_keys || (n_seqs && (!bases || !seq_off))) return fail(K2G_ERR_ARG, "null argument");
+  *n_keys = 0;
+  if (sample_below < 1 || sample_below > 1024) return fail(K2G_ERR_ARG, "sample_below must be in [1, 1024]");
+  if (!db->opts.dna_db) return fail(K2G_ERR_ARG, "protein databases are not supported");
+  if (!n_seqs) return K2G_OK;
+  K2G_CUDA_TRY(cudaSetDevice(db->device));
+  StreamGuard guard;
+  K2G_CUDA_TRY(cudaStreamCreateWithFlags(&guard.s, cudaStreamNonBlocking));
+  cudaStream_t st = guard.s;
+  Scratch s;
+  Gathered g;
+  // whole sequences: one block, no subblocks (MinimizerScanner::LoadSequence(seq))
+  const uint64_t whole = UINT64_MAX / 4;
+  k2g_status r = gather(db, bases, seq_off, nullptr, n_seqs, whole, whole, sample_below, s, st, g);
+  if (r != K2G_OK || !g.n) return r;
+  const uint64_t n = g.n;
+  uint64_t *d_alt, *sorted = nullptr;
+  uint32_t *d_hist, *d_hsums, *d_flag, *d_fsums;
+  K2G_CUDA_TRY(s.get(&d_alt, n));
+  K2G_CUDA_TRY(s.get(&d_hist, rsort::hist_entries(n)));
+  K2G_CUDA_TRY(s.get(&d_hsums, rsort::sum_entries(n) + 1));
+  K2G_CUDA_TRY(rsort::sort_u64(g.keys, d_alt, n, 2 * db->scan_view().l, d_hist, d_hsums, st, &sorted));
+  uint64_t *d_out = sorted == g.keys ? d_alt : g.keys;
+  K2G_CUDA_TRY(s.get(&d_flag, n));
+  K2G_CUDA_TRY(s.get(&d_fsums, (n + rsort::kScanChunk - 1) / rsort::kScanChunk + 1));
+  const unsigned gr = (unsigned)((n + 255) / 256);
+  key_first_kernel<<<gr, 256, 0, st>>>(sorted, n, d_flag);
+  note_launches();
+  uint32_t last_flag = 0, last_pos = 0;
+  K2G_CUDA_TRY(cudaMemcpyAsync(&last_flag, d_flag + n - 1, 4, cudaMemcpyDeviceToHost, st));
+  K2G_CUDA_TRY(rsort::exclusive_scan(d_flag, n, d_fsums, st));
+  K2G_CUDA_TRY(cudaMemcpyAsync(&last_pos, d_flag + n - 1, 4, cudaMemcpyDeviceToHost, st));
+  key_unique_kernel<<<gr, 256, 0, st>>>(sorted, n, d_flag, d_out);
+  note_launches();
+  K2G_CUDA_TRY(cudaGetLastError());
+  K2G_CUDA_TRY(cudaStreamSynchronize(st));
+  const uint64_t n_unique = (uint64_t)last_pos + last_flag;
+  *n_keys = n_unique;
+  if (n_unique > keys_cap) return fail(K2G_ERR_CAPACITY, "key buffer too small");
+  if (n_unique) {
+    if (!keys) return fail(K2G_ERR_ARG, "null argument");
+    K2G_CUDA_TRY(cudaMemcpy(keys, d_out, n_unique * 8, cudaMemcpyDeviceToHost));
+  }
   return K2G_OK;
 }

@@ -126,3 +126,29 @@ def build(library: bytes, id_map: dict, parent: np.ndarray, external_id: np.ndar
         raise RuntimeError("compact hash table capacity exceeded")
     return struct.pack("<QQQQ", capacity, size.value, 32 - value_bits, value_bits) + \
         table.astype("<u4").tobytes()
+
+
+def estimate_capacity(library: bytes, k: int, l: int, mask: int, toggle: int, n: int,
+                      threads: int) -> int:
+    """EstimateCapacity (src/estimate_capacity.cc:57-92, :180-203): `threads`
+    readers take records one at a time, each stopping at its first failed
+    read; every record's whole-sequence minimizers of unambiguous k-mers
+    whose MurmurHash3 mod 1024 is below n are counted once; the count plus
+    one is scaled by 1024 / n."""
+    from . import scan
+    opts = index_opts(k, l, mask, toggle, 1, 0)
+    seen = set()
+    failures = 0
+    for recs, ended in ks.block_attempts(library, count=1):
+        if ended:
+            break
+        if not recs:
+            failures += 1
+            if failures == threads:
+                break
+            continue
+        mins, amb = scan(opts, recs[0].seq)
+        m = mins[amb == 0]
+        m = m[(murmur3_np(m) & np.uint64(1023)) < np.uint64(n)]
+        seen.update(m.tolist())
+    return int((len(seen) + 1) * 1024 * 1.0 / n)

@@ -1,6 +1,6 @@
 #!/usr/bin/env python3
-"""Golden outputs of the reference's build_db (oracle/_ref/build_db, built by
-``make -C oracle ref``) for the build drop-in's tests.
+"""Golden outputs of the reference's build_db and estimate_capacity
+(oracle/_ref/, built by ``make -C oracle ref``) for the build drop-ins' tests.
 
 Run from the repository root:  python tests/golden/make_builds.py
 
@@ -8,7 +8,9 @@ For every build variant in VARIANTS the inputs are regenerated from seeds
 (``write_inputs``), the reference build_db runs with the variant's flags, and
 builds.json records its exit code, the end of its stderr, the sha256 of
 taxo.k2d and, when it succeeded, of hash.k2d and the opts.k2d fields; and the
-stderr/exit code of the usage-error cases.  The tests regenerate the
+stderr/exit code of the usage-error cases.  For every case in ESTIMATES it
+records the reference estimate_capacity's output, and the usage cases of
+that program too.  The tests regenerate the
 same inputs and compare digests, so no table is stored.
 """
 from __future__ import annotations
@@ -44,6 +46,22 @@ VARIANTS = {
     "edge": ("edge", 25, 21, 150_000, ["-B", "2048"]),
     "a_full": ("db_a", 35, 31, 30_000, ["-S", SEED_A]),
 }
+
+# name -> (input set, k, l, flags) for estimate_capacity
+ESTIMATES = {
+    "a_default": ("db_a", 35, 31, ["-S", SEED_A, "-p", "4"]),
+    "a_n64": ("db_a", 35, 31, ["-S", SEED_A, "-n", "64", "-p", "2"]),
+    "a_masks_all": ("db_a", 31, 25, ["-S", "1" * 10 + "0" + "1" * 14, "-T", "1011" * 16,
+                                     "-n", "1024"]),
+    "b": ("db_b", 25, 19, ["-n", "256"]),
+    "c_k_eq_l": ("db_c", 31, 31, ["-n", "128"]),
+    "edge": ("edge", 25, 21, ["-n", "512", "-p", "3"]),
+    "damaged_p1": ("damaged", 35, 31, ["-n", "1024", "-p", "1"]),
+    "damaged_p4": ("damaged", 35, 31, ["-n", "1024", "-p", "4"]),
+}
+
+ESTIMATE_USAGE = [["-h"], [], ["-k", "31"], ["-k", "20", "-l", "25"], ["-l", "32"],
+                  ["-k", "0"], ["-n", "0"], ["-n", "1025"], ["-p", "0"], ["-B", "0"]]
 
 # flags -> reference exit code and stderr, for the usage checks
 USAGE_CASES = [
@@ -83,6 +101,22 @@ def write_inputs(name: str, directory: str):
                                      n_genomes=s["genomes"], internal_frac=0.05)
         tax.write_dmp(tdir)
         synth.write_library(genomes, tax, lib, mp)
+        return tdir, lib, mp
+    if name == "damaged":
+        # db_a's library with records whose qualities are one short (each
+        # read fails and takes the next header line as qualities) and one
+        # too many (a clean failure), in a row and apart
+        write_inputs("db_a", directory)
+        with open(lib, "rb") as f:
+            data = f.read()
+        recs = data.split(b"\n>")
+        bad = b"@bad1\nACGTACGT\n+\nIIIIIIIII\n@bad2\nACGT\n+\nIIIII\n"
+        short = b"@bad3\nACGTACGT\n+\nIIII\n"
+        cut1, cut2 = len(recs) // 3, 2 * len(recs) // 3
+        out = b"\n>".join(recs[:cut1]) + b"\n" + bad + b">" + b"\n>".join(recs[cut1:cut2]) + \
+            b"\n" + short + b">" + b"\n>".join(recs[cut2:])
+        with open(lib, "wb") as f:
+            f.write(out)
         return tdir, lib, mp
     assert name == "edge"
     s = readsets.DB_SPECS["db_a"]
@@ -161,6 +195,12 @@ def build_args(exe, variant, directory):
     return args, lib, out
 
 
+def estimate_args(exe, name, directory):
+    inp, k, l, flags = ESTIMATES[name]
+    tdir, lib, mp = write_inputs(inp, os.path.join(directory, "in"))
+    return [exe, "-k", str(k), "-l", str(l), *flags], lib
+
+
 def sha(path):
     return hashlib.sha256(open(path, "rb").read()).hexdigest()
 
@@ -186,6 +226,19 @@ def main():
     for case in USAGE_CASES:
         r = subprocess.run([REF, *case], capture_output=True)
         out["usage"].append({"args": case, "rc": r.returncode, "stderr": r.stderr.decode()})
+    est = os.path.join(os.path.dirname(REF), "estimate_capacity")
+    out["estimates"], out["estimate_usage"] = {}, []
+    for v in ESTIMATES:
+        args, lib = estimate_args(est, v, os.path.join(work, "est_" + v))
+        with open(lib, "rb") as f:
+            r = subprocess.run(args, stdin=f, capture_output=True)
+        if r.returncode != 0:
+            sys.exit(f"estimate {v}: {r.stderr.decode()[-2000:]}")
+        out["estimates"][v] = int(r.stdout.decode().strip())
+    for case in ESTIMATE_USAGE:
+        r = subprocess.run([est, *case], capture_output=True)
+        out["estimate_usage"].append({"args": case, "rc": r.returncode,
+                                      "stderr": r.stderr.decode()})
     shutil.rmtree(work)
     with open(os.path.join(HERE, "builds.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)

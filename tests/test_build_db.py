@@ -181,3 +181,50 @@ def test_gather_model_equals_subblock_scans(k, l, B, b):
             if i >= 1 and i + k - 1 <= finish and clean[i:i + k - 1].all():
                 model.add(int(((lm[i:i + k - l] ^ tg).min()) ^ tg))
         assert model == literal, (j, len(model ^ literal))
+
+
+def _strtol2(s: str) -> int:
+    """strtol(s, nullptr, 2): a value above LONG_MAX clamps to it."""
+    return min(int(s, 2), (1 << 63) - 1)
+
+
+def estimate_exe():
+    k2g.lib()
+    p = k2build.estimate_capacity_path()
+    assert os.path.exists(p)
+    return p
+
+
+@pytest.mark.parametrize("case", BUILDS["estimate_usage"],
+                         ids=[" ".join(c["args"]) or "none" for c in BUILDS["estimate_usage"]])
+def test_estimate_usage_matches_reference(case):
+    r = subprocess.run([estimate_exe(), *case["args"]], capture_output=True)
+    assert r.returncode == case["rc"]
+    assert r.stderr.decode() == case["stderr"]
+
+
+ESTIMATES = sorted(BUILDS["estimates"].items())
+
+
+@pytest.mark.parametrize("name,want", ESTIMATES, ids=[v for v, _ in ESTIMATES])
+def test_oracle_estimate_matches_reference(name, want, tmp_path):
+    from oracle import build_db as ob
+    inp, k, l, flags = make_builds.ESTIMATES[name]
+    f = dict(zip(flags[::2], flags[1::2]))
+    _, lib, _ = make_builds.write_inputs(inp, str(tmp_path / "in"))
+    mask = _expand(_strtol2(f["-S"])) if "-S" in f else 0
+    toggle = _strtol2(f["-T"]) if "-T" in f else 0xe37e28c4271b5a2d
+    with open(lib, "rb") as fh:
+        got = ob.estimate_capacity(fh.read(), k, l, mask, toggle, int(f.get("-n", 4)),
+                                   int(f.get("-p", 1)))
+    assert got == want
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,want", ESTIMATES, ids=[v for v, _ in ESTIMATES])
+def test_estimate_matches_reference(name, want, tmp_path):
+    args, lib = make_builds.estimate_args(estimate_exe(), name, str(tmp_path / name))
+    with open(lib, "rb") as f:
+        r = subprocess.run(args, stdin=f, capture_output=True)
+    assert r.returncode == 0, r.stderr.decode()[-2000:]
+    assert int(r.stdout.decode().strip()) == want
