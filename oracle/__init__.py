@@ -24,7 +24,7 @@ U8P = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 class IndexOpts(C.Structure):
     _fields_ = [("k", C.c_int), ("l", C.c_int), ("spaced_seed_mask", C.c_uint64),
                 ("toggle_mask", C.c_uint64), ("revcom_version", C.c_int),
-                ("min_hash", C.c_uint64)]
+                ("min_hash", C.c_uint64), ("protein", C.c_int)]
 
 
 class Ctx(C.Structure):
@@ -74,6 +74,9 @@ def lib():
         L.ko_lca.argtypes = [U64P, C.c_uint64, C.c_uint64]
         L.ko_scan.restype = C.c_size_t
         L.ko_scan.argtypes = [C.POINTER(IndexOpts), C.c_char_p, C.c_size_t, U64P, U8P]
+        L.ko_translate.restype = None
+        L.ko_translate.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t,
+                                   C.POINTER(C.c_size_t)]
         L.ko_scan_range.restype = C.c_size_t
         L.ko_scan_range.argtypes = [C.POINTER(IndexOpts), C.c_char_p, C.c_size_t, C.c_size_t,
                                     C.c_size_t, U64P, U8P]
@@ -98,9 +101,20 @@ def murmur3(key: int) -> int:
     return lib().ko_murmur3(key)
 
 
-def index_opts(k, l, mask, toggle, revcom=1, min_hash=0):
-    return IndexOpts(k, l, mask, toggle & ((1 << (2 * l)) - 1) if l < 32 else toggle,
-                     revcom, min_hash)
+def index_opts(k, l, mask, toggle, revcom=1, min_hash=0, protein=False):
+    bits = (4 if protein else 2) * l
+    return IndexOpts(k, l, mask, toggle & ((1 << bits) - 1) if bits < 64 else toggle,
+                     revcom, min_hash, int(protein))
+
+
+def translate(dna: bytes) -> list:
+    """The six frames of TranslateToAllFrames (ko_translate)."""
+    cap = len(dna) // 3 + 1
+    out = C.create_string_buffer(6 * cap)
+    lens = (C.c_size_t * 6)()
+    lib().ko_translate(dna, len(dna), out, cap, lens)
+    raw = out.raw
+    return [raw[f * cap:f * cap + lens[f]] for f in range(6)]
 
 
 def scan_range(opts: IndexOpts, seq: bytes, start: int, finish: int):
@@ -151,11 +165,13 @@ class Oracle:
         calls = np.zeros(n_frags, np.uint64)
         hg = np.zeros(n_frags, np.int64)
         nr = np.zeros(n_frags, np.uint32)
-        runs = np.zeros(int(seq_off[-1]) + 2 * n_frags + 2, RUN_DTYPE)
+        mul, add = (2, 32) if self.opts.protein else (1, 2)   # ko_run_base
+        runs = np.zeros(mul * int(seq_off[-1]) + add * n_frags + 2, RUN_DTYPE)
         lib().ko_classify_many(C.byref(c), bases, quals, seq_off, n_frags, threads, calls, hg,
                                nr, runs.ctypes.data)
         per = 2 if params.get("paired") else 1
-        base = seq_off[0:n_frags * per:per] + 2 * np.arange(n_frags, dtype=np.uint64)
+        base = np.uint64(mul) * seq_off[0:n_frags * per:per] + \
+            np.uint64(add) * np.arange(n_frags, dtype=np.uint64)
         return calls, hg, nr, runs, base
 
     def taxon_counters(self, bases, quals, seq_off, n_frags, blocks, kmer_data=True, **params):

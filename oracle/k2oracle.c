@@ -173,6 +173,7 @@ typedef struct {
   int k, l;
   uint64_t mask, toggle, lmer_mask;
   int revcom_version;
+  int protein, bits;        /* bits per character: 2 (DNA) or 4 (protein) */
   const char *str;
   size_t start, finish, pos;
   uint64_t lmer, last_min, last_ambig;
@@ -189,6 +190,30 @@ static inline uint8_t dna_code(unsigned char c) {
     case 'C': case 'c': return 1;
     case 'G': case 'g': return 2;
     case 'T': case 't': return 3;
+    default: return 0xFF;
+  }
+}
+
+/* The 15-group reduced amino-acid alphabet (mmscanner.cc:47-95), either
+ * case; B, Z, J, X and anything else are ambiguous. */
+static inline uint8_t aa_code(unsigned char c) {
+  switch (c >= 'a' && c <= 'z' ? c - 32 : c) {
+    case '*': case 'U': case 'O': return 0x0;
+    case 'A': return 0x1;
+    case 'N': case 'Q': case 'S': return 0x2;
+    case 'C': return 0x3;
+    case 'D': case 'E': return 0x4;
+    case 'F': return 0x5;
+    case 'G': return 0x6;
+    case 'H': return 0x7;
+    case 'I': case 'L': return 0x8;
+    case 'K': return 0x9;
+    case 'P': return 0xa;
+    case 'R': return 0xb;
+    case 'M': case 'V': return 0xc;
+    case 'T': return 0xd;
+    case 'W': return 0xe;
+    case 'Y': return 0xf;
     default: return 0xFF;
   }
 }
@@ -210,7 +235,9 @@ static void scanner_init(ko_scanner *s, const ko_index_opts *o) {
   s->k = o->k;
   s->l = o->l;
   s->mask = o->spaced_seed_mask;
-  s->lmer_mask = (1ULL << (o->l * 2)) - 1;
+  s->protein = o->protein;
+  s->bits = o->protein ? 4 : 2;
+  s->lmer_mask = (1ULL << (o->l * s->bits)) - 1;
   s->toggle = o->toggle_mask & s->lmer_mask;
   s->revcom_version = o->revcom_version;
 }
@@ -254,15 +281,16 @@ static int scanner_next(ko_scanner *s, uint64_t *mn, int *amb) {
     if (s->loaded == s->l) s->loaded--;
     while (s->loaded < s->l && s->pos < s->finish) {
       s->loaded++;
-      s->lmer <<= 2;
-      s->last_ambig <<= 2;
-      uint8_t code = dna_code((unsigned char)s->str[s->pos++]);
+      s->lmer <<= s->bits;
+      s->last_ambig <<= s->bits;
+      const unsigned char ch = (unsigned char)s->str[s->pos++];
+      uint8_t code = s->protein ? aa_code(ch) : dna_code(ch);
       if (code == 0xFF) {
         s->qh = s->qn = 0;
         s->queue_pos = 0;
         s->lmer = 0;
         s->loaded = 0;
-        s->last_ambig |= 3;
+        s->last_ambig |= (1u << s->bits) - 1;
       } else {
         s->lmer |= code;
       }
@@ -275,8 +303,11 @@ static int scanner_next(ko_scanner *s, uint64_t *mn, int *amb) {
       }
     }
     if (s->loaded < s->l) return 0;
-    uint64_t rc = revcomp(s->lmer, s->l, s->revcom_version);
-    uint64_t canon = s->lmer < rc ? s->lmer : rc;
+    uint64_t canon = s->lmer;   /* protein l-mers are not canonicalised */
+    if (!s->protein) {
+      uint64_t rc = revcomp(s->lmer, s->l, s->revcom_version);
+      canon = s->lmer < rc ? s->lmer : rc;
+    }
     if (s->mask) canon &= s->mask;
     uint64_t cand = canon ^ s->toggle;
     if (s->k == s->l) {
@@ -340,11 +371,62 @@ size_t ko_scan_range(const ko_index_opts *o, const char *seq, size_t len, size_t
   return n;
 }
 
+/* TranslateToAllFrames -- aa_translate.cc:41-100.  Codons are coded A=0,
+ * G=1, C=2, T=3 (the order of the translation string); a codon ending at
+ * base i goes to frame i mod 3 (forward) and, reverse-complemented, is
+ * prepended to frame 3 + i mod 3.  A non-ACGT base makes the three codons
+ * that hold it 'X'.  Sequences shorter than 3 give six frames of one space
+ * each, as the reference's untrimmed buffers. */
+void ko_translate(const char *dna, size_t len, char *out, size_t cap, size_t lens[6]) {
+  static const char map[] = "KKNNRRSSTTTTIMIIEEDDGGGGAAAAVVVVQQHHRRRRPPPPLLLL**YY*WCCSSSSLLFF";
+  const size_t max_size = len / 3 + 1;
+  for (int f = 0; f < 6; f++) lens[f] = 0;
+  if (len < 3) {
+    for (int f = 0; f < 6; f++) {
+      memset(out + f * cap, ' ', max_size);
+      lens[f] = max_size;
+    }
+    return;
+  }
+  unsigned fwd = 0, rev = 0;
+  int countdown = 0;
+  /* reverse frames are filled from the back of a max_size buffer, then
+   * moved to the front */
+  for (size_t i = 0; i < len; i++) {
+    const size_t frame = i % 3;
+    fwd = (fwd << 2) & 0x3f;
+    rev >>= 2;
+    if (countdown) countdown--;
+    unsigned fc = 0xFF, rc = 0;
+    switch (dna[i]) {
+      case 'A': case 'a': fc = 0; rc = 0x30; break;
+      case 'G': case 'g': fc = 1; rc = 0x20; break;
+      case 'C': case 'c': fc = 2; rc = 0x10; break;
+      case 'T': case 't': fc = 3; rc = 0x00; break;
+    }
+    if (fc == 0xFF) {
+      countdown = 3;
+    } else {
+      fwd |= fc;
+      rev |= rc;
+    }
+    if (i >= 2) {
+      out[frame * cap + lens[frame]++] = countdown == 0 ? map[fwd] : 'X';
+      char *r = out + (frame + 3) * cap;
+      r[max_size - 1 - lens[frame + 3]++] = countdown == 0 ? map[rev] : 'X';
+    }
+  }
+  for (int f = 3; f < 6; f++) {
+    char *r = out + f * cap;
+    memmove(r, r + max_size - lens[f], lens[f]);
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Classification of one fragment -- src/classify.cc:773-991                 */
 /* ------------------------------------------------------------------------ */
 
-enum { TOK_LOOKUP, TOK_SKIP, TOK_REPEAT, TOK_AMBIG, TOK_BORDER_MATE };
+enum { TOK_LOOKUP, TOK_SKIP, TOK_REPEAT, TOK_AMBIG, TOK_BORDER_MATE, TOK_BORDER_FRAME };
 
 /* Small open-addressing taxon->count map standing in for taxon_counts_t. */
 typedef struct { uint64_t *key; uint64_t *val; size_t cap, n; } cmap;
@@ -402,12 +484,13 @@ typedef struct {
   char *m1, *m2;
   uint64_t *mkey, *mval; size_t mcap;
   ko_scanner *sc;
+  char *frames; size_t fcap;   /* six translated frames of one mate */
 } ko_ws;
 
 static void ws_init(ko_ws *w) { memset(w, 0, sizeof(*w)); w->sc = (ko_scanner *)malloc(sizeof(ko_scanner)); }
 static void ws_free(ko_ws *w) {
   free(w->kind); free(w->kidx); free(w->keys); free(w->vals); free(w->taxa);
-  free(w->m1); free(w->m2); free(w->mkey); free(w->mval); free(w->sc);
+  free(w->m1); free(w->m2); free(w->mkey); free(w->mval); free(w->sc); free(w->frames);
 }
 static void ws_reserve(ko_ws *w, size_t n) {
   if (n <= w->cap) return;
@@ -433,7 +516,10 @@ static const char *mask_into(const char *seq, const char *qual, size_t len, int 
 static void classify_ws(const ko_ctx *c, const char *seq1, size_t len1, const char *qual1,
                         const char *seq2, size_t len2, const char *qual2, ko_frag_result *res,
                         ko_run *runs, ko_hit *hits, ko_ws *w) {
-  size_t maxtok = len1 + len2 + 2;
+  const int translated = c->idx.protein;
+  /* translated: six frames of at most len / 3 + 1 residues, five frame
+   * borders, per mate */
+  size_t maxtok = translated ? 2 * (len1 + len2) + 32 : len1 + len2 + 2;
   ws_reserve(w, maxtok);
   const char *s1 = mask_into(seq1, qual1, len1, c->min_quality, w->m1);
   const char *s2 = c->paired ? mask_into(seq2, qual2, len2, c->min_quality, w->m2) : NULL;
@@ -446,28 +532,45 @@ static void classify_ws(const ko_ctx *c, const char *seq1, size_t len1, const ch
   ko_scanner *sc = w->sc;
   scanner_init(sc, &c->idx);
 
-  /* Phase 1: token stream (classify.cc:797-838). */
+  /* Phase 1: token stream (classify.cc:797-838); with translated search
+   * each mate's six frames, separated by frame borders. */
   for (int mate = 0; mate < 2; mate++) {
     if (mate == 1 && !c->paired) break;
-    scanner_load(sc, mate == 0 ? s1 : s2, mate == 0 ? len1 : len2);
-    uint64_t last_minimizer = UINT64_MAX, m;
-    int amb;
-    while (scanner_next(sc, &m, &amb)) {
-      if (amb) {
-        kind[ntok++] = TOK_AMBIG;
-      } else if (m != last_minimizer) {
-        last_minimizer = m;
-        int skip = c->idx.min_hash && ko_murmur3(m) < c->idx.min_hash;
-        if (skip) {
-          kind[ntok++] = TOK_SKIP;
-        } else {
-          kind[ntok] = TOK_LOOKUP;
-          kidx[ntok++] = (uint32_t)nkeys;
-          keys[nkeys++] = m;
-        }
-      } else {
-        kind[ntok++] = TOK_REPEAT;
+    const char *ms = mate == 0 ? s1 : s2;
+    const size_t ml = mate == 0 ? len1 : len2;
+    size_t flen[6];
+    const size_t fcap = ml / 3 + 1;
+    if (translated) {
+      if (6 * fcap > w->fcap) {
+        w->fcap = 6 * fcap;
+        w->frames = (char *)realloc(w->frames, w->fcap);
       }
+      ko_translate(ms, ml, w->frames, fcap, flen);
+    }
+    const int frame_ct = translated ? 6 : 1;
+    for (int fi = 0; fi < frame_ct; fi++) {
+      if (translated) scanner_load(sc, w->frames + fi * fcap, flen[fi]);
+      else scanner_load(sc, ms, ml);
+      uint64_t last_minimizer = UINT64_MAX, m;
+      int amb;
+      while (scanner_next(sc, &m, &amb)) {
+        if (amb) {
+          kind[ntok++] = TOK_AMBIG;
+        } else if (m != last_minimizer) {
+          last_minimizer = m;
+          int skip = c->idx.min_hash && ko_murmur3(m) < c->idx.min_hash;
+          if (skip) {
+            kind[ntok++] = TOK_SKIP;
+          } else {
+            kind[ntok] = TOK_LOOKUP;
+            kidx[ntok++] = (uint32_t)nkeys;
+            keys[nkeys++] = m;
+          }
+        } else {
+          kind[ntok++] = TOK_REPEAT;
+        }
+      }
+      if (translated && fi != 5) kind[ntok++] = TOK_BORDER_FRAME;
     }
     if (c->paired && mate == 0) kind[ntok++] = TOK_BORDER_MATE;
   }
@@ -496,6 +599,7 @@ static void classify_ws(const ko_ctx *c, const char *seq1, size_t len1, const ch
     switch (kind[ti]) {
       case TOK_AMBIG: taxa[ntaxa++] = KO_AMBIGUOUS; continue;
       case TOK_BORDER_MATE: taxa[ntaxa++] = KO_MATE_BORDER; continue;
+      case TOK_BORDER_FRAME: taxa[ntaxa++] = KO_FRAME_BORDER; continue;
       case TOK_SKIP: taxon = 0; last_taxon = 0; break;
       case TOK_LOOKUP:
         taxon = vals[kidx[ti]];
@@ -517,6 +621,8 @@ static void classify_ws(const ko_ctx *c, const char *seq1, size_t len1, const ch
 finished:;
   uint64_t total_kmers = ntaxa;
   if (c->paired) total_kmers--;
+  /* the reference takes 2 (4 for pairs) for the five frame borders per mate */
+  if (translated) total_kmers -= c->paired ? 4 : 2;
   uint64_t call = resolve_tree(&hit_counts, c->parent, total_kmers, c->confidence);
   if (call && hit_groups < c->min_hit_groups) call = 0;
 
@@ -543,6 +649,13 @@ void ko_classify_fragment(const ko_ctx *c, const char *seq1, size_t len1,
   ws_free(&w);
 }
 
+/* Where fragment f's runs start in ko_classify_many's output: a fragment of
+ * n bases has at most n + 2 runs, or, translated (six frames and five frame
+ * borders per mate), at most 2n + 32. */
+uint64_t ko_run_base(const ko_ctx *c, uint64_t first_base, uint64_t f) {
+  return c->idx.protein ? 2 * first_base + 32 * f : first_base + 2 * f;
+}
+
 typedef struct {
   const ko_ctx *c; const char *bases, *quals; const uint64_t *seq_off;
   uint64_t lo, hi; uint64_t *calls; int64_t *hit_groups; uint32_t *n_runs;
@@ -562,7 +675,7 @@ static void *cm_thread(void *p) {
     classify_ws(j->c, j->bases + a, b - a, j->quals ? j->quals + a : NULL,
                 per == 2 ? j->bases + a2 : NULL, b2 - a2,
                 (per == 2 && j->quals) ? j->quals + a2 : NULL, &r,
-                j->runs + j->seq_off[f * per] + 2 * f, NULL, &w);
+                j->runs + ko_run_base(j->c, j->seq_off[f * per], f), NULL, &w);
     j->calls[f] = r.call;
     if (j->hit_groups) j->hit_groups[f] = r.hit_groups;
     j->n_runs[f] = (uint32_t)r.n_runs;
@@ -798,8 +911,9 @@ void ko_taxon_counters(const ko_ctx *c, const char *bases, const char *quals,
     uint64_t l = seq_off[(f + 1) * per] - seq_off[f * per];
     if (l > maxlen) maxlen = l;
   }
-  ko_run *runs = (ko_run *)malloc((maxlen + 4) * sizeof(ko_run));
-  ko_hit *hits = (ko_hit *)malloc((maxlen + 4) * sizeof(ko_hit));
+  /* a translated fragment has up to 2 * len + 32 taxa */
+  ko_run *runs = (ko_run *)malloc((2 * maxlen + 64) * sizeof(ko_run));
+  ko_hit *hits = (ko_hit *)malloc((2 * maxlen + 64) * sizeof(ko_hit));
   for (uint64_t f = 0; f < n_frags; f++) {
     uint64_t a = seq_off[f * per], b = seq_off[f * per + 1], a2 = 0, b2 = 0;
     if (per == 2) { a2 = seq_off[f * per + 1]; b2 = seq_off[f * per + 2]; }

@@ -53,7 +53,15 @@ typedef struct {
   uint64_t spaced_seed_mask, toggle_mask;
   int revcom_version;
   uint64_t min_hash;        /* IndexOptions::minimum_acceptable_hash_value */
+  int protein;              /* !IndexOptions::dna_db: 4-bit reduced alphabet,
+                               no reverse complement; classification then
+                               translates reads into six frames */
 } ko_index_opts;
+
+/* TranslateToAllFrames (src/aa_translate.cc:41-100): the six frames of
+ * dna[0,len), frame f at out + f * cap (cap >= len / 3 + 1); lens[f]
+ * receives each frame's length. */
+void ko_translate(const char *dna, size_t len, char *out, size_t cap, size_t lens[6]);
 
 /* Scans seq[0,len) and writes one (minimizer, ambiguous) pair per k-mer;
  * returns the number of pairs (len-k+1, or 0). */
@@ -98,6 +106,10 @@ void ko_classify_fragment(const ko_ctx *c, const char *seq1, size_t len1,
  * mate 1 and 2i+1 mate 2.  calls/hit_groups/n_runs are per fragment; runs are
  * written at run_off[i] = seq_off[first seq of i] + 2*i (caller allocates
  * total_bases + 2*n entries). */
+/* Index of fragment f's first run in ko_classify_many's `runs`, given the
+ * offset of its first base (n + 2 runs per fragment of n bases; 2n + 32
+ * translated). */
+uint64_t ko_run_base(const ko_ctx *c, uint64_t first_base, uint64_t f);
 void ko_classify_many(const ko_ctx *c, const char *bases, const char *quals,
                       const uint64_t *seq_off, uint64_t n_frags, int threads,
                       uint64_t *calls, int64_t *hit_groups, uint32_t *n_runs,

@@ -13,6 +13,12 @@
 //   ref_probe hll                           < commands
 //       "n I" new sketch I, "i I KEY" insert, "m I J" merge J into I (const&),
 //       "e I" prints ertlCardinality (src/hyperloglogplus.cc) of sketch I
+//   ref_probe translate                     < one DNA sequence per line
+//       prints TranslateToAllFrames (src/aa_translate.cc:41-100): the six
+//       frames, tab-separated
+//   ref_probe scanx K L MASK TOGGLE START FINISH PROTEIN < one sequence per line
+//       as scan, with a protein scanner when PROTEIN is 1 and
+//       LoadSequence(seq, START, FINISH) (FINISH 0: the whole sequence)
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
@@ -22,6 +28,7 @@
 
 #include "compact_hash.h"
 #include "hyperloglogplus.h"
+#include "aa_translate.h"
 #include "mmscanner.h"
 #include "taxonomy.h"
 
@@ -98,6 +105,40 @@ static int do_hll() {
   return 0;
 }
 
+static int do_translate() {
+  std::string line;
+  std::vector<std::string> frames(6);
+  while (std::getline(std::cin, line)) {
+    TranslateToAllFrames(line, frames);
+    for (int f = 0; f < 6; f++) printf("%s%s", f ? "\t" : "", frames[f].c_str());
+    printf("\n");
+  }
+  return 0;
+}
+
+static int do_scanx(int argc, char **argv) {
+  if (argc < 9) return 64;
+  long k = atol(argv[2]), l = atol(argv[3]);
+  uint64_t mask = strtoull(argv[4], nullptr, 0);
+  uint64_t toggle = strtoull(argv[5], nullptr, 0);
+  size_t start = strtoull(argv[6], nullptr, 0), finish = strtoull(argv[7], nullptr, 0);
+  bool protein = atoi(argv[8]) != 0;
+  MinimizerScanner scanner(k, l, mask, !protein, toggle);
+  std::string line;
+  while (std::getline(std::cin, line)) {
+    scanner.LoadSequence(line, start, finish ? finish : SIZE_MAX);
+    uint64_t *m;
+    bool first = true;
+    while ((m = scanner.NextMinimizer()) != nullptr) {
+      printf("%s%llu:%d", first ? "" : " ", (unsigned long long)*m,
+             scanner.is_ambiguous() ? 1 : 0);
+      first = false;
+    }
+    printf("\n");
+  }
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) return 64;
   std::string mode = argv[1];
@@ -105,5 +146,7 @@ int main(int argc, char **argv) {
   if (mode == "lookup") return do_lookup(argc, argv);
   if (mode == "insert") return do_insert(argc, argv);
   if (mode == "hll") return do_hll();
+  if (mode == "translate") return do_translate();
+  if (mode == "scanx") return do_scanx(argc, argv);
   return 64;
 }

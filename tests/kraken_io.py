@@ -23,6 +23,7 @@ import synth  # noqa: E402
 from kraken2_gb300 import formats  # noqa: E402
 
 MATE_BORDER = 0xFFFFFFFFFFFFFFFF
+FRAME_BORDER = 0xFFFFFFFFFFFFFFFE
 AMBIGUOUS = 0xFFFFFFFFFFFFFFFD
 SE_BLOCK_BYTES = 3 * 1024 * 1024      # src/classify.cc:527
 PE_BLOCK_FRAGS = 10000                # src/classify.cc:32
@@ -218,6 +219,8 @@ def hitlist(runs, ext_id) -> str:
         code = int(code)
         if code == MATE_BORDER:
             parts.append("|:|" if i == last else "|:| ")
+        elif code == FRAME_BORDER:
+            parts.append("-:-" if i == last else "-:- ")
         elif code == AMBIGUOUS:
             parts.append(f"A:{cnt} ")
         else:
