@@ -79,7 +79,9 @@ const char *k2g_last_error(void);
 const char *k2g_version(void);
 
 /* Loads the three database files and uploads the table and the taxonomy's
- * parent array.  Replaces load_index (src/classify.cc:269-302): the opts
+ * parent array.  Protein (translated search) tables load -- lookups, value
+ * counts and builds serve them -- but the classify entry points refuse them
+ * with K2G_ERR_UNSUPPORTED.  Replaces load_index (src/classify.cc:269-302): the opts
  * file read (:272-279), Taxonomy::Init (src/taxonomy.cc:195-238) and
  * CompactHashTable::LoadTable (src/compact_hash.h:279-341). */
 k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
@@ -331,7 +333,9 @@ k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *
  * table is the one the reference's build leaves after the same sequences
  * (ordered == 0: the fast unordered insert, -F).  Batches must hold fewer
  * than 2^32 bases; *n_keys (may be NULL) receives the number of (block,
- * minimizer) pairs inserted.  DNA tables only.  Synchronous. */
+ * minimizer) pairs inserted.  A protein table (dna_db 0) scans the
+ * sequences as amino acids (the 15-group reduced alphabet, no reverse
+ * complement), as build_db -X does.  Synchronous. */
 k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const uint64_t *seq_off,
                                const uint32_t *taxids, uint64_t n_seqs, uint64_t block_size,
                                uint64_t subblock_size, int ordered, uint64_t *n_keys);
@@ -342,8 +346,8 @@ k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const uint64_t *se
  * whole) whose MurmurHash3 mod 1024 is below sample_below (-n, 1..1024),
  * ascending, written to keys (host, keys_cap entries).  *n_keys receives
  * their number; K2G_ERR_CAPACITY when it exceeds keys_cap (nothing
- * written).  The table of `db` is not used, only its scanner options.  DNA
- * only.  Synchronous. */
+ * written).  The table of `db` is not used, only its scanner options
+ * (amino acids for a protein table).  Synchronous. */
 k2g_status k2g_sample_minimizers(const k2g_db *db, const char *bases, const uint64_t *seq_off,
                                  uint64_t n_seqs, uint32_t sample_below, uint64_t *keys,
                                  uint64_t keys_cap, uint64_t *n_keys);

@@ -43,6 +43,31 @@ constexpr uint32_t kChunk = 2048;   // k-mer starts per scanning thread
 
 enum : uint32_t { kOpensBlock = 0, kContinues = 1, kSubblockStart = 2 };
 
+// The 15-group reduced amino-acid alphabet of the protein scanner
+// (src/mmscanner.cc:47-95), either case; anything else is ambiguous (0xFF).
+__device__ __forceinline__ uint32_t aa_code(uint32_t c) {
+  if (c >= 'a' && c <= 'z') c -= 32;
+  switch (c) {
+    case '*': case 'U': case 'O': return 0x0;
+    case 'A': return 0x1;
+    case 'N': case 'Q': case 'S': return 0x2;
+    case 'C': return 0x3;
+    case 'D': case 'E': return 0x4;
+    case 'F': return 0x5;
+    case 'G': return 0x6;
+    case 'H': return 0x7;
+    case 'I': case 'L': return 0x8;
+    case 'K': return 0x9;
+    case 'P': return 0xa;
+    case 'R': return 0xb;
+    case 'M': case 'V': return 0xc;
+    case 'T': return 0xd;
+    case 'W': return 0xe;
+    case 'Y': return 0xf;
+    default: return 0xFFu;
+  }
+}
+
 struct Chunk {
   uint64_t pos;     // base index (in the batch) of the first k-mer start, or
                     // of the subblock start
@@ -90,15 +115,18 @@ __global__ void chunk_kernel(ScanView sv, const uint8_t *bases, const Chunk *chu
   uint64_t prev_min = 0;
   uint32_t cnt = 0;
   uint64_t *out = cand + ch.slot;
+  const int bits = sv.protein ? 4 : 2;
   for (uint32_t p = 0; p < len; p++) {
-    const uint32_t code = dna_code(__ldg(seq + p));
+    const uint32_t byte = __ldg(seq + p);
+    const uint32_t code = sv.protein ? aa_code(byte) : dna_code(byte);
     uint64_t lm = ~0ull;
     if (code != 0xFFu) {
-      fwd = ((fwd << 2) | code) & sv.lmer_mask;
+      fwd = ((fwd << bits) | code) & sv.lmer_mask;
       rc = (rc >> 2) | ((uint64_t)(code ^ 3u) << top_shift);
       run++;
       if (run >= l) {
-        const uint64_t rcv = sv.revcom_version ? rc : revcomp_v0(fwd, sv.lmer_mask);
+        // protein l-mers are not canonicalised
+        const uint64_t rcv = sv.protein ? fwd : sv.revcom_version ? rc : revcomp_v0(fwd, sv.lmer_mask);
         uint64_t canon = fwd < rcv ? fwd : rcv;
         if (sv.spaced_mask) canon &= sv.spaced_mask;
         lm = canon ^ sv.toggle;
@@ -404,7 +432,6 @@ extern "C" k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const u
   if (n_keys) *n_keys = 0;
   if (!db || (n_seqs && (!bases || !seq_off || !taxids))) return fail(K2G_ERR_ARG, "null argument");
   if (!block_size || !subblock_size) return fail(K2G_ERR_ARG, "block sizes must be positive");
-  if (!db->opts.dna_db) return fail(K2G_ERR_ARG, "protein databases are not supported");
   if (!n_seqs) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   StreamGuard guard;
@@ -415,7 +442,7 @@ extern "C" k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const u
   k2g_status r = gather(db, bases, seq_off, taxids, n_seqs, block_size, subblock_size, 0, s, st, g);
   if (r != K2G_OK || !g.n) return r;
   const uint64_t n = g.n, nb = g.block_taxon.size();
-  const int l = db->scan_view().l;
+  const int key_bits = db->scan_view().l * (db->opts.dna_db ? 2 : 4);
 
   uint64_t *d_k1;
   uint32_t *d_v1, *d_hist, *d_hsums, *d_btax;
@@ -430,7 +457,7 @@ extern "C" k2g_status k2g_build_sequences(k2g_db *db, const char *bases, const u
 
   // passes: minimizer bytes (2l bits), zone, block bytes
   std::vector<Digit> passes;
-  for (int sh = 0; sh < 2 * l; sh += 8) passes.push_back(Digit{0, sh});
+  for (int sh = 0; sh < key_bits; sh += 8) passes.push_back(Digit{0, sh});
   passes.push_back(Digit{1, 0});
   for (int sh = 0; sh < 32 && (nb - 1) >> sh; sh += 8) passes.push_back(Digit{2, sh});
   uint64_t *ka = g.keys, *kb = d_k1;
@@ -477,7 +504,6 @@ extern "C" k2g_status k2g_sample_minimizers(const k2g_db *db, const char *bases,
   if (!db || !n_keys || (n_seqs && (!bases || !seq_off))) return fail(K2G_ERR_ARG, "null argument");
   *n_keys = 0;
   if (sample_below < 1 || sample_below > 1024) return fail(K2G_ERR_ARG, "sample_below must be in [1, 1024]");
-  if (!db->opts.dna_db) return fail(K2G_ERR_ARG, "protein databases are not supported");
   if (!n_seqs) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   StreamGuard guard;
@@ -495,7 +521,8 @@ extern "C" k2g_status k2g_sample_minimizers(const k2g_db *db, const char *bases,
   K2G_CUDA_TRY(s.get(&d_alt, n));
   K2G_CUDA_TRY(s.get(&d_hist, rsort::hist_entries(n)));
   K2G_CUDA_TRY(s.get(&d_hsums, rsort::sum_entries(n) + 1));
-  K2G_CUDA_TRY(rsort::sort_u64(g.keys, d_alt, n, 2 * db->scan_view().l, d_hist, d_hsums, st, &sorted));
+  K2G_CUDA_TRY(rsort::sort_u64(g.keys, d_alt, n, db->scan_view().l * (db->opts.dna_db ? 2 : 4),
+                               d_hist, d_hsums, st, &sorted));
   uint64_t *d_out = sorted == g.keys ? d_alt : g.keys;
   K2G_CUDA_TRY(s.get(&d_flag, n));
   K2G_CUDA_TRY(s.get(&d_fsums, (n + rsort::kScanChunk - 1) / rsort::kScanChunk + 1));

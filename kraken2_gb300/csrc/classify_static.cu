@@ -118,6 +118,7 @@ extern "C" k2g_status k2g_classify_static(const k2g_db *db, const k2g_reads *rea
                                           const k2g_classify_params *params, k2g_results *out,
                                           void *stream) {
   if (!db || !reads || !params || !out) return fail(K2G_ERR_ARG, "null argument");
+  if (k2g_status s = require_dna(db)) return s;
   if (!reads->n_frags) return K2G_OK;
   if (!reads->d_bases || !reads->d_seq_off || !out->d_call || !out->d_runs || !out->d_status)
     return fail(K2G_ERR_ARG, "missing required buffer");

@@ -71,10 +71,19 @@ k2g::ScanView k2g_db::scan_view() const {
   s.w = (int32_t)(opts.k - opts.l + 1);
   s.revcom_version = opts.revcom_version;
   s.spaced_mask = opts.spaced_seed_mask;
-  s.lmer_mask = (opts.l >= 32) ? ~0ull : ((1ull << (2 * opts.l)) - 1);
+  s.protein = opts.dna_db ? 0 : 1;
+  const uint64_t bits = (opts.dna_db ? 2 : 4) * opts.l;
+  s.lmer_mask = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
   s.toggle = opts.toggle_mask & s.lmer_mask;
   s.min_hash = opts.minimum_acceptable_hash_value;
   return s;
+}
+
+k2g_status k2g::require_dna(const k2g_db *db) {
+  if (db && !db->opts.dna_db)
+    return fail(K2G_ERR_UNSUPPORTED,
+                "translated search (protein databases) is not supported by the GPU classify path");
+  return K2G_OK;
 }
 
 extern "C" const char *k2g_last_error(void) { return g_last_error.c_str(); }
@@ -98,9 +107,9 @@ bool read_exact(int fd, void *buf, size_t n) {
 }
 
 k2g_status validate_options(const k2g_index_options &o) {
-  if (!o.dna_db)
-    return fail(K2G_ERR_UNSUPPORTED, "protein (translated search) databases are not supported");
-  if (o.l < 1 || o.l > 31) return fail(K2G_ERR_FORMAT, "l must be in [1, 31]");
+  // 63 bits of l-mer: 2 per base, 4 per amino acid (src/mmscanner.cc:25-27)
+  if (o.l < 1 || o.l > (o.dna_db ? 31u : 15u))
+    return fail(K2G_ERR_FORMAT, o.dna_db ? "l must be in [1, 31]" : "l must be in [1, 15]");
   if (o.k < o.l) return fail(K2G_ERR_FORMAT, "k must be >= l");
   if (o.k - o.l + 1 > kMaxWindow)
     return fail(K2G_ERR_UNSUPPORTED, "k - l + 1 larger than 16 is not supported");

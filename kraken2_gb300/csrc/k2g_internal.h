@@ -39,6 +39,7 @@ struct TableView {
 struct ScanView {
   int32_t k, l, w;        // w = k - l + 1 window of l-mers per k-mer
   int32_t revcom_version;
+  int32_t protein;        // 4-bit reduced amino-acid alphabet, no reverse complement
   uint64_t spaced_mask;   // 0 = none
   uint64_t toggle;        // toggle_mask & lmer_mask (src/mmscanner.cc:34)
   uint64_t lmer_mask;
@@ -84,6 +85,9 @@ namespace k2g {
 // Thread-local error message plumbing.
 k2g_status fail(k2g_status s, const std::string &msg);
 k2g_status cuda_fail(int err, const char *what);
+// Classification serves nucleotide tables; a protein table (translated
+// search) is refused with K2G_ERR_UNSUPPORTED.
+k2g_status require_dna(const k2g_db *db);
 // Counts each kernel launch issued by the library (k2g_kernel_launches).
 void note_launches(uint64_t n = 1);
 // One round (< 2^30 pairs) of the order-exact build insert (build_ordered.cu).

@@ -723,6 +723,7 @@ extern "C" k2g_status k2g_scan(const k2g_db *db, const char *d_bases, const uint
                                void *stream) {
   if (!db || (n_seqs && (!d_bases || !d_seq_off || !d_mins || !d_ambig)))
     return fail(K2G_ERR_ARG, "null argument");
+  if (k2g_status s = require_dna(db)) return s;
   if (!n_seqs) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   ScanView sv = db->scan_view();
@@ -748,6 +749,7 @@ k2g_status k2g::classify_keyed(const k2g_db *db, const k2g_reads *reads,
                                const k2g_classify_params *params, k2g_results *out, int mode,
                                void *stream, const void *state_key) {
   if (!db || !reads || !params || !out) return fail(K2G_ERR_ARG, "null argument");
+  if (k2g_status s = require_dna(db)) return s;
   if (!reads->n_frags) return K2G_OK;
   if (!reads->d_bases || !reads->d_seq_off || !out->d_call || !out->d_runs || !out->d_status)
     return fail(K2G_ERR_ARG, "missing required buffer");

@@ -365,6 +365,7 @@ extern "C" k2g_status k2g_server_create(const k2g_db *db, const k2g_classify_par
                                         uint64_t hbm_budget_bytes, k2g_server **out) {
   if (!db || !params || !out) return fail(K2G_ERR_ARG, "null argument");
   *out = nullptr;
+  if (k2g_status s = require_dna(db)) return s;
   if (params->confidence < 0 || params->confidence > 1)
     return fail(K2G_ERR_ARG, "confidence threshold must be in [0, 1]");
   K2G_CUDA_TRY(cudaSetDevice(db->device));

@@ -8,7 +8,8 @@
 // starts (scanned in subblocks of -b, which add a minimizer at each
 // subblock start), each block's distinct minimizers inserted in the
 // reference's order.  -F (the reference's nondeterministic build) inserts
-// each sequence's minimizers unordered.  Protein libraries (-X) and 40-bit cells (-C 40) are refused.
+// each sequence's minimizers unordered.  Protein libraries (-X) are scanned
+// as amino acids; 40-bit cells (-C 40) are refused.
 #include <err.h>
 #include <getopt.h>
 #include <sysexits.h>
@@ -183,7 +184,6 @@ void parse_command_line(int argc, char **argv, Options &o) {
               << std::endl;
     usage();
   }
-  if (o.input_is_protein) errx(EX_USAGE, "protein libraries (-X) are not supported by this build");
   if (o.cht_cell_size != 32) errx(EX_USAGE, "40-bit cells (-C 40) are not supported by this build");
 }
 
@@ -283,7 +283,7 @@ int main(int argc, char **argv) {
   idx.l = (uint64_t)o.l;
   idx.spaced_seed_mask = o.spaced_seed_mask;
   idx.toggle_mask = o.toggle_mask;
-  idx.dna_db = 1;
+  idx.dna_db = o.input_is_protein ? 0 : 1;
   idx.revcom_version = kCurrentRevcomVersion;
   idx.minimum_acceptable_hash_value = o.min_clear_hash_value;
   std::vector<uint64_t> parent(tax.nodes.size());
@@ -321,7 +321,8 @@ int main(int argc, char **argv) {
     offs.assign(1, 0);
     taxa.clear();
     if (tty)
-      std::cerr << "\rProcessed " << processed_seqs << " sequences (" << processed_chars << " bp)...";
+      std::cerr << "\rProcessed " << processed_seqs << " sequences (" << processed_chars << " "
+                << (o.input_is_protein ? "aa" : "bp") << ")...";
   };
   // the deterministic build reads on one thread and stops at the first
   // empty block; the fast one (src/build_db.h:75-137) reads on -p threads,
@@ -346,9 +347,13 @@ int main(int argc, char **argv) {
         taxid = tax.lca(taxid, in == internal.end() ? 0 : in->second);
       }
       if (!taxid) continue;
+      const uint64_t len = set.seq_len(i);
+      bases.insert(bases.end(), set.seq_at(i), set.seq_at(i) + len);
+      // protein sequences get a terminator when they lack one
+      // (src/build_db.h:173-175)
+      if (o.input_is_protein && (!len || set.seq_at(i)[len - 1] != '*')) bases.push_back('*');
       processed_seqs++;
-      processed_chars += set.seq_len(i);
-      bases.insert(bases.end(), set.seq_at(i), set.seq_at(i) + set.seq_len(i));
+      processed_chars += bases.size() - offs.back();
       offs.push_back(bases.size());
       taxa.push_back((uint32_t)taxid);
     }
@@ -357,7 +362,7 @@ int main(int argc, char **argv) {
   flush();
   if (tty) std::cerr << "\r";
   std::cerr << "Completed processing of " << processed_seqs << " sequences, " << processed_chars
-            << " bp" << std::endl;
+            << " " << (o.input_is_protein ? "aa" : "bp") << std::endl;
 
   std::cerr << "Writing data to disk... " << std::flush;
   if (k2g_db_write_hash(db, o.hashtable_filename.c_str()) != K2G_OK)
@@ -377,7 +382,7 @@ int main(int argc, char **argv) {
   file_opts.l = (uint64_t)o.l;
   file_opts.spaced_seed_mask = o.spaced_seed_mask;
   file_opts.toggle_mask = o.toggle_mask;
-  file_opts.dna_db = true;
+  file_opts.dna_db = !o.input_is_protein;
   file_opts.minimum_acceptable_hash_value = o.min_clear_hash_value;
   file_opts.revcom_version = kCurrentRevcomVersion;
   std::ofstream opts_fs(o.options_filename, std::ios::binary);

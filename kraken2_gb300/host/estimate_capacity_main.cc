@@ -3,7 +3,7 @@
 // build_db to size the table.  Same flags, usage text, checks and output:
 // the number of distinct minimizers in the library whose MurmurHash3 mod
 // 1024 is below -n, plus one, scaled by 1024 / n.  The sample is gathered
-// on the GPU (k2g_sample_minimizers); protein libraries (-X) are refused.
+// on the GPU (k2g_sample_minimizers); -X scans protein libraries.
 #include <err.h>
 #include <getopt.h>
 #include <sysexits.h>
@@ -109,7 +109,6 @@ void parse_command_line(int argc, char **argv, Options &o) {
     std::cerr << "k cannot be less than l" << std::endl;
     usage();
   }
-  if (o.input_is_protein) errx(EX_USAGE, "protein libraries (-X) are not supported by this build");
 }
 
 }  // namespace
@@ -124,7 +123,7 @@ int main(int argc, char **argv) {
   idx.l = (uint64_t)o.l;
   idx.spaced_seed_mask = o.spaced_seed_mask;
   idx.toggle_mask = o.toggle_mask;
-  idx.dna_db = 1;
+  idx.dna_db = o.input_is_protein ? 0 : 1;
   idx.revcom_version = 1;
   const uint64_t parent[1] = {0};
   k2g_db *db = nullptr;
@@ -143,6 +142,8 @@ int main(int argc, char **argv) {
   k2host::RecordSet set;
   std::vector<uint32_t> counts;
   std::vector<uint64_t> sample, batch;
+  std::vector<char> prot;           // protein sequences with their terminators
+  std::vector<uint64_t> prot_off;
   uint64_t failures_left = (uint64_t)o.threads;
   while (failures_left && !reader.done()) {
     set.clear();
@@ -151,14 +152,28 @@ int main(int argc, char **argv) {
     for (uint32_t c : counts)
       if (!c) failures_left--;
     if (!set.size()) continue;
+    const char *bases = set.seq.data();
+    const uint64_t *offs = set.seq_off.data();
+    if (o.input_is_protein) {   // a terminator when missing (src/estimate_capacity.cc:185-187)
+      prot.clear();
+      prot_off.assign(1, 0);
+      for (size_t i = 0; i < set.size(); i++) {
+        const uint64_t len = set.seq_len(i);
+        prot.insert(prot.end(), set.seq_at(i), set.seq_at(i) + len);
+        if (!len || set.seq_at(i)[len - 1] != '*') prot.push_back('*');
+        prot_off.push_back(prot.size());
+      }
+      bases = prot.data();
+      offs = prot_off.data();
+    }
     uint64_t got = 0;
     batch.resize(set.seq.size() * (uint64_t)o.n / 512 + 4096);
-    k2g_status s = k2g_sample_minimizers(db, set.seq.data(), set.seq_off.data(), set.size(),
-                                         (uint32_t)o.n, batch.data(), batch.size(), &got);
+    k2g_status s = k2g_sample_minimizers(db, bases, offs, set.size(), (uint32_t)o.n, batch.data(),
+                                         batch.size(), &got);
     if (s == K2G_ERR_CAPACITY) {
       batch.resize(got);
-      s = k2g_sample_minimizers(db, set.seq.data(), set.seq_off.data(), set.size(), (uint32_t)o.n,
-                                batch.data(), batch.size(), &got);
+      s = k2g_sample_minimizers(db, bases, offs, set.size(), (uint32_t)o.n, batch.data(),
+                                batch.size(), &got);
     }
     if (s != K2G_OK) errx(EX_SOFTWARE, "%s", k2g_last_error());
     sample.insert(sample.end(), batch.begin(), batch.begin() + got);

@@ -83,10 +83,12 @@ def lca(parent: np.ndarray, a: int, b: int) -> int:
 
 def build(library: bytes, id_map: dict, parent: np.ndarray, external_id: np.ndarray,
           k: int, l: int, mask: int, toggle: int, min_hash: int, capacity: int,
-          value_bits: int, block_size: int, subblock_size: int) -> bytes:
-    """hash.k2d bytes of the deterministic build."""
+          value_bits: int, block_size: int, subblock_size: int, protein: bool = False) -> bytes:
+    """hash.k2d bytes of the deterministic build (protein: build_db -X, the
+    sequences scanned as amino acids with a '*' terminator added when
+    missing, src/build_db.h:173-175)."""
     internal = {int(e): i for i, e in enumerate(external_id) if i}
-    opts = index_opts(k, l, mask, toggle, 1, min_hash)
+    opts = index_opts(k, l, mask, toggle, 1, min_hash, protein=protein)
     keys, taxa = [], []
     for blk in ks.blocks(library, block_bytes=block_size):
         for rec in blk:
@@ -100,6 +102,8 @@ def build(library: bytes, id_map: dict, parent: np.ndarray, external_id: np.ndar
             if not taxid:
                 continue
             seq = rec.seq
+            if protein and not seq.endswith(b"*"):
+                seq += b"*"
             for j in range(0, len(seq), block_size):
                 finish = min(j + block_size + k - 1, len(seq))
                 parts = []
@@ -129,14 +133,14 @@ def build(library: bytes, id_map: dict, parent: np.ndarray, external_id: np.ndar
 
 
 def estimate_capacity(library: bytes, k: int, l: int, mask: int, toggle: int, n: int,
-                      threads: int) -> int:
+                      threads: int, protein: bool = False) -> int:
     """EstimateCapacity (src/estimate_capacity.cc:57-92, :180-203): `threads`
     readers take records one at a time, each stopping at its first failed
     read; every record's whole-sequence minimizers of unambiguous k-mers
     whose MurmurHash3 mod 1024 is below n are counted once; the count plus
     one is scaled by 1024 / n."""
     from . import scan
-    opts = index_opts(k, l, mask, toggle, 1, 0)
+    opts = index_opts(k, l, mask, toggle, 1, 0, protein=protein)
     seen = set()
     failures = 0
     for recs, ended in ks.block_attempts(library, count=1):
@@ -147,7 +151,10 @@ def estimate_capacity(library: bytes, k: int, l: int, mask: int, toggle: int, n:
             if failures == threads:
                 break
             continue
-        mins, amb = scan(opts, recs[0].seq)
+        seq = recs[0].seq
+        if protein and not seq.endswith(b"*"):
+            seq += b"*"
+        mins, amb = scan(opts, seq)
         m = mins[amb == 0]
         m = m[(murmur3_np(m) & np.uint64(1023)) < np.uint64(n)]
         seen.update(m.tolist())

@@ -45,6 +45,8 @@ VARIANTS = {
     "c_k_eq_l": ("db_c", 31, 31, 90_000, ["-B", "3000"]),
     "edge": ("edge", 25, 21, 150_000, ["-B", "2048"]),
     "a_full": ("db_a", 35, 31, 30_000, ["-S", SEED_A]),
+    "p_default": ("protein", 15, 12, 60_000, ["-X"]),
+    "p_B500": ("protein", 15, 12, 60_000, ["-X", "-B", "500", "-b", "64"]),
 }
 
 # name -> (input set, k, l, flags) for estimate_capacity
@@ -58,6 +60,7 @@ ESTIMATES = {
     "edge": ("edge", 25, 21, ["-n", "512", "-p", "3"]),
     "damaged_p1": ("damaged", 35, 31, ["-n", "1024", "-p", "1"]),
     "damaged_p4": ("damaged", 35, 31, ["-n", "1024", "-p", "4"]),
+    "protein": ("protein", 15, 12, ["-X", "-n", "256"]),
 }
 
 ESTIMATE_USAGE = [["-h"], [], ["-k", "31"], ["-k", "20", "-l", "25"], ["-l", "32"],
@@ -102,6 +105,10 @@ def write_inputs(name: str, directory: str):
         tax.write_dmp(tdir)
         synth.write_library(genomes, tax, lib, mp)
         return tdir, lib, mp
+    if name == "protein":   # frame-0 translations of db_a's genomes
+        import make_protein
+        sys.path.insert(0, ROOT)
+        return make_protein.protein_library(directory)
     if name == "damaged":
         # db_a's library with records whose qualities are one short (each
         # read fails and takes the next header line as qualities) and one

@@ -16,7 +16,7 @@ FLAGS = {"plain": [], "mpa": ["-m"], "zeros": ["-z"], "stats": ["-s"], "mpa_zero
 def main():
     out_dir = os.path.join(HERE, "inspect")
     os.makedirs(out_dir, exist_ok=True)
-    for db in ("db_a", "db_b", "db_c"):
+    for db in ("db_a", "db_b", "db_c", "db_p"):
         d = os.path.join(HERE, db)
         base = [REF, "-H", f"{d}/hash.k2d", "-t", f"{d}/taxo.k2d", "-o", f"{d}/opts.k2d"]
         for name, flags in FLAGS.items():

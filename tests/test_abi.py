@@ -1,6 +1,7 @@
 """C-ABI surface checks that need no GPU: the library builds and loads, it
 exports every entry point include/k2g.h declares, and malformed database
 files are rejected with a status (never an abort) before any device work."""
+import ctypes
 import os
 import re
 import shutil
@@ -100,13 +101,33 @@ def test_forty_bit_cells_unsupported(tmp_path):
     assert _open_status(d) == 7
 
 
-def test_protein_db_unsupported(tmp_path):
+def test_protein_l_limit(tmp_path):
+    """A protein table packs 4 bits per residue: l = 31 does not fit (the
+    reference's scanner allows l <= 15 for proteins)."""
     d = _copy_db(tmp_path)
     p = os.path.join(d, "opts.k2d")
     raw = bytearray(open(p, "rb").read())
     raw[32] = 0
     open(p, "wb").write(raw)
-    assert _open_status(d) == 7
+    assert _open_status(d) == 3
+
+
+@pytest.mark.gpu
+def test_protein_db_opens_and_classify_refuses_it():
+    """Protein tables load (value counts and builds serve them); the GPU
+    classify entry points refuse them until translated search runs there."""
+    import numpy as np
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_p"))
+    counts, outside = db.value_counts()
+    assert counts.sum() == db.info().size
+    bases = b"ACGTACGTACGTACGTACGTACGTACGTACGTACGTACGT"
+    off = np.array([0, 40], np.uint64)
+    call = np.zeros(1, np.uint32)
+    params = k2g.ClassifyParams(0.0, 0, 0, 0, 0)
+    st = k2g.lib().k2g_classify_host(db.h, bases, None, off.ctypes.data, 1, ctypes.byref(params),
+                                     call.ctypes.data, None, None, None, None, None)
+    assert st == 7
+    db.close()
 
 
 def test_window_too_wide_unsupported(tmp_path):

@@ -53,12 +53,11 @@ def test_usage_and_errors_match_reference(case):
     assert r.stderr.decode() == case["stderr"]
 
 
-def test_protein_and_wide_cells_refused():
+def test_wide_cells_refused():
     base = ["-H", "h", "-m", "m", "-t", "t", "-n", "n", "-o", "o", "-k", "15", "-l", "12",
             "-c", "9"]
-    for extra in (["-X"], ["-C", "40"]):
-        r = subprocess.run([exe(), *base, *extra], capture_output=True)
-        assert r.returncode == 64 and b"not supported" in r.stderr
+    r = subprocess.run([exe(), *base, "-C", "40"], capture_output=True)
+    assert r.returncode == 64 and b"not supported" in r.stderr
 
 
 @pytest.mark.parametrize("name,want", VARIANTS, ids=[v for v, _ in VARIANTS])
@@ -95,6 +94,7 @@ def test_table_matches_reference(name, want, tmp_path):
 def _variant_params(name, want):
     """The table parameters the reference derives from a variant's flags."""
     _, k, l, cap, extra = make_builds.VARIANTS[name]
+    extra = [a for a in extra if a != "-X"]
     flags = dict(zip(extra[::2], extra[1::2]))
     return k, l, cap, flags
 
@@ -137,7 +137,8 @@ def test_oracle_build_matches_reference(name, want, tmp_path):
     with open(lib, "rb") as f, open(mp) as g:
         library, id_map = f.read(), ob.read_id_map(g.read())
     args = (library, id_map, tax.parent, tax.external_id, k, l, mask, toggle, min_hash, capacity,
-            vb, int(flags.get("-B", 10 * 1024 * 1024)), int(flags.get("-b", 1024)))
+            vb, int(flags.get("-B", 10 * 1024 * 1024)), int(flags.get("-b", 1024)),
+            "-X" in make_builds.VARIANTS[name][4])
     if want["rc"]:
         with pytest.raises(RuntimeError):
             ob.build(*args)
@@ -210,13 +211,15 @@ ESTIMATES = sorted(BUILDS["estimates"].items())
 def test_oracle_estimate_matches_reference(name, want, tmp_path):
     from oracle import build_db as ob
     inp, k, l, flags = make_builds.ESTIMATES[name]
+    protein = "-X" in flags
+    flags = [a for a in flags if a != "-X"]
     f = dict(zip(flags[::2], flags[1::2]))
     _, lib, _ = make_builds.write_inputs(inp, str(tmp_path / "in"))
     mask = _expand(_strtol2(f["-S"])) if "-S" in f else 0
     toggle = _strtol2(f["-T"]) if "-T" in f else 0xe37e28c4271b5a2d
     with open(lib, "rb") as fh:
         got = ob.estimate_capacity(fh.read(), k, l, mask, toggle, int(f.get("-n", 4)),
-                                   int(f.get("-p", 1)))
+                                   int(f.get("-p", 1)), protein)
     assert got == want
 
 

@@ -40,7 +40,7 @@ def test_usage_and_errors():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("db", ["db_a", "db_b", "db_c"])
+@pytest.mark.parametrize("db", ["db_a", "db_b", "db_c", "db_p"])
 @pytest.mark.parametrize("name", sorted(FLAGS))
 def test_outputs_identical_to_reference(db, name):
     r = subprocess.run([exe()] + db_args(db) + FLAGS[name], capture_output=True, check=True)
@@ -71,7 +71,7 @@ def numpy_counts(cells, value_bits, node_count):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("db", ["db_a", "db_b", "db_c"])
+@pytest.mark.parametrize("db", ["db_a", "db_b", "db_c", "db_p"])
 def test_value_counts_golden_tables(db):
     g = golden_db(db)
     d = k2g.Database.open(os.path.join(GOLDEN, db))
