@@ -53,6 +53,7 @@ typedef enum {
 
 /* Codes of the per-k-mer hit list besides taxon ids (src/classify.cc:33-35). */
 #define K2G_CODE_MATE_BORDER 0xFFFFFFFFu
+#define K2G_CODE_FRAME_BORDER 0xFFFFFFFEu   /* translated search, "-:-" */
 #define K2G_CODE_AMBIGUOUS   0xFFFFFFFDu
 
 typedef struct k2g_db k2g_db;
@@ -79,9 +80,10 @@ const char *k2g_last_error(void);
 const char *k2g_version(void);
 
 /* Loads the three database files and uploads the table and the taxonomy's
- * parent array.  Protein (translated search) tables load -- lookups, value
- * counts and builds serve them -- but the classify entry points refuse them
- * with K2G_ERR_UNSUPPORTED.  Replaces load_index (src/classify.cc:269-302): the opts
+ * parent array.  A protein table (dna_db 0) is classified by translated
+ * search (six frames per mate) in k2g_classify and the host-buffer paths;
+ * k2g_classify_static, k2g_scan and the server serve nucleotide tables only
+ * (K2G_ERR_UNSUPPORTED).  Replaces load_index (src/classify.cc:269-302): the opts
  * file read (:272-279), Taxonomy::Init (src/taxonomy.cc:195-238) and
  * CompactHashTable::LoadTable (src/compact_hash.h:279-341). */
 k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,

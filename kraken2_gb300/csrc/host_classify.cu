@@ -212,7 +212,6 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
                                 uint32_t *hit_groups, uint32_t *hitlist_len, uint64_t *runs,
                                 uint64_t *n_runs, uint64_t *taxon_reads) {
   if (!db || !bases || !seq_off || !params || !call) return fail(K2G_ERR_ARG, "null argument");
-  if (k2g_status s = require_dna(db)) return s;
   if (counters && !frag_block) return fail(K2G_ERR_ARG, "counters need frag_block");
   if (runs && !n_runs) return fail(K2G_ERR_ARG, "runs given without n_runs capacity");
   const uint64_t runs_cap = runs ? *n_runs : 0;

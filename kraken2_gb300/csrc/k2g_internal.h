@@ -85,9 +85,13 @@ namespace k2g {
 // Thread-local error message plumbing.
 k2g_status fail(k2g_status s, const std::string &msg);
 k2g_status cuda_fail(int err, const char *what);
-// Classification serves nucleotide tables; a protein table (translated
-// search) is refused with K2G_ERR_UNSUPPORTED.
+// The paths that serve nucleotide tables only (the static kernel, the
+// server) refuse a protein table with K2G_ERR_UNSUPPORTED.
 k2g_status require_dna(const k2g_db *db);
+// Translated search for a protein table (translated.cu), on `st`.
+k2g_status classify_translated(const k2g_db *db, const k2g_reads *reads,
+                               const k2g_classify_params *params, k2g_results *out,
+                               cudaStream_t st);
 // Counts each kernel launch issued by the library (k2g_kernel_launches).
 void note_launches(uint64_t n = 1);
 // One round (< 2^30 pairs) of the order-exact build insert (build_ordered.cu).

@@ -749,12 +749,15 @@ k2g_status k2g::classify_keyed(const k2g_db *db, const k2g_reads *reads,
                                const k2g_classify_params *params, k2g_results *out, int mode,
                                void *stream, const void *state_key) {
   if (!db || !reads || !params || !out) return fail(K2G_ERR_ARG, "null argument");
-  if (k2g_status s = require_dna(db)) return s;
   if (!reads->n_frags) return K2G_OK;
   if (!reads->d_bases || !reads->d_seq_off || !out->d_call || !out->d_runs || !out->d_status)
     return fail(K2G_ERR_ARG, "missing required buffer");
   if (params->confidence < 0 || params->confidence > 1)
     return fail(K2G_ERR_ARG, "confidence threshold must be in [0, 1]");
+  if (!db->opts.dna_db) {   // translated search (translated.cu)
+    K2G_CUDA_TRY(cudaSetDevice(db->device));
+    return classify_translated(db, reads, params, out, (cudaStream_t)stream);
+  }
   if (out->d_hit_keys && (!out->d_hit_taxa || !out->d_hit_order || !out->d_hits_used))
     return fail(K2G_ERR_ARG, "incomplete hit event buffers");
   if (reads->max_seq_len >= (1ull << 31)) return fail(K2G_ERR_ARG, "sequence too long");

@@ -442,6 +442,8 @@ class Pipeline {
             if (j) ko.push_back(' ');
             if (code == K2G_CODE_MATE_BORDER) {
               ko += "|:|";
+            } else if (code == K2G_CODE_FRAME_BORDER) {
+              ko += "-:-";
             } else if (code == K2G_CODE_AMBIGUOUS) {
               ko += "A:";
               append_u64(ko, cnt);
@@ -606,12 +608,6 @@ int main(int argc, char **argv) {
   if (k2g_db_open(o.index_filename.c_str(), o.taxonomy_filename.c_str(),
                   o.options_filename.c_str(), 0, &db) != K2G_OK)
     errx(EX_DATAERR, "%s", k2g_last_error());
-  {
-    k2g_db_info info{};
-    if (k2g_db_info_get(db, &info) != K2G_OK) errx(EX_SOFTWARE, "%s", k2g_last_error());
-    if (!info.opts.dna_db)
-      errx(EX_DATAERR, "translated search (protein databases) is not supported by this build");
-  }
   std::cerr << " done." << std::endl;
 
   const bool report = !o.report_filename.empty();

@@ -113,9 +113,9 @@ def test_protein_l_limit(tmp_path):
 
 
 @pytest.mark.gpu
-def test_protein_db_opens_and_classify_refuses_it():
-    """Protein tables load (value counts and builds serve them); the GPU
-    classify entry points refuse them until translated search runs there."""
+def test_protein_db_opens_and_classifies():
+    """Protein tables load; value counts serve them and the host-buffer
+    classify path runs translated search on them."""
     import numpy as np
     db = k2g.Database.open(os.path.join(GOLDEN, "db_p"))
     counts, outside = db.value_counts()
@@ -126,7 +126,7 @@ def test_protein_db_opens_and_classify_refuses_it():
     params = k2g.ClassifyParams(0.0, 0, 0, 0, 0)
     st = k2g.lib().k2g_classify_host(db.h, bases, None, off.ctypes.data, 1, ctypes.byref(params),
                                      call.ctypes.data, None, None, None, None, None)
-    assert st == 7
+    assert st == 0
     db.close()
 
 
