@@ -27,6 +27,7 @@ MODE_PLAIN = 0
 MODE_PERSISTENT = 1
 MODE_PIPELINED = 2
 CODE_MATE_BORDER = 0xFFFFFFFF
+CODE_FRAME_BORDER = 0xFFFFFFFE   # translated search, printed "-:-"
 CODE_AMBIGUOUS = 0xFFFFFFFD
 HIT_MARK_RESET = 1          # K2G_HIT_MARK_RESET
 HIT_MARK_STOP = 2           # K2G_HIT_MARK_STOP

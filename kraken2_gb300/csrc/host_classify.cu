@@ -245,7 +245,11 @@ static k2g_status host_classify(const k2g_db *db, const char *bases, const char 
     chunk_frags = std::max(chunk_frags, cuts[c + 1] - cuts[c]);
     chunk_bases = std::max(chunk_bases, seq_off[cuts[c + 1] * per] - seq_off[cuts[c] * per]);
   }
-  const uint64_t hits_cap = counters ? chunk_bases + 4 * chunk_frags + 16 : 0;
+  // at most one lookup per k-mer; translated, six frames of a third of the
+  // bases each (two lookups per base) plus the frames' ends
+  const uint64_t hits_cap = !counters ? 0
+                            : db->opts.dna_db ? chunk_bases + 4 * chunk_frags + 16
+                                              : 2 * chunk_bases + 32 * chunk_frags + 16;
 
   HostCache &hc = g_host[db->device & 63];
   std::lock_guard<std::mutex> lock(hc.mu);

@@ -57,6 +57,8 @@ class DeviceResult:
             code = int(x) >> 32
             if code == k2g.CODE_MATE_BORDER:
                 code = 0xFFFFFFFFFFFFFFFF
+            elif code == k2g.CODE_FRAME_BORDER:
+                code = 0xFFFFFFFFFFFFFFFE
             elif code == k2g.CODE_AMBIGUOUS:
                 code = 0xFFFFFFFFFFFFFFFD
             out.append((code, int(x) & 0xFFFFFFFF))
