@@ -40,6 +40,8 @@ RUNS = {
     "p_pe": (["-P", "-T", "0.05", "-g", "2", "-R", "x", "-K"], "p_pe"),
     "p_quick": (["-q", "-g", "1"], "p_se"),
     "p_edge": (["-T", "0", "-g", "0", "-R", "x"], "p_edge"),
+    "p_minqual": (["-Q", "25", "-T", "0", "-g", "2", "-R", "x", "-K"], "p_se"),
+    "p_pe_minqual": (["-P", "-Q", "20", "-g", "1", "-R", "x"], "p_pe"),
 }
 
 

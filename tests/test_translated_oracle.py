@@ -66,20 +66,22 @@ def _batch(key):
     r = make_protein.read_set(key)
     paired = key == "p_pe"
     m1, m2 = (r if paired else (r, None))
-    seqs, headers, lens = [], [], []
+    seqs, quals, headers, lens = [], [], [], []
     for i in range(len(m1.names)):
         headers.append(split_header(m1.names[i])[0])
         if paired:
             seqs += [m1.seqs[i], m2.seqs[i]]
+            quals += [m1.quals[i], m2.quals[i]]
             lens.append((len(m1.seqs[i]), len(m2.seqs[i])))
         else:
             seqs.append(m1.seqs[i])
+            quals.append(m1.quals[i])
             lens.append((len(m1.seqs[i]),))
     off = np.zeros(len(seqs) + 1, np.uint64)
     off[1:] = np.cumsum([len(x) for x in seqs])
-    quals = b"".join(q for m in ((m1, m2) if paired else (m1,)) for q in [])  # unused
     blocks = np.zeros(len(headers), np.uint32)
-    return Batch(b"".join(seqs), None, off, len(headers), paired, headers, lens, blocks)
+    return Batch(b"".join(seqs), b"".join(quals), off, len(headers), paired, headers, lens,
+                 blocks)
 
 
 @pytest.mark.parametrize("tag,run", RUNS, ids=[t for t, _ in RUNS])
@@ -95,7 +97,7 @@ def test_translated_runs(tag, run):
                                           o.revcom_version, o.minimum_acceptable_hash_value,
                                           protein=True))
     b = _batch(run["reads"])
-    calls, hg, nr, runs, base = orc.classify(b.bases, None, b.seq_off, b.n_frags, threads=4,
+    calls, hg, nr, runs, base = orc.classify(b.bases, b.quals, b.seq_off, b.n_frags, threads=4,
                                              **params)
     lines = [kraken_line(int(calls[i]), b.headers[i], b.lens[i], _runs_of(runs, base[i], nr[i]),
                          g.taxo, b.paired, names=flags["names"], quick=params["quick"])
@@ -106,7 +108,7 @@ def test_translated_runs(tag, run):
     assert not bad, f"{len(bad)} lines differ, first: {lines[bad[0]]!r} vs {want[bad[0]]!r}"
     if flags["report"]:
         clade_reads, taxon_reads, clade_kmers, distinct = orc.taxon_counters(
-            b.bases, None, b.seq_off, b.n_frags, b.blocks, kmer_data=flags["kmer_data"],
+            b.bases, b.quals, b.seq_off, b.n_frags, b.blocks, kmer_data=flags["kmer_data"],
             **params)
         ext = g.taxo.external_id
         rep = golden_report(tag)
