@@ -184,7 +184,7 @@ void parse_command_line(int argc, char **argv, Options &o) {
               << std::endl;
     usage();
   }
-  if (o.cht_cell_size != 32) errx(EX_USAGE, "40-bit cells (-C 40) are not supported by this build");
+  if (o.cht_cell_size != 32) errx(EX_USAGE, "40-bit cells (-C 40) are not supported");
 }
 
 // ReadIDToTaxonMap (src/build_db.cc:147-163): "<seqid> <taxid>" per line

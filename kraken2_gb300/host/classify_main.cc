@@ -598,7 +598,7 @@ void report_stats(const timeval &t1, const timeval &t2, const Stats &s) {
 int main(int argc, char **argv) {
   Options o;
   parse_command_line(argc, argv, o);
-  if (o.daemon_mode) errx(EX_USAGE, "daemon mode (-D) is not supported by this build");
+  if (o.daemon_mode) errx(EX_USAGE, "daemon mode (-D) is not supported");
 
   std::cerr << "Loading database information...";
   k2host::TaxonomyFile tax;
