@@ -31,7 +31,8 @@ class Ctx(C.Structure):
     _fields_ = [("table", C.c_void_p), ("capacity", C.c_uint64), ("key_bits", C.c_int),
                 ("value_bits", C.c_int), ("parent", C.c_void_p), ("node_count", C.c_uint64),
                 ("idx", IndexOpts), ("confidence", C.c_double), ("min_hit_groups", C.c_int),
-                ("quick", C.c_int), ("paired", C.c_int), ("min_quality", C.c_int)]
+                ("quick", C.c_int), ("paired", C.c_int), ("min_quality", C.c_int),
+                ("cell40", C.c_int)]
 
 
 class Run(C.Structure):
@@ -67,6 +68,11 @@ def lib():
         L.ko_get_batch.restype = None
         L.ko_get_batch.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_void_p,
                                    C.c_void_p, C.c_size_t, C.c_int]
+        L.ko_get40.restype = C.c_uint32
+        L.ko_get40.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_uint64]
+        L.ko_insert_lca40.restype = C.c_int
+        L.ko_insert_lca40.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_int, U64P, U64P,
+                                      U32P, C.c_size_t, C.POINTER(C.c_uint64)]
         L.ko_insert_lca.restype = C.c_int
         L.ko_insert_lca.argtypes = [U32P, C.c_uint64, C.c_int, C.c_int, U64P, U64P, U32P,
                                     C.c_size_t, C.POINTER(C.c_uint64)]
@@ -139,7 +145,9 @@ class Oracle:
 
     def __init__(self, table: np.ndarray, capacity: int, key_bits: int, value_bits: int,
                  parent: np.ndarray, opts: IndexOpts):
-        self.table = np.ascontiguousarray(table, dtype=np.uint32)
+        # 40-bit cells (key + value bits = 40) are held as 5 packed bytes each
+        self.cell40 = key_bits + value_bits == 40
+        self.table = np.ascontiguousarray(table, dtype=np.uint8 if self.cell40 else np.uint32)
         self.parent = np.ascontiguousarray(parent, dtype=np.uint64)
         self.capacity, self.key_bits, self.value_bits = capacity, key_bits, value_bits
         self.opts = opts
@@ -147,7 +155,7 @@ class Oracle:
     def ctx(self, confidence=0.0, min_hit_groups=0, quick=False, paired=False, min_quality=0):
         return Ctx(self.table.ctypes.data, self.capacity, self.key_bits, self.value_bits,
                    self.parent.ctypes.data, len(self.parent), self.opts, confidence,
-                   min_hit_groups, int(quick), int(paired), min_quality)
+                   min_hit_groups, int(quick), int(paired), min_quality, int(self.cell40))
 
     def get_batch(self, keys: np.ndarray, threads: int = 1) -> np.ndarray:
         keys = np.ascontiguousarray(keys, dtype=np.uint64)

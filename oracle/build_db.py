@@ -83,7 +83,8 @@ def lca(parent: np.ndarray, a: int, b: int) -> int:
 
 def build(library: bytes, id_map: dict, parent: np.ndarray, external_id: np.ndarray,
           k: int, l: int, mask: int, toggle: int, min_hash: int, capacity: int,
-          value_bits: int, block_size: int, subblock_size: int, protein: bool = False) -> bytes:
+          value_bits: int, block_size: int, subblock_size: int, protein: bool = False,
+          cell_bits: int = 32) -> bytes:
     """hash.k2d bytes of the deterministic build (protein: build_db -X, the
     sequences scanned as amino acids with a '*' terminator added when
     missing, src/build_db.h:173-175)."""
@@ -120,16 +121,24 @@ def build(library: bytes, id_map: dict, parent: np.ndarray, external_id: np.ndar
                 taxa.append(np.full(len(m), taxid, np.uint32))
     keys = np.concatenate(keys) if keys else np.zeros(0, np.uint64)
     taxa = np.concatenate(taxa) if taxa else np.zeros(0, np.uint32)
-    table = np.zeros(capacity, np.uint32)
     size = C.c_uint64(0)
     par = np.ascontiguousarray(parent, dtype=np.uint64)
-    rc = lib().ko_insert_lca(table, capacity, 32 - value_bits, value_bits, par,
-                             np.ascontiguousarray(keys), np.ascontiguousarray(taxa), len(keys),
-                             C.byref(size))
+    key_bits = cell_bits - value_bits
+    if cell_bits == 40:   # build_db -C 40: packed 5-byte cells
+        table = np.zeros(5 * capacity, np.uint8)
+        rc = lib().ko_insert_lca40(table.ctypes.data, capacity, key_bits, value_bits, par,
+                                   np.ascontiguousarray(keys), np.ascontiguousarray(taxa),
+                                   len(keys), C.byref(size))
+        cells = table.tobytes()
+    else:
+        table = np.zeros(capacity, np.uint32)
+        rc = lib().ko_insert_lca(table, capacity, key_bits, value_bits, par,
+                                 np.ascontiguousarray(keys), np.ascontiguousarray(taxa), len(keys),
+                                 C.byref(size))
+        cells = table.astype("<u4").tobytes()
     if rc != 0:
         raise RuntimeError("compact hash table capacity exceeded")
-    return struct.pack("<QQQQ", capacity, size.value, 32 - value_bits, value_bits) + \
-        table.astype("<u4").tobytes()
+    return struct.pack("<QQQQ", capacity, size.value, key_bits, value_bits) + cells
 
 
 def estimate_capacity(library: bytes, k: int, l: int, mask: int, toggle: int, n: int,

@@ -164,6 +164,90 @@ int ko_insert_lca(uint32_t *table, uint64_t capacity, int key_bits,
   return 0;
 }
 
+/* ---- 40-bit cells: CompactHashCell40 (src/compact_hash.h:50-89), packed
+ * five bytes: a (value in the low value_bits, the key's low 32 - value_bits
+ * bits above it), then b (the key's next 8 bits).  hashed_key rebuilds the
+ * key in 32-bit arithmetic, so with fewer than 8 value bits the key's top
+ * bit is lost and such keys never match; the restatement keeps that. */
+static inline uint32_t c40_a(const uint8_t *t, uint64_t i) {
+  const uint8_t *p = t + 5 * i;
+  return (uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24;
+}
+static inline uint32_t c40_value(const uint8_t *t, uint64_t i, int vb) {
+  return c40_a(t, i) & (uint32_t)((1u << vb) - 1);
+}
+static inline uint64_t c40_key(const uint8_t *t, uint64_t i, int vb) {
+  const uint32_t a = c40_a(t, i), b = t[5 * i + 4];
+  return (uint32_t)((a >> vb) | (b << (32 - vb)));
+}
+static inline void c40_populate(uint8_t *t, uint64_t i, uint64_t key, uint32_t val, int vb) {
+  const int a_bits = 32 - vb;
+  val &= (uint32_t)((1u << vb) - 1);
+  const uint32_t a = (uint32_t)(((key & ((1ull << a_bits) - 1)) << vb) | val);
+  uint8_t *p = t + 5 * i;
+  p[0] = (uint8_t)a;
+  p[1] = (uint8_t)(a >> 8);
+  p[2] = (uint8_t)(a >> 16);
+  p[3] = (uint8_t)(a >> 24);
+  p[4] = (uint8_t)(key >> a_bits);
+}
+
+/* CompactHashTable<CompactHashCell40>::Get -- src/compact_hash.h:355-374. */
+uint32_t ko_get40(const uint8_t *table, uint64_t capacity, int key_bits, int value_bits,
+                  uint64_t key) {
+  uint64_t hc = ko_murmur3(key);
+  uint64_t compacted = hc >> (64 - key_bits);
+  uint64_t idx = hc % capacity, first = idx;
+  for (;;) {
+    if (!c40_value(table, idx, value_bits)) break;
+    if (c40_key(table, idx, value_bits) == compacted) return c40_value(table, idx, value_bits);
+    idx += 1;
+    idx %= capacity;
+    if (idx == first) break;
+  }
+  return 0;
+}
+
+/* CompareAndSet and SetMinimizerLCA over 40-bit cells (src/compact_hash.h:
+ * 417-462, src/build_db.h:187-194). */
+static int cas40(uint8_t *table, uint64_t capacity, int key_bits, int value_bits, uint64_t key,
+                 uint32_t new_value, uint32_t *old_value, uint64_t *size) {
+  if (new_value == 0) return 0;
+  if ((uint64_t)new_value > ((1ull << value_bits) - 1)) return -2;
+  uint64_t hc = ko_murmur3(key);
+  uint64_t compacted = hc >> (64 - key_bits);
+  uint64_t idx = hc % capacity, first = idx;
+  for (;;) {
+    const uint32_t v = c40_value(table, idx, value_bits);
+    if (!v || c40_key(table, idx, value_bits) == compacted) {
+      if (*old_value == v) {
+        c40_populate(table, idx, compacted, new_value, value_bits);
+        if (!*old_value) (*size)++;
+        return 1;
+      }
+      *old_value = v;
+      return 0;
+    }
+    idx += 1;
+    idx %= capacity;
+    if (idx == first) return -1;
+  }
+}
+
+int ko_insert_lca40(uint8_t *table, uint64_t capacity, int key_bits, int value_bits,
+                    const uint64_t *parent, const uint64_t *keys, const uint32_t *taxids,
+                    size_t n, uint64_t *size) {
+  for (size_t i = 0; i < n; i++) {
+    uint32_t old_value = 0, new_value = taxids[i];
+    int r;
+    while ((r = cas40(table, capacity, key_bits, value_bits, keys[i], new_value, &old_value,
+                      size)) == 0)
+      new_value = (uint32_t)ko_lca(parent, old_value, taxids[i]);
+    if (r < 0) return r;
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Minimizer scanner -- src/mmscanner.cc:20-46, :98-189, :193-220            */
 /* ------------------------------------------------------------------------ */
@@ -577,7 +661,9 @@ static void classify_ws(const ko_ctx *c, const char *seq1, size_t len1, const ch
 
   /* Phase 2: batched lookup (classify.cc:841-844). */
   for (size_t i = 0; i < nkeys; i++)
-    vals[i] = ko_get(c->table, c->capacity, c->key_bits, c->value_bits, keys[i]);
+    vals[i] = c->cell40 ? ko_get40((const uint8_t *)c->table, c->capacity, c->key_bits,
+                                   c->value_bits, keys[i])
+                        : ko_get(c->table, c->capacity, c->key_bits, c->value_bits, keys[i]);
 
   /* Phase 3: replay (classify.cc:847-888). */
   cmap hit_counts;

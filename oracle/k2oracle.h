@@ -42,6 +42,13 @@ int ko_compare_and_set(uint32_t *table, uint64_t capacity, int key_bits,
                        uint32_t *old_value, uint64_t *size);
 uint64_t ko_lca(const uint64_t *parent, uint64_t a, uint64_t b);
 int ko_is_ancestor(const uint64_t *parent, uint64_t a, uint64_t b);
+/* The same over packed 5-byte 40-bit cells (CompactHashCell40,
+ * src/compact_hash.h:50-89), keeping its 32-bit key reassembly. */
+uint32_t ko_get40(const uint8_t *table, uint64_t capacity, int key_bits, int value_bits,
+                  uint64_t key);
+int ko_insert_lca40(uint8_t *table, uint64_t capacity, int key_bits, int value_bits,
+                    const uint64_t *parent, const uint64_t *keys, const uint32_t *taxids,
+                    size_t n, uint64_t *size);
 /* SetMinimizerLCA over a list, in list order (src/build_db.h:187-194). */
 int ko_insert_lca(uint32_t *table, uint64_t capacity, int key_bits,
                   int value_bits, const uint64_t *parent, const uint64_t *keys,
@@ -79,6 +86,7 @@ typedef struct {
   ko_index_opts idx;
   double confidence;
   int min_hit_groups, quick, paired, min_quality;
+  int cell40;               /* table holds packed 5-byte CompactHashCell40 cells */
 } ko_ctx;
 
 typedef struct { uint64_t code; uint32_t count; } ko_run;
