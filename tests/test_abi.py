@@ -1,7 +1,6 @@
 """C-ABI surface checks that need no GPU: the library builds and loads, it
 exports every entry point include/k2g.h declares, and malformed database
 files are rejected with a status (never an abort) before any device work."""
-import ctypes
 import os
 import re
 import shutil
@@ -111,23 +110,6 @@ def test_protein_l_limit(tmp_path):
     open(p, "wb").write(raw)
     assert _open_status(d) == 3
 
-
-@pytest.mark.gpu
-def test_protein_db_opens_and_classifies():
-    """Protein tables load; value counts serve them and the host-buffer
-    classify path runs translated search on them."""
-    import numpy as np
-    db = k2g.Database.open(os.path.join(GOLDEN, "db_p"))
-    counts, outside = db.value_counts()
-    assert counts.sum() == db.info().size
-    bases = b"ACGTACGTACGTACGTACGTACGTACGTACGTACGTACGT"
-    off = np.array([0, 40], np.uint64)
-    call = np.zeros(1, np.uint32)
-    params = k2g.ClassifyParams(0.0, 0, 0, 0, 0)
-    st = k2g.lib().k2g_classify_host(db.h, bases, None, off.ctypes.data, 1, ctypes.byref(params),
-                                     call.ctypes.data, None, None, None, None, None)
-    assert st == 0
-    db.close()
 
 
 def test_window_too_wide_unsupported(tmp_path):

@@ -3,6 +3,7 @@ the reference classify's runs on a protein table (tests/golden/protein.json,
 made by tests/golden/make_protein.py): through k2g_classify, every kraken
 line and taxon read count; through the classify drop-in, stdout and reports
 byte for byte."""
+import ctypes
 import gzip
 import json
 import os
@@ -67,3 +68,20 @@ def test_dropin_outputs_match_reference(tag, run, tmp_path):
     if "-R" in args:
         with open(report, "rb") as f, open(os.path.join(GOLDEN, "runs", tag + ".report"), "rb") as g:
             assert f.read() == g.read()
+
+
+def test_protein_db_opens_and_classifies():
+    """Protein tables load; value counts serve them and the host-buffer
+    classify path runs translated search on them."""
+    import numpy as np
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_p"))
+    counts, outside = db.value_counts()
+    assert counts.sum() == db.info().size
+    bases = b"ACGTACGTACGTACGTACGTACGTACGTACGTACGTACGT"
+    off = np.array([0, 40], np.uint64)
+    call = np.zeros(1, np.uint32)
+    params = k2g.ClassifyParams(0.0, 0, 0, 0, 0)
+    st = k2g.lib().k2g_classify_host(db.h, bases, None, off.ctypes.data, 1, ctypes.byref(params),
+                                     call.ctypes.data, None, None, None, None, None)
+    assert st == 0
+    db.close()
