@@ -2,7 +2,8 @@
 the reference classify's runs on a protein table (tests/golden/protein.json,
 made by tests/golden/make_protein.py): through k2g_classify, every kraken
 line and taxon read count; through the classify drop-in, stdout and reports
-byte for byte."""
+byte for byte.  Collected after the nucleotide GPU tests and before
+test_zz_no_alloc."""
 import ctypes
 import gzip
 import json
