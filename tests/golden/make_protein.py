@@ -33,7 +33,8 @@ import reads as readsets  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref")
 
-# tag -> (classify flags, read set)
+# tag -> (classify flags, read set); tags starting "pm_" use db_pm, the
+# protein table built with -M (subsampled minimizers: skipped lookups)
 RUNS = {
     "p_se": (["-T", "0", "-g", "2", "-R", "x", "-K"], "p_se"),
     "p_se_conf": (["-T", "0.2", "-g", "1", "-n", "-R", "x"], "p_se"),
@@ -42,6 +43,8 @@ RUNS = {
     "p_edge": (["-T", "0", "-g", "0", "-R", "x"], "p_edge"),
     "p_minqual": (["-Q", "25", "-T", "0", "-g", "2", "-R", "x", "-K"], "p_se"),
     "p_pe_minqual": (["-P", "-Q", "20", "-g", "1", "-R", "x"], "p_pe"),
+    "pm_se": (["-T", "0", "-g", "1", "-R", "x", "-K"], "p_se"),
+    "pm_pe": (["-P", "-T", "0.02", "-g", "1", "-R", "x"], "p_pe"),
 }
 
 
@@ -156,6 +159,15 @@ def main():
                         "-H", os.path.join(out, "hash.k2d"), "-t", os.path.join(out, "taxo.k2d"),
                         "-o", os.path.join(out, "opts.k2d"), "-n", tdir, "-m", mp, "-p", "4"],
                        stdin=f, capture_output=True, check=True)
+    # db_pm: the same library with -M, a maximum capacity of half the table
+    outm = os.path.join(HERE, "db_pm")
+    os.makedirs(outm, exist_ok=True)
+    with open(lib, "rb") as f:
+        subprocess.run([os.path.join(REF, "build_db"), "-k", "15", "-l", "12", "-X", "-c", str(cap),
+                        "-M", str(cap // 2), "-H", os.path.join(outm, "hash.k2d"),
+                        "-t", os.path.join(outm, "taxo.k2d"), "-o", os.path.join(outm, "opts.k2d"),
+                        "-n", tdir, "-m", mp, "-p", "4"],
+                       stdin=f, capture_output=True, check=True)
     manifest = {"capacity": cap, "estimate": est, "library": hashlib.sha256(
         open(lib, "rb").read()).hexdigest(), "runs": {}, "reads": {}}
     for key in ("p_se", "p_pe", "p_edge"):
@@ -163,8 +175,10 @@ def main():
         manifest["reads"][key] = [hashlib.sha256(open(p, "rb").read()).hexdigest() for p in paths]
     for tag, (args, key) in RUNS.items():
         paths = write_reads(key, os.path.join(work, "reads"))
-        cmd = [os.path.join(REF, "classify"), "-H", f"{out}/hash.k2d", "-t", f"{out}/taxo.k2d",
-               "-o", f"{out}/opts.k2d", "-p", "4"] + list(args)
+        db = "db_pm" if tag.startswith("pm_") else "db_p"
+        dbd = os.path.join(HERE, db)
+        cmd = [os.path.join(REF, "classify"), "-H", f"{dbd}/hash.k2d", "-t", f"{dbd}/taxo.k2d",
+               "-o", f"{dbd}/opts.k2d", "-p", "4"] + list(args)
         rep = os.path.join(work, tag + ".report")
         if "-R" in cmd:
             cmd[cmd.index("-R") + 1] = rep
@@ -173,7 +187,7 @@ def main():
         if os.path.exists(rep):
             with open(rep, "rb") as f, open(os.path.join(HERE, "runs", tag + ".report"), "wb") as g:
                 g.write(f.read())
-        manifest["runs"][tag] = {"args": args, "reads": key, "db": "db_p",
+        manifest["runs"][tag] = {"args": args, "reads": key, "db": db,
                                  "sha256": hashlib.sha256(r.stdout).hexdigest()}
     with open(os.path.join(HERE, "protein.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)

@@ -42,10 +42,10 @@ def tx_check(tmp_path_factory):
 def test_core_matches_reference_runs(tx_check, tag, run, tmp_path):
     params, flags = parse_args(run["args"])
     files = make_protein.write_reads(run["reads"], str(tmp_path))
-    r = subprocess.run([tx_check, os.path.join(GOLDEN, "db_p"), str(params["confidence"]),
+    r = subprocess.run([tx_check, os.path.join(GOLDEN, run["db"]), str(params["confidence"]),
                         str(params["min_hit_groups"]), str(int(params["quick"])),
                         str(params["min_quality"]), *files], capture_output=True, check=True)
-    taxo = golden_db("db_p").taxo
+    taxo = golden_db(run["db"]).taxo
     reads = make_protein.read_set(run["reads"])
     m1, m2 = reads if params["paired"] else (reads, None)
     lines = []

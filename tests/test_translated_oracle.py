@@ -88,7 +88,7 @@ def _batch(key):
 def test_translated_runs(tag, run):
     from test_oracle_golden import _runs_of
     params, flags = parse_args(run["args"])
-    g = golden_db("db_p")
+    g = golden_db(run["db"])
     o = g.opts
     assert not o.dna_db
     orc = oracle.Oracle(g.hash.cells, g.hash.capacity, g.hash.key_bits, g.hash.value_bits,

@@ -32,10 +32,10 @@ with open(os.path.join(GOLDEN, "protein.json")) as _f:
 def test_device_lines_match_reference(tag, run):
     params, flags = parse_args(run["args"])
     b = _batch(run["reads"])
-    db = k2g.Database.open(os.path.join(GOLDEN, "db_p"))
+    db = k2g.Database.open(os.path.join(GOLDEN, run["db"]))
     r = classify_batch(db, b, params)
     assert r.status == 0
-    taxo = golden_db("db_p").taxo
+    taxo = golden_db(run["db"]).taxo
     lines = [kraken_line(int(r.call[i]), b.headers[i], b.lens[i], r.runs_of(i), taxo, b.paired,
                          names=flags["names"], quick=params["quick"]) for i in range(b.n_frags)]
     want = golden_output(tag)
@@ -55,7 +55,7 @@ def test_device_lines_match_reference(tag, run):
 def test_dropin_outputs_match_reference(tag, run, tmp_path):
     from kraken2_gb300 import build as k2build
     k2g.lib()
-    d = os.path.join(GOLDEN, "db_p")
+    d = os.path.join(GOLDEN, run["db"])
     files = make_protein.write_reads(run["reads"], str(tmp_path / "in"))
     args = list(run["args"])
     report = str(tmp_path / "report.txt")
