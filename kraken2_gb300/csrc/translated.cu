@@ -32,7 +32,7 @@ struct TxArgs {
   unsigned long long *hits_used;
   uint32_t *status;
   uint8_t *frames;        // per thread: frame_bytes
-  uint32_t *maps;         // per thread: 2 * map_cap
+  uint32_t *maps;         // per thread: 3 * map_cap (keys, counts, occupied slots)
   uint32_t frame_cap, frame_bytes, map_cap;
   uint64_t max_len;       // longest mate the scratch holds
   uint32_t node_count;
@@ -42,8 +42,9 @@ __global__ void translated_kernel(TxArgs a) {
   const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   uint8_t *frames = a.frames + tid * a.frame_bytes;
-  uint32_t *mk = a.maps + tid * 2ull * a.map_cap;
-  tx::TaxonMap map{mk, mk + a.map_cap, a.map_cap, 0};
+  uint32_t *mk = a.maps + tid * 3ull * a.map_cap;
+  for (uint32_t i = 0; i < a.map_cap; i++) mk[i] = 0;   // empty keys, once per thread
+  tx::TaxonMap map{mk, mk + a.map_cap, mk + 2ull * a.map_cap, a.map_cap, 0};
   const uint64_t per = a.p.paired ? 2 : 1;
   for (uint64_t f = tid; f < a.n_frags; f += stride) {
     const uint64_t o0 = a.seq_off[f * per], o1 = a.seq_off[f * per + 1];
@@ -141,7 +142,7 @@ k2g_status classify_translated(const k2g_db *db, const k2g_reads *reads,
   uint64_t cap = 16;
   while (cap < 2 * std::min(lookups, taxa)) cap <<= 1;
   a.map_cap = (uint32_t)cap;
-  const uint64_t per_thread = a.frame_bytes + 8ull * a.map_cap;
+  const uint64_t per_thread = a.frame_bytes + 12ull * a.map_cap;
   int sms = 0;
   K2G_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, db->device));
   constexpr uint64_t kScratchBudget = 2ull << 30;

@@ -161,12 +161,14 @@ K2G_HD bool is_ancestor(const uint32_t *parent, uint32_t a, uint32_t b) {
   return b == a;
 }
 
-// Open-addressing taxon -> count map in caller scratch (cap a power of two).
+// Open-addressing taxon -> count map in caller scratch (cap a power of two;
+// key[] all zero before first use).  slot[0, n) lists the occupied slots, so
+// clearing and walking the map cost the taxa it holds, not its capacity.
 struct TaxonMap {
-  uint32_t *key, *val;
+  uint32_t *key, *val, *slot;
   uint32_t cap, n;
   K2G_HD void clear() {
-    for (uint32_t i = 0; i < cap; i++) key[i] = 0;
+    for (uint32_t i = 0; i < n; i++) key[slot[i]] = 0;
     n = 0;
   }
   K2G_HD bool add(uint32_t t) {   // false when full
@@ -179,7 +181,7 @@ struct TaxonMap {
       if (!key[i]) {
         key[i] = t;
         val[i] = 1;
-        n++;
+        slot[n++] = i;
         return true;
       }
     }
@@ -202,12 +204,13 @@ K2G_HD uint32_t resolve_tree(const TaxonMap &m, const uint32_t *parent, uint64_t
                              double confidence) {
   uint32_t max_taxon = 0, max_score = 0;
   const uint32_t required = (uint32_t)ceil(confidence * (double)total);
-  for (uint32_t i = 0; i < m.cap; i++) {
-    if (!m.key[i]) continue;
-    const uint32_t t = m.key[i];
+  for (uint32_t a = 0; a < m.n; a++) {
+    const uint32_t t = m.key[m.slot[a]];
     uint32_t score = 0;
-    for (uint32_t j = 0; j < m.cap; j++)
-      if (m.key[j] && is_ancestor(parent, m.key[j], t)) score += m.val[j];
+    for (uint32_t b = 0; b < m.n; b++) {
+      const uint32_t j = m.slot[b];
+      if (is_ancestor(parent, m.key[j], t)) score += m.val[j];
+    }
     if (score > max_score) {
       max_score = score;
       max_taxon = t;
@@ -218,8 +221,10 @@ K2G_HD uint32_t resolve_tree(const TaxonMap &m, const uint32_t *parent, uint64_t
   max_score = m.get(max_taxon);
   while (max_taxon && max_score < required) {
     max_score = 0;
-    for (uint32_t i = 0; i < m.cap; i++)
-      if (m.key[i] && is_ancestor(parent, max_taxon, m.key[i])) max_score += m.val[i];
+    for (uint32_t b = 0; b < m.n; b++) {
+      const uint32_t j = m.slot[b];
+      if (is_ancestor(parent, max_taxon, m.key[j])) max_score += m.val[j];
+    }
     if (max_score >= required) return max_taxon;
     max_taxon = parent[max_taxon];
   }

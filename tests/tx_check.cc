@@ -68,7 +68,7 @@ int main(int argc, char **argv) {
     if (p.paired && r2.read(s2) < 0) break;
   }
   std::vector<uint8_t> frames;
-  std::vector<uint32_t> mkey, mval;
+  std::vector<uint32_t> mkey, mval, mslot;
   for (size_t i = 0; i < s1.size(); i++) {
     const uint8_t *mates[2] = {reinterpret_cast<const uint8_t *>(s1.seq_at(i)),
                                p.paired ? reinterpret_cast<const uint8_t *>(s2.seq_at(i)) : nullptr};
@@ -83,7 +83,8 @@ int main(int argc, char **argv) {
     while (mcap < 2 * (2 * (lens[0] + lens[1]) + 32)) mcap <<= 1;
     mkey.assign(mcap, 0);
     mval.assign(mcap, 0);
-    k2g::tx::TaxonMap map{mkey.data(), mval.data(), mcap, 0};
+    mslot.assign(mcap, 0);
+    k2g::tx::TaxonMap map{mkey.data(), mval.data(), mslot.data(), mcap, 0};
     std::vector<std::pair<uint32_t, uint32_t>> runs;
     auto lookup = [&](uint64_t key) {
       return ko_get(cells, cap, (int)kb, (int)vb, key);
