@@ -862,37 +862,42 @@ def barrier(pg):
     torch.cuda.synchronize()
 
 
-def random_sector_rate(wl, n_loads: int = 1 << 31) -> float:
-    """Random 32-byte loads/s over the resident table (k2g_sector_gather):
-    the ceiling for a lookup stream, measured on the same memory."""
+GATHER_SWEEP = [(d, w) for w in (32, 64, 128) for d in (1, 4, 8, 16)]
+
+
+def random_sector_rate(wl, n_loads: int = 1 << 30) -> dict:
+    """Random loads/s over the resident table (k2g_sector_gather), swept over
+    loads in flight per thread and load width: the ceiling for a lookup
+    stream, measured on the same memory.  Each point is the best of three
+    event-timed launches; the result keeps every point and the best rate of
+    32-byte sectors (random_sectors_per_s), the unit lookups are counted in."""
     torch = wl.torch
     sink = torch.zeros(1, dtype=torch.int32, device=wl.dev)
     st = wl.stream.cuda_stream
-    wl.db.sector_gather(n_loads // 8, sink.data_ptr(), st)
-    threads = torch.cuda.get_device_properties(wl.dev).multi_processor_count * 16 * 256
-    per = -(-(-(-n_loads // threads)) // 4) * 4      # the kernel's rounding
-    issued = per * threads
-    best = 0.0
-    for _ in range(3):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(wl.stream)
-        wl.db.sector_gather(n_loads, sink.data_ptr(), st)
-        b.record(wl.stream)
-        b.synchronize()
-        best = max(best, issued / (a.elapsed_time(b) / 1e3))
-    return best
+    sweep = []
+    for depth, nbytes in GATHER_SWEEP:
+        wl.db.sector_gather(n_loads // 16, sink.data_ptr(), st, depth, nbytes)
+        best = 0.0
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(wl.stream)
+            issued = wl.db.sector_gather(n_loads, sink.data_ptr(), st, depth, nbytes)
+            b.record(wl.stream)
+            b.synchronize()
+            best = max(best, issued / (a.elapsed_time(b) / 1e3))
+        sweep.append({"depth": depth, "bytes": nbytes, "g_loads_per_s": round(best / 1e9, 2)})
+    best32 = max(p["g_loads_per_s"] for p in sweep if p["bytes"] == 32)
+    return {"random_sectors_per_s": best32 * 1e9, "sweep": sweep}
 
 
-def profiled_dram_bytes_per_read() -> float | None:
-    """DRAM bytes per read of the classification step kernel, from the
-    committed ncu summary (a 'dram_bytes_per_read = X' line)."""
-    path = os.path.join(ROOT, "profiles", "pipe_step_kernel_150bp.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.strip().startswith("dram_bytes_per_read ="):
-            return float(line.split("=")[1].split()[0])
-    return None
+# DRAM bytes per 150 bp read of the classification step, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over every beat of one call)
+# of the 2 GB-table / 5M-read case of this workload:
+#   python bench.py --scale 0.05 --profile  under
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#       --clock-control none -k regex:pipe_step -s <beats of the first call> -c <beats of one call>
+# Traffic grows in proportion to the reads, so it scales to a full call.
+DRAM_BYTES_PER_READ = 7713.0
 
 
 def value_counts_run(wl: Workload, reps: int = 5) -> dict:
@@ -1067,14 +1072,14 @@ def run_ours(args, log):
 
     # roofline of the dominant kernel (the classify launch of each batch)
     peak, peak_kind = hbm_peak()
-    rs_loads_s = random_sector_rate(wl)
+    gather = random_sector_rate(wl)
+    rs_loads_s = gather["random_sectors_per_s"]
     kern_reads = sum(n for n, _ in call_ms)
     kern_ms = sum(ms for _, ms in call_ms)
     achieved = bytes_per_read * kern_reads / (kern_ms / 1e3) / 1e9
     traffic = None
-    dram_per_read = profiled_dram_bytes_per_read()
-    if dram_per_read:
-        traffic = round(dram_per_read * kern_reads / max(len(call_ms), 1))
+    if DRAM_BYTES_PER_READ:
+        traffic = round(DRAM_BYTES_PER_READ * kern_reads / max(len(call_ms), 1))
 
     # CPU baseline: the oracle restatement with every host thread
     threads = os.cpu_count() or 1
@@ -1141,6 +1146,9 @@ def run_ours(args, log):
                      "frac_of_random_sector": round(achieved / (rs_loads_s * 32 / 1e9), 4),
                      "sectors_per_s": round(sectors_per_read * kern_reads / (kern_ms / 1e3) / 1e9, 3),
                      "random_sectors_per_s": round(rs_loads_s / 1e9, 3),
+                     "frac_sectors_of_random": round(sectors_per_read * kern_reads / (kern_ms / 1e3)
+                                                     / rs_loads_s, 4),
+                     "gather_sweep": gather["sweep"],
                      "kernel_ms_per_launch": round(kern_ms / max(len(call_ms), 1), 3),
                      "reads_per_launch": int(kern_reads / max(len(call_ms), 1))},
         "cpu_baseline": {"value": round(rate * 60 / 1e6, 3), "unit": "Mreads/min",

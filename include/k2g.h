@@ -298,12 +298,16 @@ k2g_status k2g_host_free(void *ptr);
 
 /* ---- diagnostics (no counterpart in the reference) */
 
-/* Issues at least n_loads random 32-byte loads spread uniformly over the
- * table's cells (each thread rounds its share up to a multiple of 4) and
- * writes nothing unless a data-dependent sentinel matches (d_sink: 4 device
- * bytes).  Timing it on `stream` gives the random-sector rate that bounds
- * k2g_lookup / k2g_classify on this table. */
-k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint32_t *d_sink, void *stream);
+/* Issues at least n_loads random loads spread uniformly over the table's
+ * cells and writes nothing unless a data-dependent sentinel matches (d_sink:
+ * 4 device bytes).  A load is `bytes` = 32 (one sector), 64 (two adjacent
+ * sectors) or 128 (one line, shared by 4 lanes) bytes, each 32-byte sector
+ * fetched by one 256-bit load; every thread keeps `depth` (1, 2, 4, 8, 16)
+ * loads in flight.  *issued (may be NULL) = loads actually issued (shares are
+ * rounded up).  Timing it on `stream` gives the random-access rate that
+ * bounds k2g_lookup / k2g_classify on this table. */
+k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint32_t depth, uint32_t bytes,
+                             uint64_t *issued, uint32_t *d_sink, void *stream);
 
 /* Number of kernels this library has launched in this process so far. */
 uint64_t k2g_kernel_launches(void);

@@ -123,7 +123,7 @@ def lib():
             "k2g_build_insert": [vp, vp, vp, u64, i32, vp],
             "k2g_build_sequences": [vp, vp, vp, vp, u64, u64, u64, i32, C.POINTER(u64)],
             "k2g_sample_minimizers": [vp, vp, vp, u64, C.c_uint32, vp, u64, C.POINTER(u64)],
-            "k2g_sector_gather": [vp, u64, vp, vp],
+            "k2g_sector_gather": [vp, u64, C.c_uint32, C.c_uint32, C.POINTER(u64), vp, vp],
             "k2g_classify_static": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams),
                                     C.POINTER(Results), vp],
             "k2g_counters_create": [vp, C.POINTER(vp)],
@@ -230,9 +230,14 @@ class Database:
         check(lib().k2g_lookup_host(self.h, keys.ctypes.data, vals.ctypes.data, len(keys)))
         return vals
 
-    def sector_gather(self, n_loads: int, d_sink: int, stream: int = 0):
-        """Random 32-byte loads over the table (random-access ceiling probe)."""
-        check(lib().k2g_sector_gather(self.h, n_loads, d_sink, stream))
+    def sector_gather(self, n_loads: int, d_sink: int, stream: int = 0, depth: int = 4,
+                      nbytes: int = 32) -> int:
+        """Random loads over the table (random-access ceiling probe); returns
+        the number of loads issued."""
+        issued = C.c_uint64(0)
+        check(lib().k2g_sector_gather(self.h, n_loads, depth, nbytes, C.byref(issued), d_sink,
+                                      stream))
+        return int(issued.value)
 
     def scan(self, d_bases: int, d_seq_off: int, n_seqs: int, d_mins: int, d_ambig: int,
              stream: int = 0):

@@ -655,27 +655,32 @@ extern "C" k2g_status k2g_lookup(const k2g_db *db, const uint64_t *d_keys, uint3
   return K2G_OK;
 }
 
-// Random 32-byte sector gathers over the table's own cells: the access
-// pattern of a lookup without its hashing and compare, timed by callers to
-// get the random-access ceiling that lookups are measured against.  Each
-// thread keeps kGatherDepth independent loads in flight.
-constexpr int kGatherDepth = 4;
-
-__global__ void sector_gather_kernel(const uint4 *cells, uint64_t n_sectors, uint64_t per_thread,
+// Random gathers over the table's own cells: the access pattern of a lookup
+// without its hashing and compare, timed by callers to get the random-access
+// ceiling that lookups are measured against.  Each thread keeps D independent
+// loads in flight; a load is NSEC consecutive 32-byte sectors (one 256-bit
+// load each), or with LINE a 128-byte line loaded by 4 consecutive lanes.
+template <int D, int NSEC, bool LINE>
+__global__ void sector_gather_kernel(const uint32_t *cells, uint64_t n_units, uint64_t per_thread,
                                      uint64_t seed, uint32_t *sink) {
   const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t who = LINE ? tid >> 2 : tid;
+  const uint32_t sub = LINE ? (uint32_t)(threadIdx.x & 3) : 0u;
   uint32_t acc = 0;
-  for (uint64_t it = 0; it < per_thread; it += kGatherDepth) {
-    uint4 v[kGatherDepth][2];
+  for (uint64_t it = 0; it < per_thread; it += D) {
+    Sector v[D][NSEC];
 #pragma unroll
-    for (int u = 0; u < kGatherDepth; u++) {
-      const uint64_t h = murmur3((tid << 24) ^ (it + u) ^ seed);
-      const uint4 *p = cells + 2 * __umul64hi(h, n_sectors);
-      v[u][0] = __ldg(p);
-      v[u][1] = __ldg(p + 1);
+    for (int u = 0; u < D; u++) {
+      const uint64_t h = murmur3((who << 24) ^ (it + u) ^ seed);
+      const uint64_t unit = __umul64hi(h, n_units);
+      const uint64_t cell = LINE ? unit * 32 + sub * 8 : unit * (8 * NSEC);
+#pragma unroll
+      for (int w = 0; w < NSEC; w++) v[u][w] = load_sector(cells, cell + 8 * w);
     }
 #pragma unroll
-    for (int u = 0; u < kGatherDepth; u++) acc ^= v[u][0].x ^ v[u][1].w;
+    for (int u = 0; u < D; u++)
+#pragma unroll
+      for (int w = 0; w < NSEC; w++) acc ^= v[u][w].lo.x ^ v[u][w].hi.w;
   }
   if (acc == 0x5eed5eedu) *sink = acc;   // keeps the loads live
 }
@@ -700,19 +705,42 @@ extern "C" k2g_status k2g_lookup_host(const k2g_db *db, const uint64_t *keys, ui
   return s;
 }
 
-extern "C" k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint32_t *d_sink,
+template <int D>
+static void launch_gather(uint32_t bytes, const uint32_t *cells, uint64_t units, uint64_t per,
+                          unsigned blocks, uint32_t *sink, cudaStream_t st) {
+  const uint64_t seed = 0x9E3779B97F4A7C15ull;
+  if (bytes == 32) sector_gather_kernel<D, 1, false><<<blocks, 256, 0, st>>>(cells, units, per, seed, sink);
+  else if (bytes == 64) sector_gather_kernel<D, 2, false><<<blocks, 256, 0, st>>>(cells, units, per, seed, sink);
+  else sector_gather_kernel<D, 1, true><<<blocks, 256, 0, st>>>(cells, units, per, seed, sink);
+}
+
+extern "C" k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint32_t depth,
+                                        uint32_t bytes, uint64_t *issued, uint32_t *d_sink,
                                         void *stream) {
   if (!db || !d_sink) return fail(K2G_ERR_ARG, "null argument");
-  const uint64_t n_sectors = db->capacity / 8;   // whole 32-byte sectors of cells
-  if (!n_loads || !n_sectors) return K2G_OK;
+  if (depth != 1 && depth != 2 && depth != 4 && depth != 8 && depth != 16)
+    return fail(K2G_ERR_ARG, "depth must be 1, 2, 4, 8 or 16");
+  if (bytes != 32 && bytes != 64 && bytes != 128) return fail(K2G_ERR_ARG, "bytes must be 32, 64 or 128");
+  const uint64_t n_units = db->capacity / (bytes / 4);   // whole units of cells
+  if (issued) *issued = 0;
+  if (!n_loads || !n_units) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   const uint64_t threads = (uint64_t)sm_count(db->device) * 16 * 256;
-  uint64_t per = (n_loads + threads - 1) / threads;
-  per = (per + kGatherDepth - 1) / kGatherDepth * kGatherDepth;
-  sector_gather_kernel<<<(unsigned)(threads / 256), 256, 0, (cudaStream_t)stream>>>(
-      reinterpret_cast<const uint4 *>(db->d_cells), n_sectors, per, 0x9E3779B97F4A7C15ull, d_sink);
+  const uint64_t loaders = bytes == 128 ? threads / 4 : threads;
+  uint64_t per = (n_loads + loaders - 1) / loaders;
+  per = (per + depth - 1) / depth * depth;
+  const unsigned blocks = (unsigned)(threads / 256);
+  const cudaStream_t st = (cudaStream_t)stream;
+  switch (depth) {
+    case 1: launch_gather<1>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
+    case 2: launch_gather<2>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
+    case 4: launch_gather<4>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
+    case 8: launch_gather<8>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
+    default: launch_gather<16>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
+  }
   note_launches();
   K2G_CUDA_TRY(cudaGetLastError());
+  if (issued) *issued = per * loaders;
   return K2G_OK;
 }
 

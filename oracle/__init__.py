@@ -45,10 +45,13 @@ MATE_BORDER = 0xFFFFFFFFFFFFFFFF
 AMBIGUOUS = 0xFFFFFFFFFFFFFFFD
 
 
-def build():
+def build(ref_src: str | None = None):
+    """Builds liboracle.so; with `ref_src` (or the REF_SRC environment
+    variable) naming the reference's src/ directory, also the reference
+    programs in _ref/."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_src = "/root/reference/src"
-    if os.path.isdir(ref_src):
+    ref_src = ref_src or os.environ.get("REF_SRC")
+    if ref_src and os.path.isdir(ref_src):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
 
 
