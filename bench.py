@@ -629,124 +629,528 @@ def _oracle_calls(wl, cells, bases, off, n_frags, paired, params):
     return calls
 
 
-def paired_and_uneven_run(log) -> dict:
-    """Paired 2 x 150 bp reads and an uneven-length mix on a 2 GB table
-    (0.5e9 cells, load 0.7): the batched path against the plain GPU form,
-    with oracle parity on a sample."""
-    import torch
-    cfg = Config(0.05)
-    cfg.n_reads = 100_000
-    wl = Workload(cfg, 0, log=lambda *a: None)
-    k2g = wl.k2g
-    st = wl.stream.cuda_stream
-    g = torch.Generator(device=wl.dev).manual_seed(21)
-    lut = torch.tensor(list(b"ACGT"), dtype=torch.uint8, device=wl.dev)
-    cells, _ = wl.db.download()
-    out = {"table": "0.5e9 cells (2 GB) at load 0.7, 50000 taxa"}
+def capped_taxonomy(n: int, max_depth: int, seed: int) -> np.ndarray:
+    """Random recursive tree (parent < child, root 1) whose depth stays at
+    most max_depth: each node attaches to a uniformly chosen earlier node
+    that is not yet at the depth limit."""
+    rng = np.random.default_rng(seed)
+    parent = np.zeros(n, np.uint64)
+    depth = np.zeros(n, np.int64)
+    depth[1] = 1
+    open_ = [1]
+    for i in range(2, n):
+        while True:
+            j = int(rng.integers(0, len(open_)))
+            p_ = open_[j]
+            if depth[p_] < max_depth:
+                break
+            open_[j] = open_[-1]
+            open_.pop()
+        parent[i] = p_
+        depth[i] = depth[p_] + 1
+        open_.append(i)
+    return parent
 
-    # -- 10M pairs of 2 x 150 bp, fragment length ~N(300, 50), 1% substitutions
-    n_pairs, L = 10_000_000, 150
-    frag = torch.clamp(torch.normal(300.0, 50.0, (n_pairs,), generator=g, device=wl.dev), 150, 600).long()
-    start = torch.randint(0, wl.src.numel() - 700, (n_pairs,), generator=g, device=wl.dev)
-    ar = torch.arange(L, device=wl.dev)
-    bases = torch.empty(n_pairs * 2 * L + 16, dtype=torch.uint8, device=wl.dev)
-    step = 2_000_000
+
+def leaves_of(parent: np.ndarray) -> np.ndarray:
+    has_child = np.zeros(len(parent), bool)
+    has_child[parent[2:].astype(np.int64)] = True
+    ids = np.arange(len(parent))
+    return ids[(~has_child) & (ids >= 1)]
+
+
+ACGT = np.frombuffer(b"ACGT", np.uint8)
+
+
+def _revcomp_dev(torch, seq):
+    """Reverse complement of a uint8 tensor of ACGT rows (last dim)."""
+    lut = torch.zeros(256, dtype=torch.uint8, device=seq.device)
+    for a_, b_ in (b"AT", b"TA", b"CG", b"GC"):
+        lut[a_] = b_
+    return lut[seq.long()].flip(-1)
+
+
+def _bits_for(n: int) -> int:
+    b = 1
+    while (1 << b) < n:
+        b += 1
+    return b
+
+
+def _small_opts(k2g, min_hash: int = 0):
+    return k2g.IndexOptions(35, 31, spaced_mask(SEED_TEMPLATE), TOGGLE, 1, 1, min_hash)
+
+
+def build_library_db(k2g, genomes: np.ndarray, glen: int, taxa: np.ndarray, parent: np.ndarray,
+                     max_bytes: int | None, log, batch_genomes: int = 1000):
+    """build_kraken2_db.sh's two steps on the GPU: estimate_capacity over a
+    1/16 sample (-n 64), capacity = (estimate + 8192) / 0.7, and, where that
+    exceeds max_bytes (kraken2-build --max-db-size), build_db -M: the table
+    is max_bytes / 4 cells and minimizers hashing below
+    (1 - max / required) * UINT64_MAX are left out (src/build_db.cc:78-84).
+    Then the order-exact build of every genome (-B 16384 -b 1024).  Returns
+    (db, build description)."""
+    n_g = len(taxa)
+    vb = _bits_for(len(parent))
+    probe = k2g.Database.create(_small_opts(k2g), 64, 32 - vb, vb, parent)
+    sample = np.zeros(0, np.uint64)
+    t0 = time.time()
+    for g0 in range(0, n_g, batch_genomes):
+        g1 = min(n_g, g0 + batch_genomes)
+        off = np.arange(g1 - g0 + 1, dtype=np.uint64) * glen
+        keys = probe.sample_minimizers(genomes[g0 * glen:g1 * glen], off, 64,
+                                       keys_cap=(g1 - g0) * glen // 16)
+        sample = np.union1d(sample, keys)
+    probe.close()
+    estimate = int(len(sample)) * 1024 // 64 + 8192
+    required = int(estimate / 0.7)
+    capacity, min_hash = required, 0
+    if max_bytes and max_bytes < required * 4:
+        capacity = max_bytes // 4
+        frac = capacity / required
+        min_hash = int((1.0 - frac) * 18446744073709551615.0)
+    db = k2g.Database.create(_small_opts(k2g, min_hash), capacity, 32 - vb, vb, parent)
+    pairs = 0
+    for g0 in range(0, n_g, batch_genomes):
+        g1 = min(n_g, g0 + batch_genomes)
+        off = np.arange(g1 - g0 + 1, dtype=np.uint64) * glen
+        pairs += db.build_sequences(genomes[g0 * glen:g1 * glen], off, taxa[g0:g1], 16384, 1024, True)
+    size = int(db.info().size)
+    log(f"library db: {n_g} genomes x {glen} bp, estimate {estimate}, capacity {capacity}, "
+        f"size {size} ({size / capacity:.3f}), {time.time() - t0:.1f}s")
+    return db, {"genomes": n_g, "genome_bp": glen, "taxa": len(parent) - 1, "value_bits": vb,
+                "key_bits": 32 - vb, "estimate": estimate, "capacity": capacity,
+                "table_gb": round(capacity * 4 / 1e9, 3), "size": size,
+                "load": round(size / capacity, 4), "min_hash": min_hash,
+                "max_db_size": max_bytes, "pairs_inserted": pairs,
+                "build_s": round(time.time() - t0, 2)}
+
+
+class TableOracle:
+    """The oracle over a host copy of a GPU table (parity checks only)."""
+
+    def __init__(self, db, parent, min_hash=0):
+        import oracle
+        inf = db.info()
+        self.cells, _ = db.download()
+        self.o = oracle.Oracle(self.cells, inf.capacity, inf.key_bits, inf.value_bits, parent,
+                               oracle.index_opts(35, 31, spaced_mask(SEED_TEMPLATE), TOGGLE, 1,
+                                                 min_hash))
+        self.inf = inf
+
+    def classify(self, bases: bytes, off: np.ndarray, n: int, params, paired: bool):
+        calls, hg, nr, runs, base = self.o.classify(
+            bases, None, off.astype(np.uint64), n, threads=os.cpu_count() or 1,
+            confidence=params.confidence, min_hit_groups=params.min_hit_groups, paired=paired)
+        return calls, hg, nr, runs, base
+
+
+def _host_runs(bufs, n):
+    return (bufs["call"][:n].cpu().numpy().view(np.uint32), bufs["hg"][:n].cpu().numpy().view(np.uint32),
+            bufs["hoff"][:n].cpu().numpy().view(np.uint64), bufs["hlen"][:n].cpu().numpy().view(np.uint32),
+            bufs["runs"].cpu().numpy().view(np.uint64))
+
+
+def _gather_runs(runs: np.ndarray, start: np.ndarray, count: np.ndarray) -> np.ndarray:
+    """runs[start[i] : start[i] + count[i]] for every i, concatenated."""
+    count = count.astype(np.int64)
+    total = int(count.sum())
+    first = np.cumsum(count) - count
+    idx = np.repeat(start.astype(np.int64), count) + (np.arange(total) - np.repeat(first, count))
+    return runs[idx]
+
+
+def _parity(gpu, oracle_out, n) -> dict:
+    """Calls, hit groups and hit lists of the GPU against the oracle."""
+    call, hg, hoff, hlen, runs = gpu
+    ocalls, ohg, onr, oruns, obase = oracle_out
+    bad_calls = int((call[:n].astype(np.uint64) != ocalls[:n]).sum())
+    bad_hg = int((hg[:n].astype(np.int64) != ohg[:n]).sum())
+    glen = hlen[:n].astype(np.int64)
+    olen = onr[:n].astype(np.int64)
+    same_len = glen == olen
+    bad_hl = int((~same_len).sum())
+    keep = np.nonzero(same_len)[0]
+    g = _gather_runs(runs, hoff[keep], glen[keep])
+    o = _gather_runs(oruns, obase[keep], olen[keep])
+    ocode = o["code"].astype(np.uint64)
+    # device codes are 32-bit; the oracle writes the special codes 64 bits wide
+    ocode = np.where(ocode > np.uint64(0xFFFFFFFF), ocode & np.uint64(0xFFFFFFFF), ocode)
+    diff = ((g >> np.uint64(32)) != ocode) | ((g & np.uint64(0xFFFFFFFF)) != o["count"].astype(np.uint64))
+    owner = np.repeat(np.arange(len(keep)), glen[keep])
+    bad_hl += int(len(np.unique(owner[diff])))
+    return {"call_mismatches_vs_oracle": bad_calls, "hit_group_mismatches": bad_hg,
+            "hitlist_mismatches": bad_hl}
+
+
+def _classify_dev(k2g, db, bases_t, off_t, n, max_len, total, params, bufs, runs_cap, mode,
+                  st, frag_base=0):
+    rd = k2g.Reads(d_bases=bases_t.data_ptr(), d_quals=None, d_seq_off=off_t.data_ptr(), n_frags=n,
+                   max_seq_len=max_len, total_bases=total, d_frag_block=None, frag_base=frag_base)
+    res = _results(k2g, bufs, runs_cap)
+    db.classify(rd, params, res, mode=mode, stream=st)
+    return rd, res
+
+
+def small_db_run(log) -> dict:
+    """The small-database configuration: a 200-node taxonomy (depth <= 8),
+    50 leaf genomes of 100 kb whose siblings share 30% of their sequence at
+    2% divergence, built on the GPU (k=35, l=31, 7 spaced positions; table
+    about 10 MB, so L2-resident), and 110k single-end 150 bp reads (100k from
+    the genomes with 1% substitutions, 10k random), confidence 0, minimum hit
+    groups 2.  Timed resident, against the L2 random-sector rate measured on
+    the same table; every read checked against the oracle."""
+    import torch
+    import kraken2_gb300 as k2g
+    rng = np.random.default_rng(31)
+    parent = capped_taxonomy(200, 8, 31)
+    lv = leaves_of(parent)
+    chosen = rng.choice(lv, 50, replace=False)
+    glen, shared = 100_000, 30_000
+    seg = {}
+    genomes = np.empty(50 * glen, np.uint8)
+    for i, t in enumerate(chosen):
+        p_ = int(parent[t])
+        if p_ not in seg:
+            seg[p_] = ACGT[rng.integers(0, 4, shared)]
+        s_ = seg[p_].copy()
+        mut = rng.random(shared) < 0.02
+        s_[mut] = ACGT[rng.integers(0, 4, int(mut.sum()))]
+        genomes[i * glen:i * glen + shared] = s_
+        genomes[i * glen + shared:(i + 1) * glen] = ACGT[rng.integers(0, 4, glen - shared)]
+    db, binfo = build_library_db(k2g, genomes, glen, chosen.astype(np.uint32), parent, None, log)
+    n_src, n_rnd, L = 100_000, 10_000, 150
+    gi = rng.integers(0, 50, n_src)
+    st_ = rng.integers(0, glen - L + 1, n_src)
+    reads = genomes[(gi * glen + st_)[:, None] + np.arange(L)[None, :]]
+    mut = rng.random(reads.shape) < 0.01
+    reads[mut] = ACGT[rng.integers(0, 4, int(mut.sum()))]
+    reads = np.concatenate([reads, ACGT[rng.integers(0, 4, (n_rnd, L))]])
+    reads = reads[rng.permutation(len(reads))]
+    n = len(reads)
+    host = reads.reshape(-1).tobytes()
+    off = np.arange(n + 1, dtype=np.uint64) * L
+    dev = torch.device("cuda", 0)
+    b_t = torch.from_numpy(np.frombuffer(host + b"\0" * 16, np.uint8).copy()).to(dev)
+    o_t = torch.from_numpy(off.view(np.int64).copy()).to(dev)
+    runs_cap = n * (L + 2) + 8
+    bufs = _gpu_buffers(torch, n, runs_cap, len(parent))
+    params = k2g.ClassifyParams(0.0, 2, 0, 0, 0)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    out = {"workload": "200-node taxonomy (depth <= 8), 50 x 100 kb genomes (siblings share 30% "
+                       "at 2% divergence), 100k x 150 bp reads at 1% substitutions + 10k random",
+           "build": binfo}
+    times = {}
+    for name, mode in (("batched", k2g.MODE_PIPELINED), ("plain", k2g.MODE_PLAIN)):
+        reps = 50
+        _classify_dev(k2g, db, b_t, o_t, n, L, n * L, params, bufs, runs_cap, mode, st)
+        torch.cuda.synchronize(dev)
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record()
+        for _ in range(reps):
+            _classify_dev(k2g, db, b_t, o_t, n, L, n * L, params, bufs, runs_cap, mode, st)
+        b_.record()
+        torch.cuda.synchronize(dev)
+        times[name] = a_.elapsed_time(b_) / 1e3 / reps
+    _classify_dev(k2g, db, b_t, o_t, n, L, n * L, params, bufs, runs_cap, k2g.MODE_PIPELINED, st)
+    torch.cuda.synchronize(dev)
+    gpu = _host_runs(bufs, n)
+    orc = TableOracle(db, parent)
+    t0 = time.perf_counter()
+    oo = orc.classify(host, off, n, params, False)
+    cpu_s = time.perf_counter() - t0
+    par = _parity(gpu, oo, n)
+    # algorithmic bytes against the L2 random-sector rate on this table
+    sink = torch.zeros(1, dtype=torch.int32, device=dev)
+    best = 0.0
+    for depth in (4, 8, 16):
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            issued = db.sector_gather(1 << 28, sink.data_ptr(), st, depth, 32)
+            e1.record()
+            e1.synchronize()
+            best = max(best, issued / (e0.elapsed_time(e1) / 1e3))
+    sect = _sectors_per_read(orc, host, n, L)
+    runs_per_read = float(gpu[3].mean())
+    bpr = 32 * sect + L + 8 + 4 + 4 + 8 + 4 + 8 * runs_per_read
+    rate = n / times["batched"]
+    out.update({
+        "reads": n, "mreads_min": round(rate * 60 / 1e6, 1),
+        "plain_mreads_min": round(n / times["plain"] * 60 / 1e6, 1),
+        "plain_form": "one MODE_PLAIN launch per call (one thread per read)",
+        "batched_over_plain": round(times["plain"] / times["batched"], 3),
+        "ms_per_call": round(times["batched"] * 1e3, 4),
+        "roofline": {"bound": "l2", "sectors_per_read": round(sect, 3),
+                     "bytes_per_read": round(bpr, 1),
+                     "l2_random_sectors_per_s": round(best / 1e9, 2),
+                     "sectors_per_s": round(sect * rate / 1e9, 3),
+                     "frac_sectors_of_l2_random": round(sect * rate / best, 4)},
+        "cpu_baseline": {"mreads_min": round(n / cpu_s * 60 / 1e6, 2), "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"all {n} reads"},
+        "parity": {"reads": n, **par}})
+    del b_t, o_t, bufs
+    db.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def _sectors_per_read(orc: "TableOracle", host: bytes, n: int, L: int, sample: int = 20_000) -> float:
+    """32-byte sectors a reference Get walks per read (host replay of every
+    LOOKUP key of the first `sample` reads)."""
+    import oracle
+    keys = []
+    opts = orc.o.opts
+    for i in range(min(n, sample)):
+        m, a_m = oracle.scan(opts, host[i * L:(i + 1) * L])
+        prev = None
+        for x, amb in zip(m, a_m):
+            if amb:
+                continue
+            if x != prev:
+                keys.append(int(x))
+            prev = x
+    keys = np.array(keys, np.uint64)
+    inf = orc.inf
+    if orc.o.opts.min_hash:
+        keys = keys[murmur3_np(keys) >= np.uint64(orc.o.opts.min_hash)]
+    sectors, _ = probe_sectors(orc.cells, inf.capacity, inf.key_bits, inf.value_bits, keys)
+    return float(sectors.sum()) / min(n, sample)
+
+
+def mutation_tree_genomes(torch, parent: np.ndarray, glen: int, seed: int, dev):
+    """Genomes of every taxonomy node from a seeded ancestral-mutation tree:
+    the root's is uniform random, every other node's is its parent's with
+    uniform substitutions at a rate drawn from U(0.5%, 5%) for that edge
+    (parent < child, so one pass in node order).  One row per node."""
+    g = torch.Generator(device=dev).manual_seed(seed)
+    lut = torch.from_numpy(ACGT.copy()).to(dev)
+    n = len(parent)
+    G = torch.empty((n, glen), dtype=torch.uint8, device=dev)
+    G[1] = lut[torch.randint(0, 4, (glen,), generator=g, device=dev).long()]
+    rates = np.random.default_rng(seed).uniform(0.005, 0.05, n)
+    for i in range(2, n):
+        row = G[int(parent[i])].clone()
+        hit = torch.rand(glen, generator=g, device=dev) < float(rates[i])
+        row[hit] = lut[torch.randint(0, 4, (int(hit.sum()),), generator=g, device=dev).long()]
+        G[i] = row
+    return G
+
+
+def _pairs_dev(torch, G, pick, n_pairs, L, g, dev, subs=0.01):
+    """n_pairs fragments of length ~N(300, 50) (clipped to [L, 600]) from the
+    genomes' rows `pick`: mate 1 the fragment's first L bases, mate 2 the
+    reverse complement of its last L, each with uniform substitutions."""
+    lut = torch.from_numpy(ACGT.copy()).to(dev)
+    glen = G.shape[1]
+    frag = torch.clamp(torch.normal(300.0, 50.0, (n_pairs,), generator=g, device=dev), L, 600).long()
+    row = pick[torch.randint(0, len(pick), (n_pairs,), generator=g, device=dev)]
+    start = (torch.rand(n_pairs, generator=g, device=dev) * (glen - frag + 1).double()).long()
+    ar = torch.arange(L, device=dev)
+    out = torch.empty(n_pairs * 2 * L + 16, dtype=torch.uint8, device=dev)
+    out[n_pairs * 2 * L:] = 0
+    step = 1_000_000
     for p0 in range(0, n_pairs, step):
         p1 = min(n_pairs, p0 + step)
-        m1 = wl.src[start[p0:p1, None] + ar[None, :]]
-        m2 = wl.src[(start[p0:p1] + frag[p0:p1] - L)[:, None] + ar[None, :]]
-        bases[p0 * 2 * L:p1 * 2 * L] = torch.stack([m1, m2], 1).reshape(-1)
-    _substitute(torch, bases[:n_pairs * 2 * L], 0.01, g, lut)
-    bases[n_pairs * 2 * L:] = 0
+        r = row[p0:p1, None]
+        m1 = G[r, start[p0:p1, None] + ar[None, :]]
+        m2 = _revcomp_dev(torch, G[r, (start[p0:p1] + frag[p0:p1] - L)[:, None] + ar[None, :]])
+        out[p0 * 2 * L:p1 * 2 * L] = torch.stack([m1, m2], 1).reshape(-1)
+    hit = torch.rand(n_pairs * 2 * L, generator=g, device=dev) < subs
+    body = out[:n_pairs * 2 * L]
+    body[hit] = lut[torch.randint(0, 4, (int(hit.sum()),), generator=g, device=dev).long()]
+    return out
+
+
+def _uneven_dev(torch, G, pick, lens: np.ndarray, g, dev, subs=0.04, indel=0.01):
+    """Reads of the given template lengths from the genomes' rows `pick`,
+    with uniform substitutions and indels (half insertions of a random base
+    after a template base, half deletions of a template base), so read
+    lengths differ from template lengths.  Returns (bases, offsets)."""
+    lut = torch.from_numpy(ACGT.copy()).to(dev)
+    glen = G.shape[1]
+    n = len(lens)
+    chunks, offs = [], [np.zeros(1, np.int64)]
+    total = 0
+    step = 100_000
+    for r0 in range(0, n, step):
+        r1 = min(n, r0 + step)
+        ln = torch.from_numpy(lens[r0:r1]).to(dev)
+        row = pick[torch.randint(0, len(pick), (r1 - r0,), generator=g, device=dev)]
+        start = (torch.rand(r1 - r0, generator=g, device=dev) * (glen - ln + 1).double()).long()
+        first = torch.cumsum(ln, 0) - ln
+        m = int(ln.sum())
+        within = torch.arange(m, device=dev) - torch.repeat_interleave(first, ln)
+        tmpl = G[torch.repeat_interleave(row, ln), torch.repeat_interleave(start, ln) + within]
+        u = torch.rand(m, generator=g, device=dev)
+        copies = torch.ones(m, dtype=torch.long, device=dev)
+        copies[u < indel / 2] = 0                           # deletion
+        copies[(u >= indel / 2) & (u < indel)] = 2          # insertion after this base
+        rd = torch.repeat_interleave(tmpl, copies)
+        # the second copy of an inserted base becomes a random base
+        ends = torch.cumsum(copies, 0) - 1
+        ins = ends[copies == 2]
+        rd[ins] = lut[torch.randint(0, 4, (len(ins),), generator=g, device=dev).long()]
+        hit = torch.rand(len(rd), generator=g, device=dev) < subs
+        rd[hit] = lut[torch.randint(0, 4, (int(hit.sum()),), generator=g, device=dev).long()]
+        per_read = torch.zeros(r1 - r0, dtype=torch.long, device=dev)
+        per_read.index_add_(0, torch.repeat_interleave(torch.arange(r1 - r0, device=dev), ln), copies)
+        chunks.append(rd)
+        offs.append(total + np.cumsum(per_read.cpu().numpy()))
+        total += int(per_read.sum())
+    bases = torch.cat(chunks + [torch.zeros(16, dtype=torch.uint8, device=dev)])
+    return bases, np.concatenate(offs).astype(np.int64)
+
+
+def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
+                parity_uneven: int = 1_000_000) -> dict:
+    """The mid-size database (5,000-node taxonomy of depth <= 12; 2,000
+    genomes of 2 Mb from a seeded ancestral-mutation tree at 0.5-5%
+    divergence per edge; built on the GPU into a 2 GB table, the way
+    kraken2-build --max-db-size 2000000000 caps it) and the two read sets on
+    it: 10M pairs of 2 x 150 bp (fragments ~N(300, 50), 1% substitutions,
+    confidence 0.1), and 1M log-normal reads (mean 5 kb, 150 bp - 50 kb)
+    interleaved with 5M of 150 bp, all with 4% substitutions and 1% indels,
+    classified in one call.  Each is autotuned, then timed with its reads
+    resident, against the plain GPU form, and checked against the oracle."""
+    import torch
+    import kraken2_gb300 as k2g
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    parent = capped_taxonomy(5_000, 12, 41)
+    lv = leaves_of(parent)
+    rng = np.random.default_rng(41)
+    chosen = np.sort(rng.choice(lv, min(2_000, len(lv)), replace=False))
+    glen = 2_000_000
+    t0 = time.time()
+    G = mutation_tree_genomes(torch, parent, glen, 41, dev)
+    torch.cuda.synchronize(dev)
+    log(f"mutation tree: {len(parent)} genomes x {glen} bp in {time.time() - t0:.1f}s")
+    pick = torch.from_numpy(chosen.astype(np.int64)).to(dev)
+    lib = G[pick].cpu().numpy().reshape(-1)
+    db, binfo = build_library_db(k2g, lib, glen, chosen.astype(np.uint32), parent, 2_000_000_000, log)
+    del lib
+    out = {"db": {"workload": "5,000-node taxonomy (depth <= 12), 2,000 x 2 Mb genomes from a "
+                              "seeded ancestral-mutation tree (0.5-5% substitutions per edge), "
+                              "built on the GPU capped at 2 GB (kraken2-build --max-db-size)",
+                  **binfo}}
+    orc = TableOracle(db, parent, binfo["min_hash"])
+    g = torch.Generator(device=dev).manual_seed(43)
+
+    # -- paired 2 x 150 bp
+    L = 150
+    bases = _pairs_dev(torch, G, pick, n_pairs, L, g, dev)
     params = k2g.ClassifyParams(0.1, 2, 0, 1, 0)
     batch = 2_500_000
-    off = torch.arange(2 * batch + 1, dtype=torch.int64, device=wl.dev) * L
+    off = torch.arange(2 * batch + 1, dtype=torch.int64, device=dev) * L
     runs_cap = batch * (2 * L + 2) + 8
-    buf = _gpu_buffers(torch, batch, runs_cap, cfg.nodes)
-    res = _results(k2g, buf, runs_cap)
+    bufs = _gpu_buffers(torch, batch, runs_cap, len(parent))
 
     def run_pairs(mode, per_launch, sync):
-        t0 = time.perf_counter()
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record()
         for b0 in range(0, n_pairs, per_launch):
             n = min(per_launch, n_pairs - b0)
-            rd = k2g.Reads(d_bases=bases.data_ptr() + b0 * 2 * L, d_quals=None,
-                           d_seq_off=off.data_ptr(), n_frags=n, max_seq_len=L,
-                           total_bases=n * 2 * L, d_frag_block=None, frag_base=b0)
-            wl.db.classify(rd, params, res, mode=mode, stream=st)
+            v = bases[b0 * 2 * L:]
+            _classify_dev(k2g, db, v, off, n, L, n * 2 * L, params, bufs, runs_cap, mode, st, b0)
             if sync:
-                wl.stream.synchronize()
-        torch.cuda.synchronize()
-        return time.perf_counter() - t0
+                torch.cuda.current_stream(dev).synchronize()
+        b_.record()
+        torch.cuda.synchronize(dev)
+        return a_.elapsed_time(b_) / 1e3
 
     run_pairs(k2g.MODE_PIPELINED, batch, False)
+    t_default = run_pairs(k2g.MODE_PIPELINED, batch, False)
+    default = db.tuning(1, 0).as_dict()
+    rd, res = _classify_dev(k2g, db, bases, off, batch, L, batch * 2 * L, params, bufs, runs_cap,
+                            k2g.MODE_PIPELINED, st)
+    chosen_t, _ = db.autotune(rd, params, res, trials=2, stream=st)
     t_batched = run_pairs(k2g.MODE_PIPELINED, batch, False)
-    t_plain = run_pairs(k2g.MODE_PLAIN, 10_000, True)     # one launch per 10,000-pair reader batch
-    ns = 20_000
-    run_pairs(k2g.MODE_PIPELINED, batch, False)          # leaves the last batch's calls
-    rd = k2g.Reads(d_bases=bases.data_ptr(), d_quals=None, d_seq_off=off.data_ptr(), n_frags=ns,
-                   max_seq_len=L, total_bases=ns * 2 * L, d_frag_block=None, frag_base=0)
-    wl.db.classify(rd, params, res, mode=k2g.MODE_PIPELINED, stream=st)
-    torch.cuda.synchronize()
-    gcalls = buf["call"][:ns].cpu().numpy().view(np.uint32).astype(np.uint64)
-    ocalls = _oracle_calls(wl, cells, bases[:ns * 2 * L].cpu().numpy().tobytes(),
-                           np.arange(2 * ns + 1, dtype=np.uint64) * L, ns, True, params)
+    t_plain_call = run_pairs(k2g.MODE_PLAIN, batch, False)      # one plain launch per call
+    t_plain_block = run_pairs(k2g.MODE_PLAIN, 10_000, True)     # one launch per 10,000-pair batch
+    ns = min(parity_pairs, batch)
+    _classify_dev(k2g, db, bases, off, ns, L, ns * 2 * L, params, bufs, runs_cap,
+                  k2g.MODE_PIPELINED, st)
+    torch.cuda.synchronize(dev)
+    gpu = _host_runs(bufs, ns)
+    host = bases[:ns * 2 * L].cpu().numpy().tobytes()
+    oo = orc.classify(host, np.arange(2 * ns + 1, dtype=np.uint64) * L, ns, params, True)
     out["paired_2x150"] = {
-        "pairs": n_pairs, "confidence": 0.1, "fragment_len": "N(300, 50)", "substitutions": 0.01,
-        "mreads_min": round(n_pairs / t_batched * 60 / 1e6, 3),
-        "plain_mreads_min": round(n_pairs / t_plain * 60 / 1e6, 3),
-        "plain_form": "one synchronous launch per 10,000-pair reader batch",
-        "batched_over_plain": round(t_plain / t_batched, 3),
-        "parity": {"pairs": ns, "call_mismatches_vs_oracle": int((gcalls != ocalls).sum())}}
-    del bases, buf, res, off, frag, start
+        "pairs": n_pairs, "confidence": 0.1, "fragment_len": "N(300, 50), mate 2 reverse-complemented",
+        "substitutions": 0.01, "call_pairs": batch,
+        "mreads_min": round(n_pairs / t_batched * 60 / 1e6, 1),
+        "default_mreads_min": round(n_pairs / t_default * 60 / 1e6, 1),
+        "tuning": {"default": default, "chosen": chosen_t.as_dict(),
+                   "gain": round(t_default / t_batched, 3)},
+        "plain_mreads_min": round(n_pairs / t_plain_call * 60 / 1e6, 1),
+        "plain_form": "one MODE_PLAIN launch per 2.5M-pair call",
+        "batched_over_plain": round(t_plain_call / t_batched, 3),
+        "plain_block_mreads_min": round(n_pairs / t_plain_block * 60 / 1e6, 1),
+        "plain_block_form": "one synchronous MODE_PLAIN launch per 10,000-pair reader batch",
+        "batched_over_plain_block": round(t_plain_block / t_batched, 3),
+        "parity": {"pairs": ns, **_parity(gpu, oo, ns)}}
+    log(f"paired: {out['paired_2x150']['mreads_min']} Mreads/min")
+    del bases, off, bufs
     torch.cuda.empty_cache()
 
-    # -- uneven lengths: 1M log-normal (mean 5 kb, 150 bp - 50 kb) + 5M x 150 bp
-    rng = np.random.default_rng(23)
+    # -- uneven lengths with indels, one call
     sigma = 0.8
     lens = np.concatenate([np.clip(rng.lognormal(np.log(5000) - sigma * sigma / 2, sigma, 1_000_000),
                                    150, 50_000).astype(np.int64), np.full(5_000_000, 150, np.int64)])
     rng.shuffle(lens)
+    seqs, offs = _uneven_dev(torch, G, pick, lens, g, dev)
+    del G
+    torch.cuda.empty_cache()
     n = len(lens)
-    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
     tot = int(offs[-1])
-    starts = torch.from_numpy(rng.integers(0, wl.src.numel() - 50_001, n)).to(wl.dev)
-    ln_t = torch.from_numpy(lens).to(wl.dev)
-    seqs = torch.empty(tot + 16, dtype=torch.uint8, device=wl.dev)
-    seqs[tot:] = 0
-    for r0 in range(0, n, 200_000):
-        r1 = min(n, r0 + 200_000)
-        l = ln_t[r0:r1]
-        first = torch.cumsum(l, 0) - l
-        within = torch.arange(int(l.sum()), device=wl.dev) - torch.repeat_interleave(first, l)
-        seqs[offs[r0]:offs[r1]] = wl.src[torch.repeat_interleave(starts[r0:r1], l) + within]
-    _substitute(torch, seqs[:tot], 0.04, g, lut)
-    d_off = torch.from_numpy(offs).to(wl.dev)
+    rl = np.diff(offs)
+    d_off = torch.from_numpy(offs).to(dev)
     params = k2g.ClassifyParams(0.1, 2, 0, 0, 0)
     runs_cap = tot + 2 * n + 8
-    buf = _gpu_buffers(torch, n, runs_cap, cfg.nodes)
-    res = _results(k2g, buf, runs_cap)
-    rd = k2g.Reads(d_bases=seqs.data_ptr(), d_quals=None, d_seq_off=d_off.data_ptr(), n_frags=n,
-                   max_seq_len=int(lens.max()), total_bases=tot, d_frag_block=None, frag_base=0)
-    t_batched = _time_classify(wl, rd, res, params, k2g.MODE_PIPELINED, st)
-    calls_b = buf["call"].cpu().numpy().copy()
-    t_plain = _time_classify(wl, rd, res, params, k2g.MODE_PLAIN, st)
-    same = bool(np.array_equal(calls_b, buf["call"].cpu().numpy()))
-    # oracle parity on a sample: the first 1,000 long and 4,000 short reads
-    idx = np.concatenate([np.nonzero(lens > 150)[0][:1000], np.nonzero(lens == 150)[0][:4000]])
-    host = seqs[:tot].cpu().numpy()
-    sb = b"".join(host[offs[i]:offs[i + 1]].tobytes() for i in idx)
-    soff = np.concatenate([[0], np.cumsum(lens[idx])]).astype(np.uint64)
-    ocalls = _oracle_calls(wl, cells, sb, soff, len(idx), False, params)
-    gcalls = calls_b.view(np.uint32)[idx].astype(np.uint64)
+    bufs = _gpu_buffers(torch, n, runs_cap, len(parent))
+    max_len = int(rl.max())
+
+    def one_call(mode):
+        _classify_dev(k2g, db, seqs, d_off, n, max_len, tot, params, bufs, runs_cap, mode, st)
+        torch.cuda.synchronize(dev)
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record()
+        _classify_dev(k2g, db, seqs, d_off, n, max_len, tot, params, bufs, runs_cap, mode, st)
+        b_.record()
+        torch.cuda.synchronize(dev)
+        return a_.elapsed_time(b_) / 1e3
+
+    cls = k2g.length_class(tot, n)
+    default = db.tuning(0, cls).as_dict()
+    t_default = one_call(k2g.MODE_PIPELINED)
+    rd, res = _classify_dev(k2g, db, seqs, d_off, n, max_len, tot, params, bufs, runs_cap,
+                            k2g.MODE_PIPELINED, st)
+    chosen_t, _ = db.autotune(rd, params, res, trials=1, stream=st)
+    t_batched = one_call(k2g.MODE_PIPELINED)
+    calls_b = bufs["call"][:n].cpu().numpy().copy()
+    t_plain = one_call(k2g.MODE_PLAIN)
+    same = bool(np.array_equal(calls_b, bufs["call"][:n].cpu().numpy()))
+    one_call(k2g.MODE_PIPELINED)
+    # oracle parity on the first reads of the call (long and short mixed)
+    ns = min(parity_uneven, n)
+    gpu = _host_runs(bufs, ns)
+    host = seqs[:int(offs[ns])].cpu().numpy().tobytes()
+    oo = orc.classify(host, offs[:ns + 1].astype(np.uint64), ns, params, False)
     out["uneven_lengths"] = {
-        "reads": n, "bases": tot, "lengths": "1M log-normal mean 5 kb (150 bp - 50 kb) + 5M x 150 bp",
-        "errors": "4% substitutions", "single_launch": True,
-        "mreads_min": round(n / t_batched * 60 / 1e6, 3), "gbases_per_s": round(tot / t_batched / 1e9, 2),
-        "plain_mreads_min": round(n / t_plain * 60 / 1e6, 3),
-        "plain_form": "one launch, one thread per read (no work stealing)",
+        "reads": n, "bases": tot,
+        "lengths": "1M log-normal mean 5 kb (150 bp - 50 kb) + 5M x 150 bp, interleaved",
+        "errors": "4% substitutions, 1% indels (half insertions, half deletions)",
+        "single_call": True, "length_class": cls,
+        "mreads_min": round(n / t_batched * 60 / 1e6, 1), "gbases_per_s": round(tot / t_batched / 1e9, 2),
+        "default_gbases_per_s": round(tot / t_default / 1e9, 2),
+        "tuning": {"default": default, "chosen": chosen_t.as_dict(), "gain": round(t_default / t_batched, 3)},
+        "plain_mreads_min": round(n / t_plain * 60 / 1e6, 1),
+        "plain_form": "one MODE_PLAIN launch, one thread per read (no work stealing, no pieces)",
         "batched_over_plain": round(t_plain / t_batched, 3), "plain_calls_identical": same,
-        "parity": {"reads": int(len(idx)), "call_mismatches_vs_oracle": int((gcalls != ocalls).sum())}}
-    del seqs, buf, res, d_off, wl
+        "parity": {"reads": ns, "long_reads": int((rl[:ns] > 300).sum()), **_parity(gpu, oo, ns)}}
+    log(f"uneven: {out['uneven_lengths']['gbases_per_s']} Gbases/s")
+    del seqs, bufs, d_off
+    db.close()
     torch.cuda.empty_cache()
     return out
 
@@ -1111,7 +1515,8 @@ def run_ours(args, log):
     if not args.skip_configs:
         del runner
         torch.cuda.empty_cache()
-        configs = paired_and_uneven_run(log)
+        configs = {"small_db": small_db_run(log)}
+        configs.update(mid_db_runs(log))
         configs["build"] = build_run(log)
     e2e_rate = cfg.e2e_reads / e2e_t
 
@@ -1173,34 +1578,82 @@ def run_ours(args, log):
     return out
 
 
+class HostWorkload:
+    """The full-size workload built in host memory by the oracle alone (the
+    CPU arm never loads this repository's library): the same taxonomy, 40 GB
+    table at load 0.7 (sources' minimizers first, then random keys with 80%
+    leaf and 20% internal values, inserted on every host thread with the
+    oracle's CompareAndSet + LCA) and 150 bp reads (70% substrings of the
+    sources, 30% random), generated with host RNGs."""
+
+    def __init__(self, cfg: Config, n_reads: int, log=print):
+        import oracle
+        t0 = time.time()
+        self.cfg = cfg
+        threads = os.cpu_count() or 1
+        self.parent = random_taxonomy(cfg.nodes, 1)
+        has_child = np.zeros(cfg.nodes, bool)
+        has_child[self.parent[2:].astype(np.int64)] = True
+        ids = np.arange(cfg.nodes)
+        leaves = ids[(~has_child) & (ids >= 1)]
+        internal = ids[has_child & (ids >= 1)]
+        rng = np.random.default_rng(3)
+        self.src_taxa = rng.choice(leaves, cfg.n_src).astype(np.uint32)
+        n_src_b = cfg.n_src * cfg.src_len
+        self.src = ACGT[np.frombuffer(rng.bytes(n_src_b), np.uint8) & 3]
+        self.opts = oracle.index_opts(cfg.k, cfg.l, spaced_mask(SEED_TEMPLATE), TOGGLE)
+        self.cells = np.zeros(cfg.capacity, np.uint32)
+        self.size = oracle.fill_table(self.cells, cfg.key_bits, cfg.value_bits, self.parent,
+                                      self.opts, self.src, cfg.src_len, self.src_taxa, leaves,
+                                      internal, int(cfg.capacity * cfg.load), 4, threads)
+        L = cfg.read_len
+        hit = rng.random(n_reads) < cfg.hit_frac
+        gi = rng.integers(0, cfg.n_src, n_reads)
+        st = rng.integers(0, cfg.src_len - L + 1, n_reads)
+        reads = ACGT[np.frombuffer(rng.bytes(n_reads * L), np.uint8) & 3].reshape(n_reads, L)
+        from_src = (gi * cfg.src_len + st)[hit]
+        reads[hit] = self.src[from_src[:, None] + np.arange(L)[None, :]]
+        self.reads = reads.reshape(-1).tobytes()
+        self.n_reads = n_reads
+        self.oracle = oracle.Oracle(self.cells, cfg.capacity, cfg.key_bits, cfg.value_bits,
+                                    self.parent, self.opts)
+        log(f"host workload {time.time() - t0:.1f}s: size {self.size} / {cfg.capacity} "
+            f"({self.size / cfg.capacity:.3f}), {n_reads} reads")
+
+    def classify(self, n: int, threads: int) -> float:
+        cfg = self.cfg
+        off = np.arange(n + 1, dtype=np.uint64) * cfg.read_len
+        t0 = time.perf_counter()
+        self.oracle.classify(self.reads, None, off, n, threads=threads, confidence=cfg.confidence,
+                             min_hit_groups=cfg.min_hit_groups)
+        return time.perf_counter() - t0
+
+
 def run_reference(args, log):
-    """CPU arm: the oracle port on the host cores, same workload and metric."""
+    """CPU arm: the oracle port on the host cores, same workload and metric,
+    built on the host (no GPU, no repository library)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    import torch
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     cfg = Config(args.scale)
-    wl = Workload(cfg, 0, log=log)
-    cells, _ = wl.db.download()
     threads = os.cpu_count() or 1
-    n = min(cfg.n_reads, 200_000)
-    dt, *_ = cpu_classify(wl, cells, n, threads)
-    n = int(min(cfg.n_reads, n * args.cpu_seconds / 4 / max(dt, 1e-3), 4_000_000))
+    sample_cap = min(cfg.n_reads, 4_000_000)
+    hw = HostWorkload(cfg, sample_cap, log=log)
+    n = min(sample_cap, 200_000)
+    dt = hw.classify(n, threads)
+    n = int(min(sample_cap, n * args.cpu_seconds / 4 / max(dt, 1e-3)))
     for _ in range(args.warmup):
-        cpu_classify(wl, cells, min(n, 100_000), threads)
-    times = []
-    for _ in range(args.steps):
-        dt, *_ = cpu_classify(wl, cells, n, threads)
-        times.append(dt)
+        hw.classify(min(n, 100_000), threads)
+    times = [hw.classify(n, threads) for _ in range(args.steps)]
     t = float(np.mean(times))
     v = round(n / t * 60 / 1e6, 3)
     return {"impl": "reference", "metric": "Mreads/min at 40GB table, bit-exact", "value": v,
             "unit": "Mreads/min", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (seeded, generated on the device)",
-            "config": {"workload": cfg.workload(), "parallelism": "host threads"},
+            "data": "synthetic (seeded, generated on the host)",
+            "config": {"workload": cfg.workload(), "parallelism": "host threads",
+                       "table_build": "host, oracle CompareAndSet + LCA on every thread"},
             "cpu_baseline": {"value": v, "unit": "Mreads/min", "cores": threads, "kind": "port",
                              "sample": f"{n} reads of the workload per step"},
             "e2e": {"value": v, "unit": "Mreads/min", "h2d_bytes_per_step": 0,

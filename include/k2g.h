@@ -197,6 +197,51 @@ k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
                         const k2g_classify_params *params, k2g_results *out,
                         int mode, void *stream);
 
+/* ---- tuning (no counterpart in the reference, whose own scheduling knobs
+ * are fixed: LoadBlock(3 MiB) at src/classify.cc:527 and GetBatch's 8-key
+ * prefetch distance at src/compact_hash.h:380-392).  Each table keeps one
+ * set of values per (single-end or paired, length class) of a batch; every
+ * k2g_classify call uses the set of its batch's class.  The values change
+ * only how the work is scheduled, never a result. */
+typedef struct {
+  /* 1: K2G_MODE_PIPELINED runs scan / probe / resolve beats over
+   * sub-batches; 0: it runs the fused work-stealing kernel instead */
+  uint32_t pipeline;
+  /* table-probe blocks per 128-fragment group in a beat (1..4): the probe
+   * lanes, and so the table loads in flight, per fragment scanned */
+  uint32_t probe_split;
+  /* most bases of one pipeline sub-batch, in MiB (16..1024) */
+  uint32_t sub_batch_mb;
+  /* nominal piece length (256..8192, a power of two): single-end fragments
+   * of twice this length and more are cut into pieces that separate lanes
+   * classify, so a read of L bases gets about L / piece_len lanes */
+  uint32_t piece_len;
+  /* 1: each call's launch sequence is captured as a CUDA graph and launched
+   * as one (the last graph is kept and updated in place for a batch of the
+   * same shape); 0: the launches are issued one by one */
+  uint32_t graphs;
+} k2g_tuning;
+
+/* Length classes of a batch, by bases per fragment (mates together):
+ * 0 = short (at most 512 on average), 1 = mixed (at most 4096), 2 = long. */
+#define K2G_LEN_CLASSES 3
+
+k2g_status k2g_tuning_get(const k2g_db *db, int paired, int length_class, k2g_tuning *out);
+/* Rejects values outside the ranges above (K2G_ERR_ARG). */
+k2g_status k2g_tuning_set(k2g_db *db, int paired, int length_class, const k2g_tuning *in);
+/* Times k2g_classify (K2G_MODE_PIPELINED) on the given batch under each
+ * candidate set of values for the batch's class -- probe split and
+ * sub-batch size for short reads; pipeline or fused kernel and piece length
+ * otherwise, then the fastest with and without graph capture -- `trials`
+ * timed calls per candidate after one warm-up, keeps
+ * the fastest for that class of this table and returns it in *chosen and
+ * its time in *best_ms (either may be NULL).  The batch's outputs are
+ * written many times over; the last call leaves them as k2g_classify
+ * would.  Synchronises `stream`. */
+k2g_status k2g_autotune(k2g_db *db, const k2g_reads *reads, const k2g_classify_params *params,
+                        k2g_results *out, int trials, k2g_tuning *chosen, double *best_ms,
+                        void *stream);
+
 /* Limits of k2g_classify_static. */
 #define K2G_STATIC_MAX_FRAGS 262144u   /* fragments per call               */
 #define K2G_STATIC_MAX_LEN 512u        /* bases per sequence (mate)        */
@@ -209,7 +254,9 @@ k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
  * (K2G_ERR_ARG) more than K2G_STATIC_MAX_FRAGS fragments or max_seq_len
  * above K2G_STATIC_MAX_LEN.
  * The first call on a device resolves the scratch address and may load the
- * module, so make it before any stream capture.  All calls on one device
+ * module, so make it before any stream capture; the address is kept for the
+ * life of the process, so do not reset the device (cudaDeviceReset) while
+ * this library is in use.  All calls on one device
  * share the scratch: calls that overlap in time race, so order them on one
  * stream or with events. */
 k2g_status k2g_classify_static(const k2g_db *db, const k2g_reads *reads,

@@ -44,7 +44,26 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_kernel_launches", "k2g_classify_static", "k2g_counters_create",
            "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
            "k2g_classify_host_blocks", "k2g_server_create", "k2g_server_submit",
-           "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy", "k2g_server_sizes"]
+           "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy", "k2g_server_sizes",
+           "k2g_tuning_get", "k2g_tuning_set", "k2g_autotune"]
+
+
+class Tuning(C.Structure):
+    """k2g_tuning: scheduling values of one batch class of a table."""
+    _fields_ = [("pipeline", C.c_uint32), ("probe_split", C.c_uint32),
+                ("sub_batch_mb", C.c_uint32), ("piece_len", C.c_uint32), ("graphs", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+LEN_CLASSES = 3   # K2G_LEN_CLASSES
+
+
+def length_class(total_bases: int, n_frags: int) -> int:
+    """Batch class by bases per fragment, mates together (k2g.h)."""
+    avg = total_bases / n_frags if n_frags else 0.0
+    return 0 if avg <= 512 else (1 if avg <= 4096 else 2)
 
 
 class K2GError(RuntimeError):
@@ -138,6 +157,10 @@ def lib():
             "k2g_server_fetch": [vp, u64, vp, vp, vp, vp, C.POINTER(u64), C.POINTER(C.c_double)],
             "k2g_server_destroy": [vp],
             "k2g_server_sizes": [vp, u64, C.POINTER(u64), C.POINTER(u64)],
+            "k2g_tuning_get": [vp, i32, i32, C.POINTER(Tuning)],
+            "k2g_tuning_set": [vp, i32, i32, C.POINTER(Tuning)],
+            "k2g_autotune": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams), C.POINTER(Results),
+                             i32, C.POINTER(Tuning), C.POINTER(C.c_double), vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -248,6 +271,24 @@ class Database:
         check(lib().k2g_classify(self.h, C.byref(reads), C.byref(params), C.byref(results),
                                  mode, stream))
 
+    def tuning(self, paired: int, length_class: int) -> Tuning:
+        t = Tuning()
+        check(lib().k2g_tuning_get(self.h, int(paired), int(length_class), C.byref(t)))
+        return t
+
+    def set_tuning(self, paired: int, length_class: int, t: Tuning):
+        check(lib().k2g_tuning_set(self.h, int(paired), int(length_class), C.byref(t)))
+
+    def autotune(self, reads: Reads, params: ClassifyParams, results: Results, trials: int = 2,
+                 stream: int = 0) -> tuple[Tuning, float]:
+        """k2g_autotune: times the candidate scheduling values on this batch,
+        keeps the fastest for its class; returns (values, ms per call)."""
+        t = Tuning()
+        ms = C.c_double(0)
+        check(lib().k2g_autotune(self.h, C.byref(reads), C.byref(params), C.byref(results),
+                                 int(trials), C.byref(t), C.byref(ms), stream))
+        return t, float(ms.value)
+
     def classify_static(self, reads: Reads, params: ClassifyParams, results: Results,
                         stream: int = 0):
         """k2g_classify_static: plain classification with no device allocation."""
@@ -257,6 +298,34 @@ class Database:
     def build_insert(self, d_keys: int, d_taxids: int, n: int, ordered: bool = False,
                      stream: int = 0):
         check(lib().k2g_build_insert(self.h, d_keys, d_taxids, n, int(ordered), stream))
+
+    def build_sequences(self, bases: bytes | np.ndarray, seq_off: np.ndarray, taxids: np.ndarray,
+                        block_size: int = 16384, subblock_size: int = 1024,
+                        ordered: bool = True) -> int:
+        """k2g_build_sequences on host sequences (one batch, < 2^32 bases);
+        returns the number of (block, minimizer) pairs inserted."""
+        b = np.frombuffer(bases, np.uint8) if isinstance(bases, (bytes, bytearray)) else bases
+        b = np.ascontiguousarray(b, np.uint8)
+        off = np.ascontiguousarray(seq_off, np.uint64)
+        tx = np.ascontiguousarray(taxids, np.uint32)
+        n_keys = C.c_uint64(0)
+        check(lib().k2g_build_sequences(self.h, b.ctypes.data, off.ctypes.data, tx.ctypes.data,
+                                        len(tx), block_size, subblock_size, int(ordered),
+                                        C.byref(n_keys)))
+        return int(n_keys.value)
+
+    def sample_minimizers(self, bases: bytes | np.ndarray, seq_off: np.ndarray,
+                          sample_below: int = 1024, keys_cap: int | None = None) -> np.ndarray:
+        """k2g_sample_minimizers: the distinct sampled minimizers, ascending."""
+        b = np.frombuffer(bases, np.uint8) if isinstance(bases, (bytes, bytearray)) else bases
+        b = np.ascontiguousarray(b, np.uint8)
+        off = np.ascontiguousarray(seq_off, np.uint64)
+        cap = keys_cap or max(1024, int(off[-1] - off[0]))
+        keys = np.zeros(cap, np.uint64)
+        n = C.c_uint64(0)
+        check(lib().k2g_sample_minimizers(self.h, b.ctypes.data, off.ctypes.data, len(off) - 1,
+                                          sample_below, keys.ctypes.data, cap, C.byref(n)))
+        return keys[:n.value]
 
 
 class Counters:

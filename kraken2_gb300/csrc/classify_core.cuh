@@ -400,9 +400,8 @@ __device__ __forceinline__ void scan_segment(Lane<W> &s, Store &st, const Classi
 #pragma unroll 1
     for (int wi = 0; wi < 4; wi++) {
       const uint32_t wd = wi == 0 ? cur.x : (wi == 1 ? cur.y : (wi == 2 ? cur.z : cur.w));
-      const uint32_t lower = wd | 0x20202020u;
-      uint32_t ok = __vcmpeq4(lower, 0x61616161u) | __vcmpeq4(lower, 0x63636363u) |
-                    __vcmpeq4(lower, 0x67676767u) | __vcmpeq4(lower, 0x74747474u);
+      const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
+      uint32_t ok = acgt_bytes(wd, codes);
       if (QUAL) {
         const uint32_t qw = wi == 0 ? qc.x : (wi == 1 ? qc.y : (wi == 2 ? qc.z : qc.w));
         ok &= ~__vcmplts4(qw, c.qthr4);
@@ -411,7 +410,6 @@ __device__ __forceinline__ void scan_segment(Lane<W> &s, Store &st, const Classi
       // bytes before base 0 of the mate read as ambiguous
       const int32_t before = -(pbase + 4 * wi);
       if (before > 0) ok = before >= 4 ? 0u : (ok & (0xFFFFFFFFu << (8 * before)));
-      const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
 #pragma unroll
       for (int b = 0; b < 4; b++) {
         const uint32_t valid = (ok >> (8 * b)) & 1u;
@@ -568,38 +566,59 @@ __device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const Clas
 }
 
 // ---- resolve and write -------------------------------------------------
-template <class L, class Store>
+// ClearMap: leave the lane's map empty for its next fragment (a lane that
+// resolves only one fragment skips it).
+template <class L, class Store, bool ClearMap = true>
 __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyArgs &a) {
   const uint32_t *parent = a.parent;
   uint32_t total = s.total_tokens;
   if (a.cls.paired) total -= 1;
   // ResolveTree (src/classify.cc:710-762)
-  uint32_t max_taxon = 0, max_score = 0;
   const uint32_t required =
       (uint32_t)ceil(__dmul_rn(a.cls.confidence, (double)total));
   const int cap = st.map_cap();
+  // The map's occupied slots: with no taxon the call is 0; with one taxon t
+  // of count n, t's score is n and so is the score of each of its ancestors
+  // (no other taxon lies below them), so the climb of ResolveTree either
+  // stops at t (n >= required) or runs past the root: call = n >= required ?
+  // t : 0.  Most reads hit one taxon or none, and skip the ancestor walks.
+  uint32_t occupied = 0, t1 = 0, n1 = 0;
   for (int i = 0; i < cap; i++) {
-    uint32_t t = st.map_key(i);
-    if (!t) continue;
-    uint32_t score = 0;
-    for (uint32_t x = t; x; x = __ldg(parent + x)) score += map_get(st, x);
-    if (score > max_score) {
-      max_score = score;
-      max_taxon = t;
-    } else if (score == max_score) {
-      max_taxon = lca(parent, max_taxon, t);
+    const uint32_t t = st.map_key(i);
+    occupied += t ? 1u : 0u;
+    if (t && !t1) {
+      t1 = t;
+      n1 = st.map_cnt(i);
     }
   }
-  max_score = map_get(st, max_taxon);
-  uint32_t call = max_taxon;
-  while (call && max_score < required) {
-    max_score = 0;
+  uint32_t call = 0;
+  if (occupied == 1) {
+    call = n1 >= required ? t1 : 0u;
+  } else if (occupied > 1) {
+    uint32_t max_taxon = 0, max_score = 0;
     for (int i = 0; i < cap; i++) {
       uint32_t t = st.map_key(i);
-      if (t && is_ancestor(parent, call, t)) max_score += st.map_cnt(i);
+      if (!t) continue;
+      uint32_t score = 0;
+      for (uint32_t x = t; x; x = __ldg(parent + x)) score += map_get(st, x);
+      if (score > max_score) {
+        max_score = score;
+        max_taxon = t;
+      } else if (score == max_score) {
+        max_taxon = lca(parent, max_taxon, t);
+      }
     }
-    if (max_score >= required) break;
-    call = __ldg(parent + call);
+    max_score = map_get(st, max_taxon);
+    call = max_taxon;
+    while (call && max_score < required) {
+      max_score = 0;
+      for (int i = 0; i < cap; i++) {
+        uint32_t t = st.map_key(i);
+        if (t && is_ancestor(parent, call, t)) max_score += st.map_cnt(i);
+      }
+      if (max_score >= required) break;
+      call = __ldg(parent + call);
+    }
   }
   if (call && (int32_t)s.hit_groups < a.cls.min_hit_groups) call = 0;
   // close the last run
@@ -616,8 +635,8 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
   if (a.hitlist_off) a.hitlist_off[f] = s.run_base;
   if (a.hitlist_len) a.hitlist_len[f] = s.n_runs;
   if (call && a.taxon_reads) atomicAdd(a.taxon_reads + call, 1ull);
-  // clear this lane's map for the next fragment
-  for (int i = 0; i < cap; i++) st.map_key(i) = 0;
+  if (ClearMap && occupied)
+    for (int i = 0; i < cap; i++) st.map_key(i) = 0;
 }
 
 // The end of a piece: its runs are already in place (the last one is written

@@ -62,8 +62,8 @@ __device__ uint32_t find_cut(const ScanConst &sc, bool rc1, const uint8_t *seq,
 }
 
 // A long single-end fragment gets a contiguous range of piece slots (one
-// per nominal cut, plus one) and is cut near every kPieceLen positions.  A
-// fragment without room, or without a single usable cut, is left whole.
+// per nominal cut, plus one) and is cut near every b.piece_len positions.
+// A fragment without room, or without a single usable cut, is left whole.
 __device__ void plan_fragment(const ClassifyArgs &a, const SplitBufs &b, const ScanConst &sc,
                               uint64_t f) {
   const bool rc1 = a.scan.revcom_version != 0;
@@ -72,9 +72,10 @@ __device__ void plan_fragment(const ClassifyArgs &a, const SplitBufs &b, const S
   const bool qall = thr > 127;
   const uint32_t k = (uint32_t)sc.k;
   const uint64_t o0 = a.seq_off[f], len = a.seq_off[f + 1] - o0;
-  if (len < kSplitMinLen) return;
-  // nominal cuts at k - 1 + j * kPieceLen, the last piece keeping half that
-  const uint32_t n_cuts = (uint32_t)((len - (k - 1) - kPieceLen / 2) / kPieceLen);
+  const uint32_t piece = b.piece_len;
+  if (len < 2ull * piece) return;
+  // nominal cuts at k - 1 + j * piece, the last piece keeping half that
+  const uint32_t n_cuts = (uint32_t)((len - (k - 1) - piece / 2) / piece);
   if (!n_cuts) return;
   const unsigned long long base = atomicAdd(b.ctr, (unsigned long long)n_cuts + 1);
   if (base + n_cuts + 1 > b.pieces_cap) return;
@@ -89,7 +90,7 @@ __device__ void plan_fragment(const ClassifyArgs &a, const SplitBufs &b, const S
   uint32_t lo = k - 1, idx = 0;
   uint64_t lm = 0;
   for (uint32_t j = 1; j <= n_cuts && !whole; j++) {
-    const uint32_t c = k - 1 + j * kPieceLen;
+    const uint32_t c = k - 1 + j * piece;
     const uint32_t end = (uint32_t)min((uint64_t)c + kCutSearch, len);
     uint64_t mp = 0;
     const uint32_t p = find_cut(sc, rc1, seq, qs, thr, qall, c, end, mp);

@@ -14,8 +14,12 @@
 
 namespace k2g {
 
-constexpr uint32_t kSplitMinLen = 2048;   // fragments at least this long are cut
-constexpr uint32_t kPieceLen = 1024;      // nominal piece length
+// Nominal piece length (a runtime tuning value, k2g_tuning::piece_len): a
+// fragment of at least twice this many bases is cut into pieces of about
+// this length, so a read of L bases is classified by about L / piece_len
+// lanes.  Bounds keep a cut's search window inside its own piece.
+constexpr uint32_t kPieceLenDefault = 1024;
+constexpr uint32_t kPieceLenMin = 256, kPieceLenMax = 8192;
 constexpr uint32_t kCutSearch = 256;      // a cut is looked for within this many positions
 constexpr uint32_t kMaxEventPiece = 60000; // longest piece when hit events are requested
 
@@ -34,13 +38,16 @@ struct SplitBufs {
   uint64_t frags_cap;
   uint32_t *map_key, *map_cnt;  // merge maps, 64 entries per piece slot
   unsigned long long *ctr;      // [0] piece slots taken, [1] split fragments, [2] work counter
+  uint32_t piece_len;           // nominal piece length; fragments of 2 * piece_len bases and more are cut
 };
 
 // Slot capacities for a call of total_bases bases.
-inline uint64_t split_pieces_cap(uint64_t total_bases) {
-  return total_bases / kPieceLen + total_bases / kSplitMinLen + 16;
+inline uint64_t split_pieces_cap(uint64_t total_bases, uint32_t piece_len) {
+  return total_bases / piece_len + total_bases / (2ull * piece_len) + 16;
 }
-inline uint64_t split_frags_cap(uint64_t total_bases) { return total_bases / kSplitMinLen + 16; }
+inline uint64_t split_frags_cap(uint64_t total_bases, uint32_t piece_len) {
+  return total_bases / (2ull * piece_len) + 16;
+}
 
 // Plans the pieces of the view's long fragments (b.ctr and b.pieces must be
 // zeroed first); marks them in b.mark.

@@ -212,6 +212,22 @@ __device__ __forceinline__ uint32_t dna_code(uint32_t c) {
   return ok ? code : 0xFFu;
 }
 
+// One byte per base of a 4-byte word of ASCII bases: 0x01 where the byte is
+// A, C, G or T in either case (src/mmscanner.cc:20-46), else 0.  `codes` is
+// ((wd >> 1) ^ (wd >> 2)) & 0x03030303, each byte's 2-bit code (A 0, C 1,
+// G 2, T 3, either case).  A byte is a base exactly when its lower-case form
+// equals the letter of its own code: the letters are looked up with one byte
+// permute (the selector nibbles come out in byte order 0, 2, 1, 3, so the word
+// is permuted the same way) and compared with an exact per-byte zero test.
+__device__ __forceinline__ uint32_t acgt_bytes(uint32_t wd, uint32_t codes) {
+  const uint32_t sel = (codes | (codes >> 12)) & 0xFFFFu;
+  const uint32_t want = __byte_perm(0x74676361u, 0u, sel);        // "acgt"[code] in order 0,2,1,3
+  const uint32_t have = __byte_perm(wd | 0x20202020u, 0u, 0x3120u);
+  const uint32_t x = want ^ have;
+  const uint32_t z = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+  return __byte_perm(z, 0u, 0x3120u) >> 7;
+}
+
 // reverse_complement for revcom_version 0 (src/mmscanner.cc:210-211):
 // pairwise reversal of the whole 64-bit word, complement, low 2n bits.
 __device__ __forceinline__ uint64_t revcomp_v0(uint64_t x, uint64_t lmer_mask) {

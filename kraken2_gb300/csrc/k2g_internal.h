@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "k2g.h"
@@ -67,6 +68,29 @@ enum : uint32_t {
 
 }  // namespace k2g
 
+namespace k2g {
+// Scheduling values of one batch class (k2g_tuning).
+struct Tuning {
+  uint32_t pipeline = 1;
+  uint32_t probe_split = 2;
+  uint32_t sub_batch_mb = 256;
+  uint32_t piece_len = 1024;
+  uint32_t graphs = 0;
+};
+// Length class of a batch (K2G_LEN_CLASSES): bases per fragment, mates together.
+inline int length_class(uint64_t total_bases, uint64_t n_frags) {
+  const double avg = n_frags ? (double)total_bases / (double)n_frags : 0.0;
+  return avg <= 512.0 ? 0 : (avg <= 4096.0 ? 1 : 2);
+}
+// The values a table starts with: the pipeline for short batches, the fused
+// kernel for batches of mostly long fragments.
+inline Tuning default_tuning(int length_class) {
+  Tuning t;
+  t.pipeline = length_class == 0 ? 1u : 0u;
+  return t;
+}
+}  // namespace k2g
+
 struct k2g_db {
   int device = 0;
   uint64_t capacity = 0, size = 0, key_bits = 0, value_bits = 0, node_count = 0;
@@ -76,6 +100,15 @@ struct k2g_db {
   uint64_t *d_size = nullptr;     // device-side size counter used by builds
   k2g::DivMagic div{};
   bool owns_table = true;
+  // scheduling values per (paired, length class); guarded by tune_mu
+  mutable std::mutex tune_mu;
+  k2g::Tuning tune[2][K2G_LEN_CLASSES] = {
+      {k2g::default_tuning(0), k2g::default_tuning(1), k2g::default_tuning(2)},
+      {k2g::default_tuning(0), k2g::default_tuning(1), k2g::default_tuning(2)}};
+  k2g::Tuning tuning(bool paired, uint64_t total_bases, uint64_t n_frags) const {
+    std::lock_guard<std::mutex> lock(tune_mu);
+    return tune[paired ? 1 : 0][k2g::length_class(total_bases, n_frags)];
+  }
 
   k2g::TableView table_view() const;
   k2g::ScanView scan_view() const;

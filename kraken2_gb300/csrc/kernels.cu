@@ -280,6 +280,8 @@ struct DeviceState {
   uint32_t *merge_map = nullptr;
   uint64_t merge_map_cap = 0;
   unsigned long long *split_ctr = nullptr;
+  // executable graph of the last captured call (tuning value `graphs`)
+  cudaGraphExec_t graph_exec = nullptr;
 };
 constexpr int kStatesPerDevice = 8;   // state_for picks among them with the top three hash bits
 struct DeviceStates {
@@ -414,13 +416,14 @@ static SlowPlan slow_plan(uint64_t max_len, bool paired) {
 // Fragments per sub-batch and slot capacity for a batch of n fragments
 // holding total_bases bases.
 static void sub_batch_plan(uint64_t n, uint64_t total_bases, int per, uint64_t max_len,
-                           uint64_t &sb_frags, uint64_t &cap_slots) {
+                           uint32_t max_sub_mb, uint64_t &sb_frags, uint64_t &cap_slots) {
   // Bigger sub-batches mean more blocks per beat and a smaller tail in each
   // (256 MB measured 6% faster than 64 MB at 40 GB), but a call needs
   // several sub-batches for its roles to overlap: about a sixth of the call,
-  // between 64 and 256 MB of bases.
-  constexpr uint64_t kMinSub = 64ull << 20, kMaxSub = 256ull << 20;
-  const uint64_t target_bases = std::min(kMaxSub, std::max(kMinSub, total_bases / 6));
+  // between 64 MB (or the tuned most, if smaller) and the tuned most.
+  const uint64_t max_sub = (uint64_t)max_sub_mb << 20;
+  const uint64_t min_sub = std::min<uint64_t>(64ull << 20, max_sub);
+  const uint64_t target_bases = std::min(max_sub, std::max(min_sub, total_bases / 6));
   const double avg = n ? (double)total_bases / (double)n : 1.0;   // bases per fragment
   sb_frags = (uint64_t)std::max(1.0, target_bases / std::max(avg, 1.0));
   sb_frags = std::min<uint64_t>(sb_frags, 4ull << 20);
@@ -475,7 +478,7 @@ static PipeArgs pipe_view(const ClassifyArgs &a, const ExecCtx &c) {
 
 static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mode,
                                uint64_t max_len, uint64_t total_bases, cudaStream_t caller,
-                               const void *state_key) {
+                               const void *state_key, const Tuning &tn) {
   const int dev = db->device;
   DeviceState &ds = state_for(dev, state_key);
   std::lock_guard<std::mutex> lock(ds.mu);
@@ -486,14 +489,15 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     ds.init = true;
   }
   const int per = a0.cls.paired ? 2 : 1;
-  // The pipeline is fastest on short fragments.  A batch whose fragments
-  // average more than kLongBatchAvg bases (mates together) is mostly long
-  // fragments, which the fused persistent kernel walks in segments with work
-  // stealing; the pipeline would defer most of them to it anyway.
-  const bool pipeline = mode == K2G_MODE_PIPELINED && !long_batch(total_bases, a0.n_frags);
+  // The pipeline is fastest on short fragments.  A batch of mostly long
+  // fragments (by default: more than 512 bases per fragment, mates together)
+  // runs on the fused persistent kernel, which walks them in segments with
+  // work stealing; the pipeline would defer most of them to it anyway.
+  const bool pipeline = mode == K2G_MODE_PIPELINED && tn.pipeline;
   if (mode == K2G_MODE_PIPELINED && !pipeline) mode = K2G_MODE_PERSISTENT;
   uint64_t sb = a0.n_frags, cap_slots = 0;
-  if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, sb, cap_slots);
+  if (pipeline) sub_batch_plan(a0.n_frags, total_bases, per, max_len, tn.sub_batch_mb, sb, cap_slots);
+  const uint32_t piece = tn.piece_len;
   const SlowPlan sp = slow_plan(max_len, a0.cls.paired != 0);
   const int nctx = pipeline ? 3 : 1;
   for (int i = 0; i < nctx; i++) {
@@ -501,14 +505,7 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     if (s != K2G_OK) return s;
   }
   cudaStream_t st = ds.st;
-  K2G_CUDA_TRY(cudaEventRecord(ds.start, caller));
-  K2G_CUDA_TRY(cudaStreamWaitEvent(st, ds.start, 0));
   const uint64_t S = (a0.n_frags + sb - 1) / sb;
-  auto slow = [&](uint64_t i) -> cudaError_t {
-    const ExecCtx &c = ds.ctx[pipeline ? i % 3 : 0];
-    const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
-    return dispatch_slow(sub_view(a0, f0, n, c, sp), sp.mcap, (unsigned)(sp.threads / 128), 128, st);
-  };
   // Pipelined mode: the fragments the pipeline deferred (long ones, and
   // those whose staging or taxon map overflowed) go to the fused kernel as
   // one list after the last beat, so its work stealing spreads the long
@@ -517,18 +514,36 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
   // Long single-end fragments of that list are cut into pieces first (see
   // classify_split.h); the fused kernel then skips them, and the merge hands
   // a fragment whose piece overflowed its taxon map to the slow kernel.
-  const bool split_deferred = pipeline && !a0.cls.paired && !a0.cls.quick && max_len >= kSplitMinLen;
-  SplitBufs dspl{};
-  if (split_deferred) {
-    const uint64_t pc = split_pieces_cap(total_bases), fc = split_frags_cap(total_bases);
-    K2G_CUDA_TRY(grow(ds.split_mark, ds.split_mark_cap, std::max<uint64_t>(a0.n_frags, 1)));
+  // Persistent mode cuts long single-end fragments into pieces first, so
+  // no lane walks a long read alone; quick mode stops inside a fragment
+  // and pairs carry a mate border, so those stay whole.
+  const bool split_deferred = pipeline && !a0.cls.paired && !a0.cls.quick && max_len >= 2ull * piece;
+  const bool split = !pipeline && mode == K2G_MODE_PERSISTENT && !a0.cls.paired && !a0.cls.quick &&
+                     max_len >= 2ull * piece;
+  // every buffer is in place before the first launch (a captured sequence
+  // may not allocate)
+  SplitBufs spl{};
+  if (split_deferred || split) {
+    const uint64_t pc = split_pieces_cap(total_bases, piece), fc = split_frags_cap(total_bases, piece);
+    K2G_CUDA_TRY(grow(ds.split_mark, ds.split_mark_cap, std::max<uint64_t>(split ? sb : a0.n_frags, 1)));
     K2G_CUDA_TRY(grow(ds.pieces, ds.pieces_cap, pc));
     K2G_CUDA_TRY(grow(ds.split_frags, ds.split_frags_cap, fc));
     K2G_CUDA_TRY(grow(ds.merge_map, ds.merge_map_cap, 128 * pc));
     if (!ds.split_ctr) K2G_CUDA_TRY(cudaMalloc(&ds.split_ctr, 3 * sizeof(unsigned long long)));
-    dspl = SplitBufs{ds.split_mark, ds.pieces, pc, ds.split_frags, fc,
-                     ds.merge_map, ds.merge_map + 64 * pc, ds.split_ctr};
+    spl = SplitBufs{ds.split_mark, ds.pieces, pc, ds.split_frags, fc,
+                    ds.merge_map, ds.merge_map + 64 * pc, ds.split_ctr, piece};
   }
+  if (pipeline) {
+    K2G_CUDA_TRY(grow(ds.defer, ds.defer_cap, std::max<uint64_t>(1024, a0.n_frags)));
+    K2G_CUDA_TRY(grow(ds.defer2, ds.defer2_cap, std::max<uint64_t>(1024, a0.n_frags)));
+    if (!ds.counters) K2G_CUDA_TRY(cudaMalloc(&ds.counters, 3 * sizeof(unsigned long long)));
+  }
+  (void)sm_count(dev);   // cached before any capture
+  auto slow = [&](uint64_t i) -> cudaError_t {
+    const ExecCtx &c = ds.ctx[pipeline ? i % 3 : 0];
+    const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+    return dispatch_slow(sub_view(a0, f0, n, c, sp), sp.mcap, (unsigned)(sp.threads / 128), 128, st);
+  };
   auto deferred = [&]() -> cudaError_t {
     ClassifyArgs a = a0;
     a.in_list = ds.defer;
@@ -543,94 +558,118 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
     a.scratch_stride = sp.stride;
     cudaError_t e;
     if (split_deferred) {
-      if ((e = cudaMemsetAsync(dspl.mark, 0, a0.n_frags, st)) != cudaSuccess) return e;
-      if ((e = cudaMemsetAsync(dspl.ctr, 0, 3 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
-      if ((e = cudaMemsetAsync(dspl.pieces, 0, dspl.pieces_cap * sizeof(SplitPiece), st)) != cudaSuccess)
+      if ((e = cudaMemsetAsync(spl.mark, 0, a0.n_frags, st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(spl.ctr, 0, 3 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(spl.pieces, 0, spl.pieces_cap * sizeof(SplitPiece), st)) != cudaSuccess)
         return e;
-      if ((e = split_plan_list(a, dspl, ds.defer_cap, sm_count(dev), st)) != cudaSuccess) return e;
+      if ((e = split_plan_list(a, spl, ds.defer_cap, sm_count(dev), st)) != cudaSuccess) return e;
       ClassifyArgs pv = a;
       pv.in_list = nullptr;
-      pv.pieces = dspl.pieces;
-      pv.n_pieces = dspl.ctr;
-      pv.next_frag = dspl.ctr + 2;
-      pv.n_frags = dspl.pieces_cap;   // bounds the piece indices and sizes the launch
+      pv.pieces = spl.pieces;
+      pv.n_pieces = spl.ctr;
+      pv.next_frag = spl.ctr + 2;
+      pv.n_frags = spl.pieces_cap;   // bounds the piece indices and sizes the launch
       if ((e = dispatch_fast(pv, 1, sm_count(dev), st)) != cudaSuccess) return e;
-      a.split_mark = dspl.mark;
+      a.split_mark = spl.mark;
     }
     if ((e = dispatch_fast(a, 1, sm_count(dev), st)) != cudaSuccess) return e;
-    if (split_deferred && (e = split_merge(a, dspl, sm_count(dev), st)) != cudaSuccess) return e;
+    if (split_deferred && (e = split_merge(a, spl, sm_count(dev), st)) != cudaSuccess) return e;
     a.in_list = nullptr;
     a.split_mark = nullptr;
     return dispatch_slow(a, sp.mcap, (unsigned)(sp.threads / 128), 128, st);
   };
-
-  if (pipeline) {
-    K2G_CUDA_TRY(grow(ds.defer, ds.defer_cap, std::max<uint64_t>(1024, a0.n_frags)));
-    K2G_CUDA_TRY(grow(ds.defer2, ds.defer2_cap, std::max<uint64_t>(1024, a0.n_frags)));
-    if (!ds.counters) K2G_CUDA_TRY(cudaMalloc(&ds.counters, 3 * sizeof(unsigned long long)));
-    K2G_CUDA_TRY(cudaMemsetAsync(ds.counters, 0, 3 * sizeof(unsigned long long), st));
-    // beat t: scan t, probe t-1, resolve t-2
-    for (uint64_t t = 0; t < S + 2; t++) {
-      StepArgs sa{};
-      PipeArgs none{};
-      none.a = a0;
-      none.a.n_frags = 0;
-      sa.scan = sa.probe = sa.resolve = none;
-      auto bind = [&](uint64_t i, PipeArgs &p, uint32_t &nb) {
-        const ExecCtx &c = ds.ctx[i % 3];
-        const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
-        p = pipe_view(sub_view(a0, f0, n, c, sp), c);
-        p.a.defer_list = ds.defer;   // one list for the whole batch
-        p.a.defer_count = ds.counters + 1;
-        p.a.defer_cap = ds.defer_cap;
-        nb = (uint32_t)((n + kPipeBlock - 1) / kPipeBlock);
-      };
-      if (t < S) bind(t, sa.scan, sa.n_scan);
-      if (t >= 1 && t - 1 < S) bind(t - 1, sa.probe, sa.n_probe);
-      if (t >= 2 && t - 2 < S) bind(t - 2, sa.resolve, sa.n_resolve);
-      if (!sa.n_scan) sa.scan = sa.probe.a.n_frags ? sa.probe : sa.resolve;   // scan config for dispatch
-      if (!sa.n_scan) sa.scan.a.n_frags = 0;
-      K2G_CUDA_TRY(dispatch_pipe_step(sa, st));
-    }
-    K2G_CUDA_TRY(deferred());
-  } else {
-    // Persistent mode cuts long single-end fragments into pieces first, so
-    // no lane walks a long read alone; quick mode stops inside a fragment
-    // and pairs carry a mate border, so those stay whole.
-    const bool split = mode == K2G_MODE_PERSISTENT && !a0.cls.paired && !a0.cls.quick &&
-                       max_len >= kSplitMinLen;
-    SplitBufs spl{};
-    if (split) {
-      const uint64_t pc = split_pieces_cap(total_bases), fc = split_frags_cap(total_bases);
-      K2G_CUDA_TRY(grow(ds.split_mark, ds.split_mark_cap, std::max<uint64_t>(sb, 1)));
-      K2G_CUDA_TRY(grow(ds.pieces, ds.pieces_cap, pc));
-      K2G_CUDA_TRY(grow(ds.split_frags, ds.split_frags_cap, fc));
-      K2G_CUDA_TRY(grow(ds.merge_map, ds.merge_map_cap, 128 * pc));
-      if (!ds.split_ctr) K2G_CUDA_TRY(cudaMalloc(&ds.split_ctr, 3 * sizeof(unsigned long long)));
-      spl = SplitBufs{ds.split_mark, ds.pieces, pc, ds.split_frags, fc,
-                      ds.merge_map, ds.merge_map + 64 * pc, ds.split_ctr};
-    }
-    for (uint64_t i = 0; i < S; i++) {
-      const ExecCtx &c = ds.ctx[0];
-      const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
-      ClassifyArgs v = sub_view(a0, f0, n, c, sp);
-      K2G_CUDA_TRY(cudaMemsetAsync(c.counters, 0, 2 * sizeof(unsigned long long), st));
-      if (split) {
-        K2G_CUDA_TRY(cudaMemsetAsync(spl.ctr, 0, 3 * sizeof(unsigned long long), st));
-        K2G_CUDA_TRY(cudaMemsetAsync(spl.pieces, 0, spl.pieces_cap * sizeof(SplitPiece), st));
-        K2G_CUDA_TRY(split_plan(v, spl, sm_count(dev), st));
-        ClassifyArgs pv = v;
-        pv.pieces = spl.pieces;
-        pv.n_pieces = spl.ctr;
-        pv.next_frag = spl.ctr + 2;
-        pv.n_frags = spl.pieces_cap;   // bounds the piece indices and sizes the launch
-        K2G_CUDA_TRY(dispatch_fast(pv, 1, sm_count(dev), st));
-        v.split_mark = spl.mark;
+  // The whole launch sequence of the call; it only enqueues work on st.
+  auto sequence = [&]() -> k2g_status {
+    if (pipeline) {
+      K2G_CUDA_TRY(cudaMemsetAsync(ds.counters, 0, 3 * sizeof(unsigned long long), st));
+      // beat t: scan t, probe t-1, resolve t-2
+      for (uint64_t t = 0; t < S + 2; t++) {
+        StepArgs sa{};
+        PipeArgs none{};
+        none.a = a0;
+        none.a.n_frags = 0;
+        sa.scan = sa.probe = sa.resolve = none;
+        auto bind = [&](uint64_t i, PipeArgs &p, uint32_t &nb) {
+          const ExecCtx &c = ds.ctx[i % 3];
+          const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+          p = pipe_view(sub_view(a0, f0, n, c, sp), c);
+          p.a.defer_list = ds.defer;   // one list for the whole batch
+          p.a.defer_count = ds.counters + 1;
+          p.a.defer_cap = ds.defer_cap;
+          nb = (uint32_t)((n + kPipeBlock - 1) / kPipeBlock);
+        };
+        if (t < S) bind(t, sa.scan, sa.n_scan);
+        if (t >= 1 && t - 1 < S) bind(t - 1, sa.probe, sa.n_probe);
+        if (t >= 2 && t - 2 < S) bind(t - 2, sa.resolve, sa.n_resolve);
+        sa.split = tn.probe_split;
+        if (!sa.n_scan) sa.scan = sa.probe.a.n_frags ? sa.probe : sa.resolve;   // scan config for dispatch
+        if (!sa.n_scan) sa.scan.a.n_frags = 0;
+        K2G_CUDA_TRY(dispatch_pipe_step(sa, st));
       }
-      K2G_CUDA_TRY(dispatch_fast(v, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), st));
-      if (split) K2G_CUDA_TRY(split_merge(v, spl, sm_count(dev), st));
-      K2G_CUDA_TRY(slow(i));
+      K2G_CUDA_TRY(deferred());
+    } else {
+      for (uint64_t i = 0; i < S; i++) {
+        const ExecCtx &c = ds.ctx[0];
+        const uint64_t f0 = i * sb, n = std::min(sb, a0.n_frags - f0);
+        ClassifyArgs v = sub_view(a0, f0, n, c, sp);
+        K2G_CUDA_TRY(cudaMemsetAsync(c.counters, 0, 2 * sizeof(unsigned long long), st));
+        if (split) {
+          K2G_CUDA_TRY(cudaMemsetAsync(spl.ctr, 0, 3 * sizeof(unsigned long long), st));
+          K2G_CUDA_TRY(cudaMemsetAsync(spl.pieces, 0, spl.pieces_cap * sizeof(SplitPiece), st));
+          K2G_CUDA_TRY(split_plan(v, spl, sm_count(dev), st));
+          ClassifyArgs pv = v;
+          pv.pieces = spl.pieces;
+          pv.n_pieces = spl.ctr;
+          pv.next_frag = spl.ctr + 2;
+          pv.n_frags = spl.pieces_cap;   // bounds the piece indices and sizes the launch
+          K2G_CUDA_TRY(dispatch_fast(pv, 1, sm_count(dev), st));
+          v.split_mark = spl.mark;
+        }
+        K2G_CUDA_TRY(dispatch_fast(v, mode == K2G_MODE_PERSISTENT ? 1 : 0, sm_count(dev), st));
+        if (split) K2G_CUDA_TRY(split_merge(v, spl, sm_count(dev), st));
+        K2G_CUDA_TRY(slow(i));
+      }
     }
+    return K2G_OK;
+  };
+
+  K2G_CUDA_TRY(cudaEventRecord(ds.start, caller));
+  K2G_CUDA_TRY(cudaStreamWaitEvent(st, ds.start, 0));
+  if (tn.graphs) {
+    // The sequence captured as one graph and launched with one call.  The
+    // state keeps the last executable graph; a batch of the same shape
+    // (the same launches, other arguments) updates it in place, another
+    // shape instantiates a new one.
+    K2G_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const k2g_status s = sequence();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (s != K2G_OK) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    if (ec != cudaSuccess) return cuda_fail((int)ec, "cudaStreamEndCapture");
+    bool updated = false;
+    if (ds.graph_exec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(ds.graph_exec, g, &info) == cudaSuccess;
+      if (!updated) {
+        (void)cudaGetLastError();   // an update refused for another shape is not an error
+        cudaGraphExecDestroy(ds.graph_exec);
+        ds.graph_exec = nullptr;
+      }
+    }
+    cudaError_t ei = cudaSuccess;
+    if (!updated) ei = cudaGraphInstantiate(&ds.graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      ds.graph_exec = nullptr;
+      return cuda_fail((int)ei, "cudaGraphInstantiate");
+    }
+    K2G_CUDA_TRY(cudaGraphLaunch(ds.graph_exec, st));
+  } else {
+    const k2g_status s = sequence();
+    if (s != K2G_OK) return s;
   }
   K2G_CUDA_TRY(cudaEventRecord(ds.done, st));
   K2G_CUDA_TRY(cudaStreamWaitEvent(caller, ds.done, 0));
@@ -832,7 +871,8 @@ k2g_status k2g::classify_keyed(const k2g_db *db, const k2g_reads *reads,
     K2G_CUDA_TRY(cudaStreamSynchronize(st));
     total = ends[1] - ends[0];
   }
-  return run_classify(db, a, mode, reads->max_seq_len, total, st, state_key);
+  return run_classify(db, a, mode, reads->max_seq_len, total, st, state_key,
+                      db->tuning(params->paired != 0, total, reads->n_frags));
 }
 
 extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,

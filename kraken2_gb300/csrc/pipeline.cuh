@@ -195,6 +195,63 @@ __device__ __forceinline__ void pipe_scan_word5(ScanLane<5> &s, const PipeArgs &
   pipe_scan_emit(s, pa, c, p0 + 3, amb[3], m3 ^ c.toggle, skey, sslot, nst);
 }
 
+// The token of a k-mer that is unambiguous and emitted (pipe_scan_emit with
+// emit true and amb false): a new minimizer opens a KEY (or SKIP) group, a
+// repeat continues the open group unless that group is ambiguous.
+__device__ __forceinline__ void pipe_scan_emit_clean(ScanLane<5> &s, const PipeArgs &pa,
+                                                     const ScanConst &c, uint64_t m,
+                                                     uint64_t *skey, uint32_t *sslot, int &nst) {
+  const bool is_new = m != s.last_min;
+  s.last_min = m;
+  bool skip = false;
+  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  const bool newg = is_new || s.gkind == G_AMBIG || s.gkind == G_NONE;
+  const bool close = newg && (s.gkind != G_NONE);
+  if (close) pa.gstream[s.gbase + s.ng] = make_group(s.gkind, s.glen);
+  s.ng += close ? 1u : 0u;
+  s.glen = newg ? 1u : s.glen + 1u;
+  s.gkind = newg ? (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT) : s.gkind;
+  const bool is_key = is_new && !skip;
+  if (is_key) {
+    skey[nst * kPipeBlock] = m;
+    sslot[nst * kPipeBlock] = (uint32_t)s.ng;
+  }
+  nst += is_key ? 1 : 0;
+}
+
+// pipe_scan_word5 for a clean word: all four bases are A/C/G/T, the l-mer
+// run is already full (run + 1 >= l), the last ambiguous base is out of
+// reach (p0 - last_amb > amb_span) and all four positions emit a token.
+// Every candidate is then valid and no k-mer is ambiguous, so the run and
+// ambiguity bookkeeping and the emit bounds drop out; the state left behind
+// is the one pipe_scan_word5 leaves.
+template <bool RC1>
+__device__ __forceinline__ void pipe_scan_word5_clean(ScanLane<5> &s, const PipeArgs &pa,
+                                                      const ScanConst &c, uint32_t codes,
+                                                      uint64_t *skey, uint32_t *sslot, int &nst) {
+  uint64_t cand[4];
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const uint32_t code = (codes >> (8 * b)) & 3u;
+    s.fwd = ((s.fwd << 2) | code) & c.lmer_mask;
+    s.rc = (s.rc >> 2) | ((uint64_t)(code ^ 3u) << c.top_shift);
+    const uint64_t rcv = RC1 ? s.rc : revcomp_v0(s.fwd, c.lmer_mask);
+    cand[b] = ((s.fwd < rcv ? s.fwd : rcv) & c.smask) ^ c.toggle;
+  }
+  s.run += 4;
+  const uint64_t q1 = min64(cand[0], cand[1]), q2 = min64(q1, cand[2]), q3 = min64(q2, cand[3]);
+  const uint64_t m0 = min64(s.win.r[0], cand[0]), m1 = min64(s.win.r[1], q1),
+                 m2 = min64(s.win.r[2], q2), m3 = min64(s.win.r[3], q3);
+  s.win.r[3] = cand[3];
+  s.win.r[2] = min64(cand[2], cand[3]);
+  s.win.r[1] = min64(cand[1], s.win.r[2]);
+  s.win.r[0] = min64(cand[0], s.win.r[1]);
+  pipe_scan_emit_clean(s, pa, c, m0 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean(s, pa, c, m1 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean(s, pa, c, m2 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean(s, pa, c, m3 ^ c.toggle, skey, sslot, nst);
+}
+
 #ifndef K2G_SCAN_WORD5
 #define K2G_SCAN_WORD5 1
 #endif
@@ -274,19 +331,21 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
 #pragma unroll 1
         for (int wi = 0; wi < 4; wi++) {
           const uint32_t wd = wi == 0 ? cur.x : (wi == 1 ? cur.y : (wi == 2 ? cur.z : cur.w));
-          const uint32_t lower = wd | 0x20202020u;
-          uint32_t ok = __vcmpeq4(lower, 0x61616161u) | __vcmpeq4(lower, 0x63636363u) |
-                        __vcmpeq4(lower, 0x67676767u) | __vcmpeq4(lower, 0x74747474u);
+          const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
+          uint32_t ok = acgt_bytes(wd, codes);
           if (QUAL) {
             const uint32_t qw = wi == 0 ? qc.x : (wi == 1 ? qc.y : (wi == 2 ? qc.z : qc.w));
             ok &= ~__vcmplts4(qw, c.qthr4);
             if (c.qall) ok = 0;
           }
-          const int32_t before = -(pbase + 4 * wi);
+          const int32_t p0 = pbase + 4 * wi;
+          const int32_t before = -p0;
           if (before > 0) ok = before >= 4 ? 0u : (ok & (0xFFFFFFFFu << (8 * before)));
-          const uint32_t codes = ((wd >> 1) ^ (wd >> 2)) & 0x03030303u;
           if constexpr (W == 5 && K2G_SCAN_WORD5) {
-            pipe_scan_word5<RC1>(s, pa, c, pbase + 4 * wi, ok, codes, skey, sslot, nst);
+            const bool clean = ok == 0x01010101u && s.run + 1 >= c.l && p0 - s.last_amb > c.amb_span &&
+                               p0 >= c.k - 1 && p0 + 3 < (int32_t)s.len;
+            if (clean) pipe_scan_word5_clean<RC1>(s, pa, c, codes, skey, sslot, nst);
+            else pipe_scan_word5<RC1>(s, pa, c, p0, ok, codes, skey, sslot, nst);
           } else {
 #pragma unroll
             for (int b = 0; b < 4; b++) {
@@ -325,13 +384,9 @@ namespace k2g {
 
 // Probe: every record of a scan block, several table loads in flight per
 // thread, result stored at the record's group slot.
-// Probe blocks per scan block: each takes every kProbeSplit-th run of
-// kPipeBlock keys of the scan block's range.  Two keep more probe warps
-// resident beside the scan and resolve blocks (measured +3% at 40 GB).
-#ifndef K2G_PROBE_SPLIT
-#define K2G_PROBE_SPLIT 2
-#endif
-constexpr int kProbeSplit = K2G_PROBE_SPLIT;
+// Probe blocks per scan block (StepArgs::split, a tuning value, 1..4): each
+// takes every split-th run of kPipeBlock keys of the scan block's range.
+constexpr uint32_t kMaxProbeSplit = 4;
 
 // Probe that resolves every key's home sector in the main loop and parks
 // the keys whose walk continues (about one in five at load 0.7) in a shared
@@ -339,10 +394,10 @@ constexpr int kProbeSplit = K2G_PROBE_SPLIT;
 // their second-sector loads overlap instead of running as a divergent tail
 // of each warp (measured 11% faster per beat at 40 GB).  Probe blocks have
 // the step kernel's shared memory to themselves.
-__device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk,
-                                                      uint32_t part, unsigned char *smem) {
+__device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk, uint32_t part,
+                                                uint32_t split, unsigned char *smem) {
   constexpr int B = 4;
-  constexpr uint32_t stride = kProbeSplit * kPipeBlock;
+  const uint32_t stride = split * kPipeBlock;
   constexpr uint32_t kCap = (uint32_t)((kScanSmem - 16) / 16);
   uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem);
   uint4 *s_list = reinterpret_cast<uint4 *>(smem + 16);   // {i, walked, next lo, next hi}
@@ -488,48 +543,39 @@ __device__ __forceinline__ void pipe_resolve_body(const PipeArgs &pa, uint32_t b
     gb = pipe_gbase(pa, f);
     ng = pa.gcount[f];
     bool done = ng != 0xFFFFFFFFu;   // else deferred by the scan
+    // The group kinds select values rather than branches, so the lanes of a
+    // warp stay together: an ambiguous group is a run of A, the mate border
+    // a run of one |:|, a KEY group takes its looked-up taxon, a SKIP group
+    // taxon 0, and a CONT group the taxon of the last KEY or SKIP group.
     for (uint32_t g = 0; done && g < ng; g++) {
       const uint32_t grp = pa.gstream[gb + g];
       const uint32_t kind = grp >> kGroupLenBits, len = grp & kGroupMaxLen;
-      uint32_t taxon;
-      if (kind == G_AMBIG) {
-        emit_run(s, a, K2G_CODE_AMBIGUOUS, len);
-        s.total_tokens += len;
-        continue;
+      const bool is_key = kind == G_KEY, sets = is_key || kind == G_SKIP;
+      uint32_t tx = 0;
+      if (is_key) tx = pa.gtax[gb + g];
+      const uint32_t taxon = sets ? tx : s.cur_taxon;
+      s.cur_taxon = taxon;
+      const bool hit = is_key && tx;
+      s.hit_groups += hit ? 1u : 0u;
+      if (hit && a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
+        s.quick_stop = true;
+        break;
       }
-      if (kind == G_BORDER) {
-        emit_run(s, a, K2G_CODE_MATE_BORDER, 1);
-        s.total_tokens += 1;
-        continue;
-      }
-      if (kind == G_KEY) {
-        taxon = pa.gtax[gb + g];
-        s.cur_taxon = taxon;
-        if (taxon) {
-          s.hit_groups++;
-          if (a.cls.quick && (int32_t)s.hit_groups >= a.cls.min_hit_groups) {
-            s.quick_stop = true;
-            break;
-          }
-        }
-      } else if (kind == G_SKIP) {
-        taxon = 0;
-        s.cur_taxon = 0;
-      } else {
-        taxon = s.cur_taxon;
-      }
-      if (taxon && !map_add(st, s.distinct, taxon, len)) {
+      const bool marker = kind == G_AMBIG || kind == G_BORDER;
+      const uint32_t code = kind == G_AMBIG ? K2G_CODE_AMBIGUOUS
+                                            : (kind == G_BORDER ? K2G_CODE_MATE_BORDER : taxon);
+      if (!marker && taxon && !map_add(st, s.distinct, taxon, len)) {
         unsigned long long at = atomicAdd(a.defer_count, 1ull);
         if (at < a.defer_cap) a.defer_list[at] = f + a.frag_off;   // index in the whole batch
         else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
         done = false;
+        break;
       }
-      if (!done) break;
-      emit_run(s, a, taxon, len);
+      emit_run(s, a, code, len);   // a border group has length 1
       s.total_tokens += len;
     }
     if (done) {
-      finish_fragment(s, st, a);
+      finish_fragment<ResolveLane, ResolveMap, false>(s, st, a);
       n_ev = s.hit_groups;
     }
   }
@@ -547,6 +593,7 @@ namespace k2g {
 struct StepArgs {
   PipeArgs scan, probe, resolve;
   uint32_t n_scan, n_probe, n_resolve;   // blocks per role
+  uint32_t split;                        // probe blocks per scan block (1..kMaxProbeSplit)
 };
 
 // Resident blocks per SM the register allocation is fitted to (7 measured
@@ -559,12 +606,12 @@ template <int W, bool QUAL, bool RC1>
 __global__ void __launch_bounds__(kPipeBlock, K2G_PIPE_MIN_BLOCKS)
 pipe_step_kernel(StepArgs sa) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr uint32_t kRoles = 2 + kProbeSplit;
-  const uint32_t role = blockIdx.x % kRoles, blk = blockIdx.x / kRoles;
+  const uint32_t roles = 2 + sa.split;
+  const uint32_t role = blockIdx.x % roles, blk = blockIdx.x / roles;
   if (role == 0) {
     if (blk < sa.n_scan) pipe_scan_body<W, QUAL, RC1>(sa.scan, blk, smem);
-  } else if (role <= (uint32_t)kProbeSplit) {
-    if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk, role - 1, smem);
+  } else if (role <= sa.split) {
+    if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk, role - 1, sa.split, smem);
   } else {
     if (blk < sa.n_resolve) pipe_resolve_body(sa.resolve, blk, smem);
   }
@@ -576,7 +623,7 @@ cudaError_t launch_pipe_step(const StepArgs &sa, cudaStream_t st) {
   if (!most) return cudaSuccess;
   const size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
                           ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
-  pipe_step_kernel<W, QUAL, RC1><<<(2 + kProbeSplit) * most, kPipeBlock, smem, st>>>(sa);
+  pipe_step_kernel<W, QUAL, RC1><<<(2 + sa.split) * most, kPipeBlock, smem, st>>>(sa);
   note_launches();
   return cudaGetLastError();
 }

@@ -96,6 +96,11 @@ def lib():
         L.ko_taxon_counters.argtypes = [C.POINTER(Ctx), C.c_char_p, C.c_char_p, U64P,
                                         C.c_uint64, U32P, C.c_int, C.c_int, U64P, U64P,
                                         U64P, U64P]
+        L.ko_fill_table.restype = C.c_int
+        L.ko_fill_table.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_int, U64P,
+                                    C.POINTER(IndexOpts), C.c_void_p, C.c_size_t, C.c_size_t,
+                                    U32P, U64P, C.c_size_t, U64P, C.c_size_t, C.c_uint64,
+                                    C.c_uint64, C.c_int, C.POINTER(C.c_uint64)]
         L.ko_hll_new.restype = C.c_void_p
         L.ko_hll_free.argtypes = [C.c_void_p]
         L.ko_hll_insert.argtypes = [C.c_void_p, C.c_uint64]
@@ -141,6 +146,26 @@ def scan(opts: IndexOpts, seq: bytes):
     amb = np.zeros(n, np.uint8)
     m = lib().ko_scan(C.byref(opts), seq, len(seq), mins, amb)
     return mins[:m], amb[:m]
+
+
+def fill_table(table: np.ndarray, key_bits: int, value_bits: int, parent: np.ndarray,
+               opts: IndexOpts, sources: np.ndarray, src_len: int, src_taxa: np.ndarray,
+               leaves: np.ndarray, internal: np.ndarray, target: int, seed: int,
+               threads: int) -> int:
+    """ko_fill_table: sources' minimizers, then random keys to `target`
+    entries, inserted on `threads` host threads; returns the table size."""
+    parent = np.ascontiguousarray(parent, dtype=np.uint64)
+    src = np.ascontiguousarray(sources, dtype=np.uint8)
+    taxa = np.ascontiguousarray(src_taxa, dtype=np.uint32)
+    lv = np.ascontiguousarray(leaves, dtype=np.uint64)
+    it = np.ascontiguousarray(internal, dtype=np.uint64)
+    size = C.c_uint64(0)
+    r = lib().ko_fill_table(table.ctypes.data, len(table), key_bits, value_bits, parent,
+                            C.byref(opts), src.ctypes.data, src_len, len(taxa), taxa, lv, len(lv),
+                            it, len(it), target, seed, threads, C.byref(size))
+    if r:
+        raise RuntimeError("ko_fill_table: table full")
+    return int(size.value)
 
 
 class Oracle:

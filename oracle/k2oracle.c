@@ -1053,3 +1053,157 @@ void ko_taxon_counters(const ko_ctx *c, const char *bases, const char *quals,
   for (uint64_t t = 0; t < nn; t++) { ko_hll_free(total[t]); ko_hll_free(block[t]); }
   free(total); free(block); free(total_kmers); free(touched); free(runs); free(hits);
 }
+
+/* ---- host table fill for the CPU arm of the benchmark: CompareAndSet
+ * (src/compact_hash.h:417-462) with SetMinimizerLCA's retry
+ * (src/build_db.h:187-194) on several threads.  The reference guards
+ * CompareAndSet with lock zones; here each cell is updated with one atomic
+ * compare-and-swap, which gives every cell the same sequence of
+ * (old value -> LCA) transitions a locked update would. */
+static int cas_lca_atomic(uint32_t *table, uint64_t capacity, int key_bits, int value_bits,
+                          const uint64_t *parent, uint64_t key, uint32_t taxid,
+                          uint64_t *size) {
+  if (!taxid) return 0;
+  const uint64_t hc = ko_murmur3(key);
+  const uint32_t compacted = (uint32_t)(hc >> (64 - key_bits));
+  uint64_t idx = hc % capacity;
+  const uint64_t first = idx;
+  for (;;) {
+    uint32_t cell = __atomic_load_n(&table[idx], __ATOMIC_RELAXED);
+    const uint32_t v = cell_value(cell, value_bits);
+    if (!v || cell_key(cell, value_bits) == compacted) {
+      const uint32_t want = v ? (uint32_t)ko_lca(parent, v, taxid) : taxid;
+      if (v && want == v) return 0;
+      const uint32_t nc = (compacted << value_bits) | want;
+      if (__atomic_compare_exchange_n(&table[idx], &cell, nc, 0, __ATOMIC_RELAXED,
+                                      __ATOMIC_RELAXED)) {
+        if (!v) (*size)++;   /* the caller's own counter */
+        return 0;
+      }
+      continue;   /* the cell changed: look at it again */
+    }
+    if (++idx == capacity) idx = 0;
+    if (idx == first) return -1;
+  }
+}
+
+typedef struct {
+  uint32_t *table;
+  uint64_t capacity;
+  int kb, vb;
+  const uint64_t *parent;
+  /* sources: sequence s is bases[s * src_len, (s + 1) * src_len) */
+  const ko_index_opts *opts;
+  const char *bases;
+  size_t src_len, s_lo, s_hi;
+  const uint32_t *src_taxa;
+  /* random fill */
+  const uint64_t *leaves, *internal;
+  size_t n_leaves, n_internal;
+  uint64_t target, seed;
+  uint64_t *size;
+  int status;
+} fill_job;
+
+/* Inserts keys[0, n) with taxa[0, n), prefetching each key's home cell
+ * 16 keys ahead (as GetBatch prefetches, src/compact_hash.h:380-392). */
+static int insert_prefetched(const fill_job *j, const uint64_t *keys, const uint32_t *taxa,
+                             size_t n) {
+  const size_t dist = 16;
+  uint64_t added = 0;   /* new cells, added to the shared count once per batch */
+  int r = 0;
+  for (size_t i = 0; i < n && !r; i++) {
+    if (i + dist < n)
+      __builtin_prefetch(&j->table[ko_murmur3(keys[i + dist]) % j->capacity], 1, 1);
+    r = cas_lca_atomic(j->table, j->capacity, j->kb, j->vb, j->parent, keys[i], taxa[i], &added);
+  }
+  __atomic_fetch_add(j->size, added, __ATOMIC_RELAXED);
+  return r;
+}
+
+static void *fill_sources_thread(void *p) {
+  fill_job *j = (fill_job *)p;
+  uint64_t *mins = (uint64_t *)malloc(j->src_len * sizeof(uint64_t));
+  uint64_t *keys = (uint64_t *)malloc(j->src_len * sizeof(uint64_t));
+  uint32_t *taxa = (uint32_t *)malloc(j->src_len * sizeof(uint32_t));
+  uint8_t *amb = (uint8_t *)malloc(j->src_len);
+  for (size_t s = j->s_lo; s < j->s_hi && !j->status; s++) {
+    const size_t n = ko_scan(j->opts, j->bases + s * j->src_len, j->src_len, mins, amb);
+    size_t m = 0;
+    for (size_t i = 0; i < n; i++)
+      if (!amb[i] && (i == 0 || mins[i] != mins[i - 1] || amb[i - 1])) {
+        keys[m] = mins[i];
+        taxa[m++] = j->src_taxa[s];
+      }
+    if (insert_prefetched(j, keys, taxa, m) < 0) j->status = -1;
+  }
+  free(mins);
+  free(keys);
+  free(taxa);
+  free(amb);
+  return NULL;
+}
+
+static inline uint64_t splitmix64(uint64_t *x) {
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static void *fill_random_thread(void *p) {
+  fill_job *j = (fill_job *)p;
+  uint64_t x = j->seed;
+  enum { kBatch = 4096 };
+  uint64_t keys[kBatch];
+  uint32_t taxa[kBatch];
+  while (__atomic_load_n(j->size, __ATOMIC_RELAXED) < j->target && !j->status) {
+    for (int b = 0; b < kBatch; b++) {
+      keys[b] = splitmix64(&x) >> 2;                /* below 2^62 */
+      const uint64_t r = splitmix64(&x);
+      taxa[b] = (uint32_t)((r % 10) < 8 ? j->leaves[(r >> 8) % j->n_leaves]
+                                        : j->internal[(r >> 8) % j->n_internal]);
+    }
+    if (insert_prefetched(j, keys, taxa, kBatch) < 0) j->status = -1;
+  }
+  return NULL;
+}
+
+/* Inserts the minimizers of n_src sources of src_len bases each (the
+ * distinct consecutive unambiguous ones), source s with taxon src_taxa[s];
+ * then, if target > *size, uniform random keys below 2^62 with 80% leaf and
+ * 20% internal taxa until *size reaches target.  Returns 0, or -1 when the
+ * table filled up. */
+int ko_fill_table(uint32_t *table, uint64_t capacity, int key_bits, int value_bits,
+                  const uint64_t *parent, const ko_index_opts *opts, const char *bases,
+                  size_t src_len, size_t n_src, const uint32_t *src_taxa,
+                  const uint64_t *leaves, size_t n_leaves, const uint64_t *internal,
+                  size_t n_internal, uint64_t target, uint64_t seed, int threads,
+                  uint64_t *size) {
+  if (threads < 1) threads = 1;
+  if (threads > 256) threads = 256;
+  pthread_t tid[256];
+  fill_job jobs[256];
+  const size_t chunk = (n_src + threads - 1) / threads;
+  for (int t = 0; t < threads; t++) {
+    fill_job j = {table, capacity, key_bits, value_bits, parent, opts, bases, src_len,
+                  t * chunk > n_src ? n_src : t * chunk,
+                  (t + 1) * chunk > n_src ? n_src : (t + 1) * chunk, src_taxa,
+                  leaves, internal, n_leaves, n_internal, target,
+                  seed * 0x100000001B3ull + (uint64_t)t * 0x632BE59BD9B4E019ull, size, 0};
+    jobs[t] = j;
+    pthread_create(&tid[t], NULL, fill_sources_thread, &jobs[t]);
+  }
+  int status = 0;
+  for (int t = 0; t < threads; t++) {
+    pthread_join(tid[t], NULL);
+    status |= jobs[t].status;
+  }
+  if (status || !n_leaves || !n_internal || *size >= target) return status;
+  for (int t = 0; t < threads; t++) pthread_create(&tid[t], NULL, fill_random_thread, &jobs[t]);
+  for (int t = 0; t < threads; t++) {
+    pthread_join(tid[t], NULL);
+    status |= jobs[t].status;
+  }
+  return status;
+}

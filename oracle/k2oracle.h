@@ -65,6 +65,17 @@ typedef struct {
                                translates reads into six frames */
 } ko_index_opts;
 
+/* Host table fill (several threads, atomic CompareAndSet + LCA): the
+ * minimizers of n_src sources of src_len bases with their taxa, then random
+ * keys below 2^62 (80% leaf, 20% internal taxa) until *size >= target.
+ * 0, or -1 when the table is full. */
+int ko_fill_table(uint32_t *table, uint64_t capacity, int key_bits, int value_bits,
+                  const uint64_t *parent, const ko_index_opts *opts, const char *bases,
+                  size_t src_len, size_t n_src, const uint32_t *src_taxa,
+                  const uint64_t *leaves, size_t n_leaves, const uint64_t *internal,
+                  size_t n_internal, uint64_t target, uint64_t seed, int threads,
+                  uint64_t *size);
+
 /* TranslateToAllFrames (src/aa_translate.cc:41-100): the six frames of
  * dna[0,len), frame f at out + f * cap (cap >= len / 3 + 1); lens[f]
  * receives each frame's length. */

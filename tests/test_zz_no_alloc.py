@@ -110,3 +110,104 @@ def test_static_rejects_beyond_limits():
     with pytest.raises(k2g.K2GError, match="at most 262144 fragments"):
         db.classify_static(too_many, p, out.results())
     db.close()
+
+
+def _stitched_reads(n_reads=16, parts=14, part_len=36, seed=5):
+    """Single-end reads of 504 bases, each stitched from 36-base pieces of
+    14 different db_a genomes: every read hits 14 or more distinct taxa, more
+    than the fused kernel's 16-slot taxon map holds (it takes at most 12), so
+    each one is deferred to the slow path and its static scratch region."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import reads as golden_reads
+    from kraken_io import Batch
+    g = golden_reads.genomes_of("db_a")
+    rng = np.random.default_rng(seed)
+    seqs = []
+    for _ in range(n_reads):
+        idx = rng.choice(len(g), parts, replace=False)
+        piece = []
+        for i in idx:
+            s = np.asarray(g[i][1], dtype=np.uint8)
+            p = int(rng.integers(0, len(s) - part_len))
+            piece.append(s[p:p + part_len].tobytes())
+        seqs.append(b"".join(piece))
+    off = np.concatenate([[0], np.cumsum([len(s) for s in seqs])]).astype(np.uint64)
+    return b"".join(seqs), off
+
+
+class Events:
+    def __init__(self, cap):
+        t = torch()
+        self.cap = cap
+        self.keys = zeros(cap, t.int64)
+        self.taxa = zeros(cap, t.int32)
+        self.order = zeros(cap, t.int64)
+        self.used = zeros(1, t.int64)
+
+    def attach(self, out: "Outputs"):
+        r = out.results()
+        r.d_hit_keys = self.keys.data_ptr()
+        r.d_hit_taxa = self.taxa.data_ptr()
+        r.d_hit_order = self.order.data_ptr()
+        r.hits_cap = self.cap
+        r.d_hits_used = self.used.data_ptr()
+        return r
+
+    def sorted(self):
+        n = int(u64(self.used)[0])
+        ev = np.stack([u64(self.order)[:n], u64(self.keys)[:n],
+                       u32(self.taxa)[:n].astype(np.uint64)], 1)
+        return ev[np.lexsort(ev.T[::-1])]
+
+
+def test_static_slow_path_matches_allocating_path_and_allocates_nothing():
+    """Reads that overflow the fused kernel's taxon map go through the slow
+    kernel, whose per-thread maps live in the static scratch; outputs and
+    add_kmer events match the allocating path on two calls in a row, at
+    least one event carries K2G_HIT_SLOW, and a call leaves the device's
+    free memory exactly as it found it."""
+    from kraken_io import Batch
+    t = torch()
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    nc = db.info().node_count
+    stitched, soff = _stitched_reads()
+    plain = batch_of("se150")
+    k = 200   # ordinary reads around the stitched ones
+    bases = stitched + plain.bases[:int(plain.seq_off[k])]
+    off = np.concatenate([soff, soff[-1] + plain.seq_off[1:k + 1]]).astype(np.uint64)
+    b = Batch(bases=bases, quals=None, seq_off=off, n_frags=len(off) - 1, paired=False,
+              headers=[], lens=[], written=0, blocks=None)
+    reads, keep = device_reads(b)
+    p = params_for(False)
+    st = t.cuda.current_stream().cuda_stream
+    cap = int(off[-1]) + 16
+
+    want = Outputs(b, nc)
+    wev = Events(cap)
+    db.classify(reads, p, wev.attach(want), mode=k2g.MODE_PLAIN, stream=st)
+    t.cuda.synchronize()
+    ref, ref_ev = want.host(), wev.sorted()
+    assert ref[5] == 0
+    assert (ref_ev[:, 0] & np.uint64(k2g.HIT_SLOW)).any(), "no read reached the slow path"
+
+    for i in range(2):
+        got = Outputs(b, nc)
+        gev = Events(cap)
+        res = gev.attach(got)
+        t.cuda.synchronize()
+        free_before = t.cuda.mem_get_info()[0]
+        db.classify_static(reads, p, res, stream=st)
+        t.cuda.synchronize()
+        if i == 1:   # the first call may load the module and resolve the scratch
+            assert t.cuda.mem_get_info()[0] == free_before, "the static call allocated device memory"
+        h, ev = got.host(), gev.sorted()
+        assert h[5] == 0
+        assert np.array_equal(h[0], ref[0])
+        assert np.array_equal(h[1], ref[1])
+        assert np.array_equal(h[2], ref[2])
+        assert h[3] == ref[3]
+        assert np.array_equal(h[4], ref[4])
+        assert np.array_equal(ev, ref_ev)
+        assert (ev[:, 0] & np.uint64(k2g.HIT_SLOW)).any()
+    db.close()
