@@ -313,6 +313,72 @@ class DeviceRunner:
                 self.wl.stream.synchronize()
 
 
+def _time_runner_call(wl, runner, reps: int = 3) -> float:
+    torch = wl.torch
+    best = float("inf")
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(wl.stream)
+        runner.classify(0, runner.batch)
+        b.record(wl.stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
+def tune_call(wl, runner) -> dict:
+    """k2g_autotune on the step's first call: the values it keeps for this
+    table and batch class, and that call timed with the default and the
+    chosen values."""
+    k2g, cfg = wl.k2g, wl.cfg
+    cls = k2g.length_class(runner.batch * cfg.read_len, runner.batch)
+    default = wl.db.tuning(0, cls)
+    t_default = _time_runner_call(wl, runner)
+    reads = k2g.Reads(d_bases=wl.reads.data_ptr(), d_quals=None, d_seq_off=runner.off.data_ptr(),
+                      n_frags=runner.batch, max_seq_len=cfg.read_len,
+                      total_bases=runner.batch * cfg.read_len, d_frag_block=None, frag_base=0)
+    res = k2g.Results(runner.call.data_ptr(), runner.hg.data_ptr(), runner.hoff.data_ptr(),
+                      runner.hlen.data_ptr(), runner.runs.data_ptr(), runner.runs_cap, None,
+                      None, None, None, 0, None, runner.status.data_ptr())
+    chosen, _ = wl.db.autotune(reads, runner.params, res, trials=2, stream=wl.stream.cuda_stream)
+    t_tuned = _time_runner_call(wl, runner)
+    return {"length_class": cls, "default": default.as_dict(), "chosen": chosen.as_dict(),
+            "default_ms_per_call": round(t_default, 3), "tuned_ms_per_call": round(t_tuned, 3),
+            "gain": round(t_default / t_tuned, 3), "reads_per_call": runner.batch}
+
+
+def small_calls_run(wl, sizes=(1_000, 10_000, 100_000, 1_000_000), reps: int = 50) -> dict:
+    """Per-call latency of k2g_classify on small batches of the resident
+    reads (the request sizes of the serving stream), with the launch
+    sequence issued launch by launch and captured as one CUDA graph: the
+    host clock around each synchronous call, median of `reps`."""
+    torch, k2g, cfg = wl.torch, wl.k2g, wl.cfg
+    out = {}
+    runner = DeviceRunner(wl, k2g.MODE_PIPELINED, batch=max(sizes))
+    cls = 0
+    before = wl.db.tuning(0, cls)
+    try:
+        for graphs in (0, 1):
+            t = k2g.Tuning(**{**before.as_dict(), "graphs": graphs})
+            wl.db.set_tuning(0, cls, t)
+            row = {}
+            for n in sizes:
+                runner.classify(0, n)
+                wl._sync()
+                ts = []
+                for _ in range(reps):
+                    t0 = time.perf_counter()
+                    runner.classify(0, n)
+                    wl.stream.synchronize()
+                    ts.append(time.perf_counter() - t0)
+                row[str(n)] = round(float(np.median(ts)) * 1e3, 4)
+            out["graphs" if graphs else "launches"] = row
+    finally:
+        wl.db.set_tuning(0, cls, before)
+    out["unit"] = "ms per synchronous call (host clock, median)"
+    return out
+
+
 class KmerRunner:
     """Classification with add_kmer events folded into the -K taxon counters
     (k2g_counters), batch by batch, then the clade estimates.  Reader blocks
@@ -524,8 +590,9 @@ def serving_run(wl: Workload, log, budget_gb: float = 8.0, n_pool: int = 1_500_0
         for t, (a, z) in items:
             sv.wait(t, 600)
             nb = int(off[z] - off[a])
+            parts = sv.timing(t)
             *_, lat = sv.fetch(t, z - a, nb + 2 * (z - a) + 8)
-            out.append((z - a, lat))
+            out.append((z - a, lat, parts))
 
     # capacity: a burst of requests submitted at once
     burst = [request() for _ in range(24)]
@@ -534,7 +601,7 @@ def serving_run(wl: Workload, log, budget_gb: float = 8.0, n_pool: int = 1_500_0
     res = []
     collect(tk, res)
     burst_s = time.perf_counter() - t0
-    cap_reads_s = sum(n for n, _ in res) / burst_s
+    cap_reads_s = sum(r[0] for r in res) / burst_s
     mean_req = (max_req - 1000) / np.log(max_req / 1000)
     rate = 0.7 * cap_reads_s / mean_req                   # requests per second
     # Poisson arrivals at 70% of capacity
@@ -575,15 +642,31 @@ def serving_run(wl: Workload, log, budget_gb: float = 8.0, n_pool: int = 1_500_0
     th.join()
     wall = time.perf_counter() - t_start
     sv.close()
-    lats = np.array([l for _, l in done])
-    reads = sum(n for n, _ in done)
+    lats = np.array([d[1] for d in done])
+    sizes = np.array([d[0] for d in done])
+    parts = np.array([d[2] for d in done])
+    reads = int(sizes.sum())
+
+    def pct(x):
+        return {"p50": round(float(np.percentile(x, 50)) * 1e3, 2),
+                "p99": round(float(np.percentile(x, 99)) * 1e3, 2),
+                "max": round(float(x.max()) * 1e3, 2)} if len(x) else None
+
+    # where the latency goes, overall and by request size
+    by_size = {}
+    for name, lo, hi in (("1k-10k", 0, 10_000), ("10k-100k", 10_000, 100_000),
+                         ("100k-1M", 100_000, 10 ** 9)):
+        m = (sizes >= lo) & (sizes < hi)
+        by_size[name] = {"requests": int(m.sum()), "latency_ms": pct(lats[m]),
+                         "queued_ms": pct(parts[m, 0]), "running_ms": pct(parts[m, 2])}
     return {"workload": "Poisson arrivals at 70% of burst capacity; requests log-uniform "
                         "1k-1M reads; lengths 5/6 x 150 bp + 1/6 log-normal mean 5 kb",
             "hbm_budget_gb": budget_gb, "requests": len(done), "offered_req_per_s": round(rate, 2),
             "reads_per_s": round(reads / wall), "burst_capacity_reads_per_s": round(cap_reads_s),
-            "latency_ms": {"p50": round(float(np.percentile(lats, 50)) * 1e3, 2),
-                           "p99": round(float(np.percentile(lats, 99)) * 1e3, 2),
-                           "max": round(float(lats.max()) * 1e3, 2)}}
+            "latency_ms": pct(lats),
+            "breakdown_ms": {"queued": pct(parts[:, 0]), "batching": pct(parts[:, 1]),
+                             "running": pct(parts[:, 2])},
+            "by_request_size": by_size}
 
 
 def _substitute(torch, seq, rate, g, lut):
@@ -591,18 +674,6 @@ def _substitute(torch, seq, rate, g, lut):
     hit = torch.rand(seq.numel(), generator=g, device=seq.device) < rate
     n = int(hit.sum())
     seq[hit] = lut[torch.randint(0, 4, (n,), generator=g, device=seq.device).long()]
-
-
-def _time_classify(wl, reads, res, params, mode, st):
-    torch = wl.torch
-    wl.db.classify(reads, params, res, mode=mode, stream=st)
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(wl.stream)
-    wl.db.classify(reads, params, res, mode=mode, stream=st)
-    b.record(wl.stream)
-    torch.cuda.synchronize()
-    return a.elapsed_time(b) / 1e3
 
 
 def _gpu_buffers(torch, n, runs_cap, nodes):
@@ -616,17 +687,6 @@ def _results(k2g, b, runs_cap):
     return k2g.Results(b["call"].data_ptr(), b["hg"].data_ptr(), b["hoff"].data_ptr(),
                        b["hlen"].data_ptr(), b["runs"].data_ptr(), runs_cap, b["tr"].data_ptr(),
                        None, None, None, 0, None, b["status"].data_ptr())
-
-
-def _oracle_calls(wl, cells, bases, off, n_frags, paired, params):
-    import oracle
-    cfg = wl.cfg
-    o = oracle.Oracle(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, wl.parent,
-                      oracle.index_opts(cfg.k, cfg.l, spaced_mask(SEED_TEMPLATE), TOGGLE))
-    calls, *_ = o.classify(bases, None, off, n_frags, threads=os.cpu_count() or 1,
-                           confidence=params.confidence, min_hit_groups=params.min_hit_groups,
-                           paired=paired)
-    return calls
 
 
 def capped_taxonomy(n: int, max_depth: int, seed: int) -> np.ndarray:
@@ -1403,6 +1463,13 @@ def run_ours(args, log):
         return None
     for _ in range(args.warmup):
         runner.step()
+    # autotune on the first call of the step (outside the timed region): the
+    # default and the chosen values, each timed on that call
+    tuning = None
+    if not args.skip_tune:
+        tuning = tune_call(wl, runner)
+        log(f"tuning: {tuning}")
+        runner.step()
     barrier(pg)
     calls = []
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1511,6 +1578,7 @@ def run_ours(args, log):
     serving = None if args.skip_serving else serving_run(wl, log)
     long_reads = None if args.skip_serving else long_reads_run(wl, log)
     value_counts = value_counts_run(wl)
+    small_calls = small_calls_run(wl)
     configs = None
     if not args.skip_configs:
         del runner
@@ -1570,6 +1638,8 @@ def run_ours(args, log):
         "serving": serving,
         "long_reads": long_reads,
         "value_counts": value_counts,
+        "tuning": tuning,
+        "small_calls": small_calls,
         "configs": configs,
         "gpu_launches": launches,
         "clocks": clk.summary(),
@@ -1675,6 +1745,8 @@ def main():
                     help="skip the paired, uneven-length and build measurements")
     ap.add_argument("--skip-serving", action="store_true",
                     help="skip the serving (Poisson request stream) measurement")
+    ap.add_argument("--skip-tune", action="store_true",
+                    help="skip the autotuner on the main workload")
     ap.add_argument("--skip-kmer", action="store_true",
                     help="skip the -K (minimizer data) measurement")
     ap.add_argument("--profile", action="store_true",

@@ -71,7 +71,10 @@ typedef struct {
 typedef struct {
   uint64_t capacity, size, key_bits, value_bits, node_count;
   k2g_index_options opts;
-  const uint32_t *d_cells;      /* the compact hash table in HBM           */
+  const uint32_t *d_cells;      /* the compact hash table in HBM: uint32
+                                   cells, or for 40-bit cells (key + value
+                                   bits = 40) uint64 cells, each the packed
+                                   5-byte cell zero-extended               */
   const uint32_t *d_parent;     /* parent id per internal taxon id         */
   int device;
 } k2g_db_info;
@@ -105,6 +108,8 @@ k2g_status k2g_db_info_get(const k2g_db *db, k2g_db_info *out);
 k2g_status k2g_db_write_hash(const k2g_db *db, const char *hash_k2d);
 /* Copies the table (capacity cells) into host memory. */
 k2g_status k2g_db_download(const k2g_db *db, uint32_t *cells, uint64_t *size);
+/* (For 40-bit cells `cells` receives capacity packed 5-byte cells, as
+ * hash.k2d stores them.) */
 /* Cells per taxon -- CompactHashTable::GetValueCounts (src/compact_hash.h:503-519),
  * what dump_table / kraken2-inspect report (src/dump_table.cc:59-101):
  * counts[t] (host, node_count entries) = cells whose value is taxon t
@@ -337,6 +342,13 @@ k2g_status k2g_server_fetch(k2g_server *s, uint64_t ticket, uint32_t *call, uint
                             double *latency_s);
 /* Result sizes of a finished request (to size the buffers for fetch). */
 k2g_status k2g_server_sizes(k2g_server *s, uint64_t ticket, uint64_t *n_frags, uint64_t *n_runs);
+/* Where a finished request's latency went (call before k2g_server_fetch):
+ * queued = submit until its first fragments were taken into a batch;
+ * batching = until its last fragments were (a request split over several
+ * batches); running = from then until its last batch's results were back.
+ * The three add up to the latency k2g_server_fetch reports. */
+k2g_status k2g_server_timing(k2g_server *s, uint64_t ticket, double *queued_s, double *batching_s,
+                             double *running_s);
 k2g_status k2g_server_destroy(k2g_server *s);
 
 /* Pinned host memory helpers for callers that stage their own buffers. */

@@ -45,7 +45,7 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
            "k2g_classify_host_blocks", "k2g_server_create", "k2g_server_submit",
            "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy", "k2g_server_sizes",
-           "k2g_tuning_get", "k2g_tuning_set", "k2g_autotune"]
+           "k2g_tuning_get", "k2g_tuning_set", "k2g_autotune", "k2g_server_timing"]
 
 
 class Tuning(C.Structure):
@@ -157,6 +157,8 @@ def lib():
             "k2g_server_fetch": [vp, u64, vp, vp, vp, vp, C.POINTER(u64), C.POINTER(C.c_double)],
             "k2g_server_destroy": [vp],
             "k2g_server_sizes": [vp, u64, C.POINTER(u64), C.POINTER(u64)],
+            "k2g_server_timing": [vp, u64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)],
             "k2g_tuning_get": [vp, i32, i32, C.POINTER(Tuning)],
             "k2g_tuning_set": [vp, i32, i32, C.POINTER(Tuning)],
             "k2g_autotune": [vp, C.POINTER(Reads), C.POINTER(ClassifyParams), C.POINTER(Results),
@@ -227,8 +229,13 @@ class Database:
         return i
 
     def download(self):
+        """(cells, size): uint32 cells, or for a 40-bit table the packed
+        5-byte cells as hash.k2d stores them (uint8, capacity * 5)."""
         inf = self.info()
-        cells = np.zeros(inf.capacity, np.uint32)
+        if inf.key_bits + inf.value_bits == 40:
+            cells = np.zeros(inf.capacity * 5, np.uint8)
+        else:
+            cells = np.zeros(inf.capacity, np.uint32)
         size = C.c_uint64()
         check(lib().k2g_db_download(self.h, cells.ctypes.data, C.byref(size)))
         return cells, size.value
@@ -383,6 +390,12 @@ class Server:
         done = C.c_int(0)
         check(lib().k2g_server_wait(self.h, ticket, timeout_s, C.byref(done)))
         return bool(done.value)
+
+    def timing(self, ticket: int) -> tuple[float, float, float]:
+        """(queued_s, batching_s, running_s) of a finished, unfetched request."""
+        q, b, r = C.c_double(0), C.c_double(0), C.c_double(0)
+        check(lib().k2g_server_timing(self.h, ticket, C.byref(q), C.byref(b), C.byref(r)))
+        return q.value, b.value, r.value
 
     def fetch(self, ticket: int, n_frags: int | None = None, runs_cap: int | None = None):
         """-> (call, hit_groups, hitlist_len, runs, latency_s) of a finished

@@ -33,10 +33,11 @@ constexpr int kIndexBits = 30;                  // pairs per round: < 2^30
 constexpr uint64_t kNoRegion = ~0ull;
 constexpr uint32_t kFlagCap = 1u << 20;         // clusters that may need a merged replay
 
+template <class C>
 struct OrderedView {
   TableView t;
-  uint32_t *cells;
-  const uint32_t *snap;       // the table before this round
+  typename C::T *cells;
+  const typename C::T *snap;  // the table before this round
   const uint32_t *occ;        // bitmap: occupied after the unordered pass
   const uint32_t *parent;
   const uint64_t *keys;
@@ -44,7 +45,8 @@ struct OrderedView {
   uint64_t n;
 };
 
-__device__ __forceinline__ bool occupied1(const OrderedView &v, uint64_t c) {
+template <class C>
+__device__ __forceinline__ bool occupied1(const OrderedView<C> &v, uint64_t c) {
   return (v.occ[c >> 5] >> (c & 31)) & 1u;
 }
 __device__ __forceinline__ uint64_t next_cell(const TableView &t, uint64_t c) {
@@ -54,14 +56,15 @@ __device__ __forceinline__ uint64_t prev_cell(const TableView &t, uint64_t c) {
   return c == 0 ? t.capacity - 1 : c - 1;
 }
 
-__global__ void occ_kernel(const uint32_t *cells, uint64_t capacity, uint32_t value_mask,
-                           uint32_t *occ) {
+template <class C>
+__global__ void occ_kernel(const typename C::T *cells, TableView t, uint32_t *occ) {
+  const uint64_t capacity = t.capacity;
   for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < (capacity + 31) / 32;
        w += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t bits = 0;
     for (int b = 0; b < 32; b++) {
       const uint64_t c = w * 32 + b;
-      if (c < capacity && (cells[c] & value_mask)) bits |= 1u << b;
+      if (c < capacity && C::value(cells[c], t)) bits |= 1u << b;
     }
     occ[w] = bits;
   }
@@ -69,7 +72,8 @@ __global__ void occ_kernel(const uint32_t *cells, uint64_t capacity, uint32_t va
 
 // (cluster start << kIndexBits | list position) per pair; pairs with taxid 0
 // are not inserted and sort last.
-__global__ void region_kernel(OrderedView v, uint64_t *out, uint32_t *status) {
+template <class C>
+__global__ void region_kernel(OrderedView<C> v, uint64_t *out, uint32_t *status) {
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < v.n;
        j += (uint64_t)gridDim.x * blockDim.x) {
     if (!v.taxids[j]) {
@@ -93,10 +97,11 @@ __global__ void region_kernel(OrderedView v, uint64_t *out, uint32_t *status) {
 // Cells from `start` for `limit` offsets belong to this replay; beyond them
 // only cells that were free after the unordered pass may be taken.  Returns
 // false when the probe reaches a cell owned by another cluster.
-__device__ bool replay_one(const OrderedView &v, uint64_t start, uint64_t &limit, uint64_t key,
+template <class C>
+__device__ bool replay_one(const OrderedView<C> &v, uint64_t start, uint64_t &limit, uint64_t key,
                            uint32_t taxid) {
   const uint64_t hc = murmur3(key);
-  const uint32_t ck = (uint32_t)(hc >> v.t.key_shift);
+  const uint64_t ck = hc >> v.t.key_shift;
   uint64_t c = fast_mod(hc, v.t.div);
   for (uint64_t step = 0; step < v.t.capacity; step++) {
     const uint64_t off = c >= start ? c - start : c + v.t.capacity - start;
@@ -106,11 +111,11 @@ __device__ bool replay_one(const OrderedView &v, uint64_t start, uint64_t &limit
       if (off > limit || occupied1(v, c)) return false;
       limit = off + 1;
     }
-    const uint32_t cell = v.cells[c];
-    const uint32_t val = cell & v.t.value_mask;
-    if (!val || (cell >> v.t.value_bits) == ck) {
+    const typename C::T cell = v.cells[c];
+    const uint32_t val = C::value(cell, v.t);
+    if (!val || C::match(cell, ck, v.t)) {
       const uint32_t nv = val ? lca(v.parent, val, taxid) : taxid;
-      v.cells[c] = (ck << v.t.value_bits) | nv;
+      v.cells[c] = C::make(ck, nv, v.t);
       return true;
     }
     c = next_cell(v.t, c);
@@ -119,7 +124,8 @@ __device__ bool replay_one(const OrderedView &v, uint64_t start, uint64_t &limit
 }
 
 // One thread per cluster: restore from the snapshot, replay in list order.
-__global__ void replay_kernel(OrderedView v, const uint64_t *sorted, uint64_t n_sorted,
+template <class C>
+__global__ void replay_kernel(OrderedView<C> v, const uint64_t *sorted, uint64_t n_sorted,
                               uint64_t *flags, unsigned long long *n_flags) {
   const uint64_t pmask = (1ull << kIndexBits) - 1;
   for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_sorted;
@@ -163,7 +169,8 @@ __device__ uint64_t lower_bound_region(const uint64_t *sorted, uint64_t n, uint6
 // thread: flags are rare).  The flagged list is sorted by cluster start.
 // A merged group spans clusters [s0 .. ]; it grows by the next cluster until
 // its replay fits.  `scratch` holds list positions (capacity scratch_cap).
-__global__ void fixup_kernel(OrderedView v, const uint64_t *sorted, uint64_t n_sorted,
+template <class C>
+__global__ void fixup_kernel(OrderedView<C> v, const uint64_t *sorted, uint64_t n_sorted,
                              const uint64_t *flags, uint64_t n_flags, uint64_t *scratch,
                              uint64_t scratch_cap, uint32_t *status) {
   if (threadIdx.x || blockIdx.x) return;
@@ -186,7 +193,7 @@ __global__ void fixup_kernel(OrderedView v, const uint64_t *sorted, uint64_t n_s
         if (ns < 64) starts[ns++] = c;
         else too_many = true;
         while (occupied1(v, c) && len < v.t.capacity) { c = next_cell(v.t, c); len++; }
-        while (!occupied1(v, c) && (v.cells[c] & v.t.value_mask) && len < v.t.capacity) {
+        while (!occupied1(v, c) && C::value(v.cells[c], v.t) && len < v.t.capacity) {
           c = next_cell(v.t, c);
           len++;
         }
@@ -246,12 +253,12 @@ __global__ void fixup_kernel(OrderedView v, const uint64_t *sorted, uint64_t n_s
   }
 }
 
-__global__ void count_kernel(const uint32_t *cells, uint64_t capacity, uint32_t value_mask,
-                             unsigned long long *size) {
+template <class C>
+__global__ void count_kernel(const typename C::T *cells, TableView t, unsigned long long *size) {
   uint64_t mine = 0;
-  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < capacity;
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < t.capacity;
        c += (uint64_t)gridDim.x * blockDim.x)
-    mine += (cells[c] & value_mask) != 0;
+    mine += C::value(cells[c], t) != 0;
   for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
   if ((threadIdx.x & 31) == 0 && mine) atomicAdd(size, (unsigned long long)mine);
 }
@@ -277,13 +284,17 @@ struct DevBuf {
 
 }  // namespace
 
-// One round (fewer than 2^30 pairs) of the order-exact insert.
-k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
-                                uint64_t n, cudaStream_t st) {
+// One round (fewer than 2^30 pairs) of the order-exact insert over cells of
+// layout C.
+template <class C>
+k2g_status insert_ordered(k2g_db *db, typename C::T *cells, const uint64_t *d_keys,
+                          const uint32_t *d_taxids, uint64_t n, cudaStream_t st) {
+  using T = typename C::T;
   const TableView t = db->table_view();
   const uint64_t cap = db->capacity;
   if (bits_of(cap) + kIndexBits > 64) return fail(K2G_ERR_UNSUPPORTED, "table too large for the ordered insert");
-  DevBuf<uint32_t> snap, occ, status;
+  DevBuf<T> snap;
+  DevBuf<uint32_t> occ, status;
   DevBuf<uint64_t> keys, alt, flags, scratch;
   DevBuf<uint32_t> hist, sums;
   DevBuf<unsigned long long> ctr;
@@ -291,28 +302,28 @@ k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32
   K2G_CUDA_TRY(occ.alloc((cap + 31) / 32));
   K2G_CUDA_TRY(status.alloc(1));
   K2G_CUDA_TRY(ctr.alloc(2));
-  K2G_CUDA_TRY(cudaMemcpyAsync(snap.p, db->d_cells, cap * 4, cudaMemcpyDeviceToDevice, st));
+  K2G_CUDA_TRY(cudaMemcpyAsync(snap.p, cells, cap * sizeof(T), cudaMemcpyDeviceToDevice, st));
   K2G_CUDA_TRY(cudaStreamSynchronize(st));
   // 1. unordered pass (validates values and capacity)
   k2g_status s = k2g_build_insert(db, d_keys, d_taxids, n, 0, st);
   if (s != K2G_OK) return s;
   K2G_CUDA_TRY(cudaMemsetAsync(status.p, 0, 4, st));
   K2G_CUDA_TRY(cudaMemsetAsync(ctr.p, 0, 16, st));
-  occ_kernel<<<grid(db->device, (cap + 31) / 32), 256, 0, st>>>(db->d_cells, cap, t.value_mask, occ.p);
+  occ_kernel<C><<<grid(db->device, (cap + 31) / 32), 256, 0, st>>>(cells, t, occ.p);
   // 2. cluster of each pair, sorted
   K2G_CUDA_TRY(keys.alloc(n));
   K2G_CUDA_TRY(alt.alloc(n));
   K2G_CUDA_TRY(hist.alloc(rsort::hist_entries(n)));
   K2G_CUDA_TRY(sums.alloc(rsort::sum_entries(n) + 1));
-  OrderedView v{t, db->d_cells, snap.p, occ.p, db->d_parent, d_keys, d_taxids, n};
-  region_kernel<<<grid(db->device, n), 256, 0, st>>>(v, keys.p, status.p);
+  OrderedView<C> v{t, cells, snap.p, occ.p, db->d_parent, d_keys, d_taxids, n};
+  region_kernel<C><<<grid(db->device, n), 256, 0, st>>>(v, keys.p, status.p);
   note_launches(2);
   K2G_CUDA_TRY(cudaGetLastError());
   uint64_t *sorted = nullptr;
   K2G_CUDA_TRY(rsort::sort_u64(keys.p, alt.p, n, 64, hist.p, sums.p, st, &sorted));
   // 3. per-cluster replays
   K2G_CUDA_TRY(flags.alloc(kFlagCap));
-  replay_kernel<<<grid(db->device, n), 256, 0, st>>>(v, sorted, n, flags.p, ctr.p);
+  replay_kernel<C><<<grid(db->device, n), 256, 0, st>>>(v, sorted, n, flags.p, ctr.p);
   note_launches();
   K2G_CUDA_TRY(cudaGetLastError());
   unsigned long long n_flags = 0;
@@ -330,7 +341,7 @@ k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32
     K2G_CUDA_TRY(cudaMemcpy(flags.p, fl.data(), n_flags * 8, cudaMemcpyHostToDevice));
     const uint64_t scratch_cap = std::min<uint64_t>(n, 1ull << 24);
     K2G_CUDA_TRY(scratch.alloc(scratch_cap));
-    fixup_kernel<<<1, 32, 0, st>>>(v, sorted, n, flags.p, n_flags, scratch.p, scratch_cap, status.p);
+    fixup_kernel<C><<<1, 32, 0, st>>>(v, sorted, n, flags.p, n_flags, scratch.p, scratch_cap, status.p);
     note_launches();
     K2G_CUDA_TRY(cudaGetLastError());
     K2G_CUDA_TRY(cudaMemcpyAsync(&st_word, status.p, 4, cudaMemcpyDeviceToHost, st));
@@ -339,12 +350,18 @@ k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32
   }
   // size: occupied cells
   K2G_CUDA_TRY(cudaMemsetAsync(db->d_size, 0, 8, st));
-  count_kernel<<<grid(db->device, cap), 256, 0, st>>>(db->d_cells, cap, t.value_mask,
-                                                       reinterpret_cast<unsigned long long *>(db->d_size));
+  count_kernel<C><<<grid(db->device, cap), 256, 0, st>>>(cells, t,
+                                                          reinterpret_cast<unsigned long long *>(db->d_size));
   note_launches();
   K2G_CUDA_TRY(cudaGetLastError());
   K2G_CUDA_TRY(cudaStreamSynchronize(st));
   return K2G_OK;
+}
+
+k2g_status build_insert_ordered(k2g_db *db, const uint64_t *d_keys, const uint32_t *d_taxids,
+                                uint64_t n, cudaStream_t st) {
+  if (db->d_wide) return insert_ordered<CellWide>(db, db->d_wide, d_keys, d_taxids, n, st);
+  return insert_ordered<Cell32>(db, db->d_cells, d_keys, d_taxids, n, st);
 }
 
 }  // namespace k2g

@@ -448,6 +448,14 @@ __device__ __forceinline__ void probe_segment(Store &st, const ClassifyArgs &a, 
                                               uint64_t frag, uint32_t key_ordinal) {
   constexpr int B = 4;
   const TableView &t = a.table;
+  if (t.wide) {   // 40-bit cells
+    for (int j = 0; j < nk; j++) {
+      const uint32_t v = table_get_wide(t, murmur3(st.key(j)));
+      if (a.hit_keys && v) emit_hit(a, frag, key_ordinal + j, st.key(j), v);
+      st.val(j) = v;
+    }
+    return;
+  }
   for (int j0 = 0; j0 < nk; j0 += B) {
     uint64_t hc[B], idx[B];
     Sector sec[B];

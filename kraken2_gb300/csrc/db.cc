@@ -10,6 +10,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cstdio>
 #include <cstring>
@@ -56,6 +57,7 @@ using namespace k2g;
 k2g::TableView k2g_db::table_view() const {
   TableView v;
   v.cells = d_cells;
+  v.wide = d_wide;
   v.capacity = capacity;
   v.div = div;
   v.key_shift = (uint32_t)(64 - key_bits);
@@ -140,13 +142,40 @@ k2g_status upload_parents(k2g_db *db, const uint64_t *parent, uint64_t n) {
 
 k2g_status alloc_table(k2g_db *db, uint64_t capacity) {
   if (capacity == 0) return fail(K2G_ERR_FORMAT, "table capacity is zero");
-  uint64_t padded = (capacity + 7) & ~7ull;   // whole 32-byte sectors
-  K2G_CUDA_TRY(cudaMalloc(&db->d_cells, padded * sizeof(uint32_t)));
-  if (padded != capacity)
-    K2G_CUDA_TRY(cudaMemset(db->d_cells + capacity, 0, (padded - capacity) * sizeof(uint32_t)));
+  if (db->cell_bytes == 5) {
+    uint64_t padded = (capacity + 3) & ~3ull;   // whole 32-byte sectors
+    K2G_CUDA_TRY(cudaMalloc(&db->d_wide, padded * 8));
+    if (padded != capacity)
+      K2G_CUDA_TRY(cudaMemset(db->d_wide + capacity, 0, (padded - capacity) * 8));
+  } else {
+    uint64_t padded = (capacity + 7) & ~7ull;   // whole 32-byte sectors
+    K2G_CUDA_TRY(cudaMalloc(&db->d_cells, padded * sizeof(uint32_t)));
+    if (padded != capacity)
+      K2G_CUDA_TRY(cudaMemset(db->d_cells + capacity, 0, (padded - capacity) * sizeof(uint32_t)));
+  }
   K2G_CUDA_TRY(cudaMalloc(&db->d_size, sizeof(uint64_t)));
   db->capacity = capacity;
   db->div = make_div_magic(capacity);
+  return K2G_OK;
+}
+
+// 40-bit cells from the file: capacity packed 5-byte cells, each widened to
+// the 64-bit device cell (little-endian bytes 0-4, upper bytes zero).
+k2g_status load_wide_cells(k2g_db *db, int fd, uint64_t capacity) {
+  const uint64_t per = 1ull << 22;   // cells per chunk
+  std::vector<unsigned char> raw(per * 5);
+  std::vector<unsigned long long> wide(per);
+  for (uint64_t done = 0; done < capacity;) {
+    const uint64_t n = std::min(per, capacity - done);
+    if (!read_exact(fd, raw.data(), n * 5)) return fail(K2G_ERR_FORMAT, "unexpected end of hash file");
+    for (uint64_t i = 0; i < n; i++) {
+      unsigned long long c = 0;
+      for (int b = 4; b >= 0; b--) c = (c << 8) | raw[i * 5 + b];
+      wide[i] = c;
+    }
+    K2G_CUDA_TRY(cudaMemcpy(db->d_wide + done, wide.data(), n * 8, cudaMemcpyHostToDevice));
+    done += n;
+  }
   return K2G_OK;
 }
 
@@ -156,6 +185,7 @@ void destroy(k2g_db *db) {
   cudaGetDevice(&cur);
   cudaSetDevice(db->device);
   if (db->d_cells) cudaFree(db->d_cells);
+  if (db->d_wide) cudaFree(db->d_wide);
   if (db->d_parent) cudaFree(db->d_parent);
   if (db->d_size) cudaFree(db->d_size);
   cudaSetDevice(cur);
@@ -246,16 +276,19 @@ extern "C" k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
   db->size = hdr[1];
   db->key_bits = hdr[2];
   db->value_bits = hdr[3];
-  if (db->key_bits + db->value_bits == 40) {
-    close(fd);
-    return fail(K2G_ERR_UNSUPPORTED, "40-bit compact hash cells are not supported");
-  }
-  if (db->key_bits + db->value_bits != 32 || db->key_bits == 0 || db->value_bits == 0) {
+  // GetKVStoreCellType (src/kv_store.h:35-57): key + value bits give the cell
+  db->cell_bytes = db->key_bits + db->value_bits == 40 ? 5 : 4;
+  if ((db->key_bits + db->value_bits != 32 && db->key_bits + db->value_bits != 40) ||
+      db->key_bits == 0 || db->value_bits == 0) {
     close(fd);
     return fail(K2G_ERR_FORMAT, "Unable to determine width of compact hash cell");
   }
+  if (db->value_bits > 31) {
+    close(fd);
+    return fail(K2G_ERR_UNSUPPORTED, "more than 31 value bits are not supported");
+  }
   struct stat sb;
-  if (hdr[0] == 0 || fstat(fd, &sb) != 0 || (uint64_t)sb.st_size != 32 + hdr[0] * 4) {
+  if (hdr[0] == 0 || fstat(fd, &sb) != 0 || (uint64_t)sb.st_size != 32 + hdr[0] * db->cell_bytes) {
     close(fd);
     return fail(K2G_ERR_FORMAT, std::string("Capacity mismatch in ") + hash_k2d);
   }
@@ -266,7 +299,11 @@ extern "C" k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
   k2g_status s = upload_parents(db.get(), parent.data(), parent.size());
   if (s == K2G_OK) s = alloc_table(db.get(), hdr[0]);
   if (s != K2G_OK) { close(fd); destroy(db.release()); return s; }
-  {
+  if (db->cell_bytes == 5) {
+    k2g_status w = load_wide_cells(db.get(), fd, hdr[0]);
+    close(fd);
+    if (w != K2G_OK) { destroy(db.release()); return w; }
+  } else {
     // stream the cells through two pinned buffers
     const size_t chunk = 64ull << 20;
     void *pin[2] = {nullptr, nullptr};
@@ -331,8 +368,10 @@ extern "C" k2g_status k2g_db_create(const k2g_index_options *opts, uint64_t capa
                                     k2g_db **out) {
   if (!opts || !parent || !out) return fail(K2G_ERR_ARG, "null argument");
   *out = nullptr;
-  if (key_bits + value_bits != 32 || key_bits == 0 || value_bits == 0)
-    return fail(K2G_ERR_ARG, "sum of key bits and value bits must equal 32");
+  if ((key_bits + value_bits != 32 && key_bits + value_bits != 40) || key_bits == 0 ||
+      value_bits == 0)
+    return fail(K2G_ERR_ARG, "sum of key bits and value bits must equal 32 or 40");
+  if (value_bits > 31) return fail(K2G_ERR_ARG, "more than 31 value bits are not supported");
   if (node_count > (1ull << value_bits))
     return fail(K2G_ERR_ARG, "value bits too narrow for the taxonomy");
   k2g_status s = validate_options(*opts);
@@ -345,11 +384,13 @@ extern "C" k2g_status k2g_db_create(const k2g_index_options *opts, uint64_t capa
   db->opts = *opts;
   db->key_bits = key_bits;
   db->value_bits = value_bits;
+  db->cell_bytes = key_bits + value_bits == 40 ? 5 : 4;
   s = upload_parents(db.get(), parent, node_count);
   if (s != K2G_OK) { destroy(db.release()); return s; }
   s = alloc_table(db.get(), capacity);
   if (s != K2G_OK) { destroy(db.release()); return s; }
-  K2G_CUDA_TRY(cudaMemset(db->d_cells, 0, capacity * sizeof(uint32_t)));
+  if (db->d_wide) K2G_CUDA_TRY(cudaMemset(db->d_wide, 0, capacity * 8));
+  else K2G_CUDA_TRY(cudaMemset(db->d_cells, 0, capacity * sizeof(uint32_t)));
   K2G_CUDA_TRY(cudaMemset(db->d_size, 0, 8));
   db->size = 0;
   *out = db.release();
@@ -376,7 +417,7 @@ extern "C" k2g_status k2g_db_info_get(const k2g_db *db, k2g_db_info *out) {
   out->value_bits = db->value_bits;
   out->node_count = db->node_count;
   out->opts = db->opts;
-  out->d_cells = db->d_cells;
+  out->d_cells = db->d_wide ? reinterpret_cast<const uint32_t *>(db->d_wide) : db->d_cells;
   out->d_parent = db->d_parent;
   out->device = db->device;
   return K2G_OK;
@@ -385,21 +426,36 @@ extern "C" k2g_status k2g_db_info_get(const k2g_db *db, k2g_db_info *out) {
 extern "C" k2g_status k2g_db_download(const k2g_db *db, uint32_t *cells, uint64_t *size) {
   if (!db || !cells) return fail(K2G_ERR_ARG, "null argument");
   K2G_CUDA_TRY(cudaSetDevice(db->device));
-  K2G_CUDA_TRY(cudaMemcpy(cells, db->d_cells, db->capacity * 4, cudaMemcpyDeviceToHost));
+  if (db->d_wide) {
+    // packed 5-byte cells, as the file holds them
+    unsigned char *out = reinterpret_cast<unsigned char *>(cells);
+    const uint64_t per = 1ull << 22;
+    std::vector<unsigned long long> wide(per);
+    for (uint64_t done = 0; done < db->capacity;) {
+      const uint64_t n = std::min(per, db->capacity - done);
+      K2G_CUDA_TRY(cudaMemcpy(wide.data(), db->d_wide + done, n * 8, cudaMemcpyDeviceToHost));
+      for (uint64_t i = 0; i < n; i++)
+        for (int b = 0; b < 5; b++) out[(done + i) * 5 + b] = (unsigned char)(wide[i] >> (8 * b));
+      done += n;
+    }
+  } else {
+    K2G_CUDA_TRY(cudaMemcpy(cells, db->d_cells, db->capacity * 4, cudaMemcpyDeviceToHost));
+  }
   if (size) K2G_CUDA_TRY(cudaMemcpy(size, db->d_size, 8, cudaMemcpyDeviceToHost));
   return K2G_OK;
 }
 
 extern "C" k2g_status k2g_db_write_hash(const k2g_db *db, const char *hash_k2d) {
   if (!db || !hash_k2d) return fail(K2G_ERR_ARG, "null argument");
-  std::vector<uint32_t> cells(db->capacity);
+  const size_t cb = db->cell_bytes;
+  std::vector<unsigned char> cells(db->capacity * cb);
   uint64_t size = 0;
-  k2g_status s = k2g_db_download(db, cells.data(), &size);
+  k2g_status s = k2g_db_download(db, reinterpret_cast<uint32_t *>(cells.data()), &size);
   if (s != K2G_OK) return s;
   FILE *f = fopen(hash_k2d, "wb");
   if (!f) return fail(K2G_ERR_IO, std::string("unable to open ") + hash_k2d);
   uint64_t hdr[4] = {db->capacity, size, db->key_bits, db->value_bits};
-  bool ok = fwrite(hdr, 8, 4, f) == 4 && fwrite(cells.data(), 4, cells.size(), f) == cells.size();
+  bool ok = fwrite(hdr, 8, 4, f) == 4 && fwrite(cells.data(), cb, db->capacity, f) == db->capacity;
   ok = (fclose(f) == 0) && ok;
   if (!ok) return fail(K2G_ERR_IO, std::string("error writing ") + hash_k2d);
   return K2G_OK;

@@ -23,7 +23,7 @@ constexpr uint32_t kMaxBins = 56 * 1024;   // 224 KB of 32-bit counts (a block m
 __global__ void __launch_bounds__(kHistThreads)
 value_hist_kernel(const uint4 *cells, uint64_t n_vec, uint32_t value_mask, uint32_t lo,
                   uint32_t bins, uint32_t node_count, unsigned long long *counts,
-                  unsigned long long *outside, int count_outside) {
+                  unsigned long long *outside, int count_outside, int wide) {
   extern __shared__ uint32_t h[];
   for (uint32_t i = threadIdx.x; i < bins; i += blockDim.x) h[i] = 0;
   __syncthreads();
@@ -47,10 +47,12 @@ value_hist_kernel(const uint4 *cells, uint64_t n_vec, uint32_t value_mask, uint3
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) {
+      // 32-bit cells: four per load; 64-bit cells (40-bit tables): two,
+      // their values in the low words
       add(c[u].x & value_mask);
-      add(c[u].y & value_mask);
+      if (!wide) add(c[u].y & value_mask);
       add(c[u].z & value_mask);
-      add(c[u].w & value_mask);
+      if (!wide) add(c[u].w & value_mask);
     }
   }
   if (count_outside && mine_outside) atomicAdd(outside, (unsigned long long)mine_outside);
@@ -70,8 +72,11 @@ extern "C" k2g_status k2g_db_value_counts(const k2g_db *db, uint64_t *counts, ui
   K2G_CUDA_TRY(cudaSetDevice(db->device));
   cudaStream_t st = (cudaStream_t)stream;
   const uint64_t n = db->node_count;
-  // the cells are padded to a multiple of 8 with empty cells
-  const uint64_t n_vec = (db->capacity + 7) / 8 * 2;
+  // the cells are padded to whole 32-byte sectors with empty cells
+  const bool wide = db->d_wide != nullptr;
+  const uint64_t n_vec = wide ? (db->capacity + 3) / 4 * 2 : (db->capacity + 7) / 8 * 2;
+  const uint4 *vec = wide ? reinterpret_cast<const uint4 *>(db->d_wide)
+                          : reinterpret_cast<const uint4 *>(db->d_cells);
   const uint32_t value_mask = db->value_bits >= 32 ? 0xFFFFFFFFu : (1u << db->value_bits) - 1u;
   unsigned long long *d_counts = nullptr, *d_outside = nullptr;
   K2G_CUDA_TRY(cudaMalloc(&d_counts, (std::max<uint64_t>(n, 1) + 1) * sizeof(unsigned long long)));
@@ -98,8 +103,8 @@ extern "C" k2g_status k2g_db_value_counts(const k2g_db *db, uint64_t *counts, ui
     const uint64_t blocks = std::max<uint64_t>(
         1, std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * sms, (n_vec + kHistThreads - 1) / kHistThreads));
     value_hist_kernel<<<(unsigned)blocks, kHistThreads, smem, st>>>(
-        reinterpret_cast<const uint4 *>(db->d_cells), n_vec, value_mask, (uint32_t)lo, bins,
-        (uint32_t)n, d_counts, d_outside, p == 0);
+        vec, n_vec, value_mask, (uint32_t)lo, bins, (uint32_t)n, d_counts, d_outside, p == 0,
+        wide ? 1 : 0);
     note_launches();
     e = cudaGetLastError();
   }

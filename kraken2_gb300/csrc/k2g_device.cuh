@@ -197,11 +197,66 @@ __device__ __forceinline__ uint32_t probe_continue(const TableView &t, uint64_t 
   }
 }
 
+// CompactHashTable::Get (src/compact_hash.h:355-374) over the 64-bit cells
+// of a 40-bit table.  The stored key is compared the way
+// CompactHashCell40::hashed_key rebuilds it, in 32-bit arithmetic
+// (src/compact_hash.h:61-64): its low 32 bits, so a compacted key wider
+// than 32 bits (fewer than 8 value bits) never matches.  Kept out of line:
+// the 32-bit tables' probes stay compact.
+static __device__ __noinline__ uint32_t probe_wide(const unsigned long long *wide, uint64_t capacity,
+                                            uint32_t key_shift, uint32_t value_bits,
+                                            uint32_t value_mask, uint64_t hc, uint64_t idx) {
+  const uint64_t ck = hc >> key_shift;
+  const uint64_t first = idx;
+  while (true) {
+    const unsigned long long cell = __ldg(wide + idx);
+    const uint32_t v = (uint32_t)cell & value_mask;
+    if (!v) return 0;
+    if ((uint64_t)(uint32_t)(cell >> value_bits) == ck) return v;
+    idx = idx + 1 == capacity ? 0 : idx + 1;
+    if (idx == first) return 0;
+  }
+}
+
+__device__ __forceinline__ uint32_t table_get_wide(const TableView &t, uint64_t hc) {
+  return probe_wide(t.wide, t.capacity, t.key_shift, t.value_bits, t.value_mask, hc,
+                    fast_mod(hc, t.div));
+}
+
 __device__ __forceinline__ uint32_t table_get(const TableView &t, uint64_t key) {
   uint64_t hc = murmur3(key);
+  if (t.wide) return table_get_wide(t, hc);
   uint64_t idx = fast_mod(hc, t.div);
   return probe_from(t, hc, idx, load_cell(t.cells + idx));
 }
+
+// The two cell layouts the build writes.  Cell32: CompactHashCell
+// (src/compact_hash.h:22-48), (compacted key << value_bits) | value in 32
+// bits.  CellWide: CompactHashCell40 (:50-90) held as the packed 5-byte cell
+// zero-extended to 64 bits -- the same (key << value_bits) | value -- whose
+// stored key is compared in 32 bits, as its hashed_key rebuilds it.
+struct Cell32 {
+  using T = uint32_t;
+  __device__ static T *table(uint32_t *cells, unsigned long long *) { return cells; }
+  __device__ static uint32_t value(T c, const TableView &t) { return c & t.value_mask; }
+  __device__ static bool match(T c, uint64_t ck, const TableView &t) {
+    return (uint64_t)(c >> t.value_bits) == ck;
+  }
+  __device__ static T make(uint64_t ck, uint32_t v, const TableView &t) {
+    return ((uint32_t)ck << t.value_bits) | v;
+  }
+};
+struct CellWide {
+  using T = unsigned long long;
+  __device__ static T *table(uint32_t *, unsigned long long *wide) { return wide; }
+  __device__ static uint32_t value(T c, const TableView &t) { return (uint32_t)c & t.value_mask; }
+  __device__ static bool match(T c, uint64_t ck, const TableView &t) {
+    return (uint64_t)(uint32_t)(c >> t.value_bits) == ck;
+  }
+  __device__ static T make(uint64_t ck, uint32_t v, const TableView &t) {
+    return ((T)ck << t.value_bits) | v;
+  }
+};
 
 // DNA code of an ASCII base (src/mmscanner.cc:20-46): ACGT in either case map
 // to 0..3; anything else is ambiguous (returns 0xFF).

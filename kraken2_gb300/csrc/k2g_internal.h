@@ -26,9 +26,13 @@ struct DivMagic {
 
 DivMagic make_div_magic(uint64_t d);
 
-// Read-only view of the table passed to kernels by value.
+// Read-only view of the table passed to kernels by value.  A table of
+// 40-bit cells (CompactHashCell40, src/compact_hash.h:50-90) is held as
+// 64-bit cells instead: each packed 5-byte cell zero-extended, i.e.
+// (key << value_bits) | value; `wide` then points to it and `cells` is null.
 struct TableView {
   const uint32_t *cells;
+  const unsigned long long *wide;
   uint64_t capacity;
   DivMagic div;
   uint32_t key_shift;     // 64 - key_bits
@@ -96,6 +100,10 @@ struct k2g_db {
   uint64_t capacity = 0, size = 0, key_bits = 0, value_bits = 0, node_count = 0;
   k2g_index_options opts{};
   uint32_t *d_cells = nullptr;    // capacity cells, padded to a multiple of 8
+  // 40-bit cells: capacity 64-bit cells (the 5-byte cell zero-extended),
+  // padded to a multiple of 4; d_cells is then null
+  unsigned long long *d_wide = nullptr;
+  uint32_t cell_bytes = 4;        // 4, or 5 for CompactHashCell40 files
   uint32_t *d_parent = nullptr;   // node_count entries
   uint64_t *d_size = nullptr;     // device-side size counter used by builds
   k2g::DivMagic div{};

@@ -46,12 +46,12 @@ namespace k2g {
 // Table utilities
 // ---------------------------------------------------------------------------
 
-__global__ void max_value_kernel(const uint32_t *cells, uint64_t n, uint32_t mask,
-                                 unsigned int *out) {
+__global__ void max_value_kernel(const uint32_t *cells, const unsigned long long *wide,
+                                 uint64_t n, uint32_t mask, unsigned int *out) {
   uint32_t m = 0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x)
-    m = max(m, cells[i] & mask);
+    m = max(m, (wide ? (uint32_t)wide[i] : cells[i]) & mask);
   for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
@@ -60,7 +60,7 @@ k2g_status max_table_value(const k2g_db *db, uint32_t *out) {
   unsigned int *d = nullptr;
   K2G_CUDA_TRY(cudaMalloc(&d, 4));
   K2G_CUDA_TRY(cudaMemset(d, 0, 4));
-  max_value_kernel<<<1216, 256>>>(db->d_cells, db->capacity,
+  max_value_kernel<<<1216, 256>>>(db->d_cells, db->d_wide, db->capacity,
                                   (uint32_t)((1ull << db->value_bits) - 1), d);
   note_launches();
   cudaError_t e = cudaMemcpy(out, d, 4, cudaMemcpyDeviceToHost);
@@ -76,6 +76,11 @@ k2g_status max_table_value(const k2g_db *db, uint32_t *out) {
 __global__ void lookup_kernel(TableView t, const uint64_t *keys, uint32_t *vals, uint64_t n) {
   constexpr int B = 4;
   uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (t.wide) {   // 40-bit cells
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+      vals[i] = table_get_wide(t, murmur3(keys[i]));
+    return;
+  }
   for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += stride * B) {
     uint64_t hc[B], idx[B];
     Sector sec[B];
@@ -158,22 +163,23 @@ __global__ void scan_kernel(ScanView sv, const uint8_t *bases, const uint64_t *s
 // SetMinimizerLCA (src/build_db.h:187-194) on top of a lock-free
 // CompareAndSet (src/compact_hash.h:417-462): the cell is claimed or updated
 // with atomicCAS, and a lost race re-reads the cell and re-evaluates.
-__device__ __forceinline__ uint32_t insert_lca(const TableView &t, uint32_t *cells,
+template <class C>
+__device__ __forceinline__ uint32_t insert_lca(const TableView &t, typename C::T *cells,
                                                const uint32_t *parent, uint64_t key,
                                                uint32_t taxid, unsigned long long *size,
                                                uint32_t *status) {
   const uint64_t hc = murmur3(key);
-  const uint32_t ck = (uint32_t)(hc >> t.key_shift);
+  const uint64_t ck = hc >> t.key_shift;
   uint64_t idx = fast_mod(hc, t.div);
   const uint64_t first = idx;
   while (true) {
-    uint32_t cell = cells[idx];
-    uint32_t v = cell & t.value_mask;
-    if (!v || (cell >> t.value_bits) == ck) {
+    typename C::T cell = cells[idx];
+    uint32_t v = C::value(cell, t);
+    if (!v || C::match(cell, ck, t)) {
       uint32_t want = v ? lca(parent, v, taxid) : taxid;
       if (v && want == v) return 1;   // already holds the LCA
-      uint32_t nc = (ck << t.value_bits) | want;
-      uint32_t prev = atomicCAS(cells + idx, cell, nc);
+      const typename C::T nc = C::make(ck, want, t);
+      const typename C::T prev = atomicCAS(cells + idx, cell, nc);
       if (prev == cell) {
         if (!v) atomicAdd(size, 1ull);
         return 1;
@@ -188,7 +194,8 @@ __device__ __forceinline__ uint32_t insert_lca(const TableView &t, uint32_t *cel
   }
 }
 
-__global__ void insert_kernel(TableView t, uint32_t *cells, const uint32_t *parent,
+template <class C>
+__global__ void insert_kernel(TableView t, typename C::T *cells, const uint32_t *parent,
                               uint64_t node_count, const uint64_t *keys, const uint32_t *taxids,
                               uint64_t n, unsigned long long *size, uint32_t *status) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -199,7 +206,7 @@ __global__ void insert_kernel(TableView t, uint32_t *cells, const uint32_t *pare
       atomicOr(status, STATUS_BUILD_VALUE);
       continue;
     }
-    insert_lca(t, cells, parent, keys[i], tx, size, status);
+    insert_lca<C>(t, cells, parent, keys[i], tx, size, status);
   }
 }
 
@@ -760,7 +767,10 @@ extern "C" k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint
   if (depth != 1 && depth != 2 && depth != 4 && depth != 8 && depth != 16)
     return fail(K2G_ERR_ARG, "depth must be 1, 2, 4, 8 or 16");
   if (bytes != 32 && bytes != 64 && bytes != 128) return fail(K2G_ERR_ARG, "bytes must be 32, 64 or 128");
-  const uint64_t n_units = db->capacity / (bytes / 4);   // whole units of cells
+  // the table's memory as 32-bit words (a 40-bit table holds 64-bit cells)
+  const uint32_t *raw = db->d_wide ? reinterpret_cast<const uint32_t *>(db->d_wide) : db->d_cells;
+  const uint64_t words = db->capacity * (db->d_wide ? 2 : 1);
+  const uint64_t n_units = words / (bytes / 4);   // whole units
   if (issued) *issued = 0;
   if (!n_loads || !n_units) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(db->device));
@@ -771,11 +781,11 @@ extern "C" k2g_status k2g_sector_gather(const k2g_db *db, uint64_t n_loads, uint
   const unsigned blocks = (unsigned)(threads / 256);
   const cudaStream_t st = (cudaStream_t)stream;
   switch (depth) {
-    case 1: launch_gather<1>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
-    case 2: launch_gather<2>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
-    case 4: launch_gather<4>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
-    case 8: launch_gather<8>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
-    default: launch_gather<16>(bytes, db->d_cells, n_units, per, blocks, d_sink, st); break;
+    case 1: launch_gather<1>(bytes, raw, n_units, per, blocks, d_sink, st); break;
+    case 2: launch_gather<2>(bytes, raw, n_units, per, blocks, d_sink, st); break;
+    case 4: launch_gather<4>(bytes, raw, n_units, per, blocks, d_sink, st); break;
+    case 8: launch_gather<8>(bytes, raw, n_units, per, blocks, d_sink, st); break;
+    default: launch_gather<16>(bytes, raw, n_units, per, blocks, d_sink, st); break;
   }
   note_launches();
   K2G_CUDA_TRY(cudaGetLastError());
@@ -895,9 +905,14 @@ extern "C" k2g_status k2g_build_insert(k2g_db *db, const uint64_t *d_keys, const
   K2G_CUDA_TRY(cudaMemsetAsync(d_status, 0, 4, st));
   TableView t = db->table_view();
   uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count(db->device) * 32);
-  insert_kernel<<<(unsigned)std::max<uint64_t>(1, blocks), 256, 0, st>>>(
-      t, db->d_cells, db->d_parent, db->node_count, d_keys, d_taxids, n,
-      reinterpret_cast<unsigned long long *>(db->d_size), d_status);
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, blocks);
+  unsigned long long *d_size = reinterpret_cast<unsigned long long *>(db->d_size);
+  if (db->d_wide)
+    insert_kernel<CellWide><<<grid, 256, 0, st>>>(t, db->d_wide, db->d_parent, db->node_count,
+                                                  d_keys, d_taxids, n, d_size, d_status);
+  else
+    insert_kernel<Cell32><<<grid, 256, 0, st>>>(t, db->d_cells, db->d_parent, db->node_count,
+                                                d_keys, d_taxids, n, d_size, d_status);
   note_launches();
   uint32_t status = 0;
   cudaError_t e = cudaGetLastError();

@@ -52,7 +52,7 @@ __device__ __forceinline__ uint64_t pipe_gbase(const PipeArgs &p, uint64_t f) {
 template <int W>
 struct ScanLane {
   const uint8_t *ap, *aq;
-  uint32_t head, nchunks, ci, len;
+  uint32_t head, nchunks, nreal, ci, len;
   const uint8_t *seq2, *qual2;
   uint32_t len2, mate;
   uint4 c0, c1, q0, q1;
@@ -74,7 +74,8 @@ __device__ __forceinline__ void scanlane_mate(ScanLane<W> &s, const uint8_t *seq
   s.ap = seq - head;
   s.aq = qual ? qual - head : nullptr;
   s.len = len;
-  s.nchunks = (head + len + 15) / 16;
+  s.nchunks = (head + len + 15) / 16;   // aligned chunks holding the mate
+  s.nreal = (len + 15) / 16;            // chunks of the mate realigned to base 0
   s.ci = 0;
   s.c0 = load_chunk(s.ap, 0, s.nchunks);
   s.c1 = load_chunk(s.ap, 1, s.nchunks);
@@ -195,6 +196,23 @@ __device__ __forceinline__ void pipe_scan_word5(ScanLane<5> &s, const PipeArgs &
   pipe_scan_emit(s, pa, c, p0 + 3, amb[3], m3 ^ c.toggle, skey, sslot, nst);
 }
 
+// Chunk ci of a mate realigned to its first base: bytes [16 ci, 16 ci + 16)
+// of the mate, cut from the aligned chunks ci (a) and ci + 1 (b) that hold
+// it, the mate starting `head` bytes into aligned chunk 0.  Every lane then
+// sees base 4 j at the start of its word j, whatever its read's alignment,
+// so the lanes of a warp reach the clean-word path at the same word.
+__device__ __forceinline__ uint4 realign_chunk(uint4 a, uint4 b, uint32_t head) {
+  const uint32_t q = head >> 2, sel = 0x3210u + (head & 3u) * 0x1111u;
+  const uint32_t d[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  uint32_t e[6], f[5];
+#pragma unroll
+  for (int k = 0; k < 6; k++) e[k] = (q & 2u) ? d[k + 2] : d[k];
+#pragma unroll
+  for (int k = 0; k < 5; k++) f[k] = (q & 1u) ? e[k + 1] : e[k];
+  return make_uint4(__byte_perm(f[0], f[1], sel), __byte_perm(f[1], f[2], sel),
+                    __byte_perm(f[2], f[3], sel), __byte_perm(f[3], f[4], sel));
+}
+
 // The token of a k-mer that is unambiguous and emitted (pipe_scan_emit with
 // emit true and amb false): a new minimizer opens a KEY (or SKIP) group, a
 // repeat continues the open group unless that group is ambiguous.
@@ -306,7 +324,7 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
   while (__any_sync(0xffffffffu, !s.done)) {
     int nst = 0;
     if (!s.done) {
-      if (s.ci >= s.nchunks) {
+      if (s.ci >= s.nreal) {
         if (s.gkind != G_NONE) pa.gstream[s.gbase + s.ng++] = make_group(s.gkind, s.glen);
         s.gkind = G_NONE;
         if (a.cls.paired && s.mate == 0) {
@@ -318,16 +336,16 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
           s.done = true;
         }
       } else {
-        const uint4 cur = s.c0;
+        const uint4 cur = realign_chunk(s.c0, s.c1, s.head);
         s.c0 = s.c1;
         s.c1 = load_chunk(s.ap, s.ci + 2, s.nchunks);
         uint4 qc = make_uint4(0, 0, 0, 0);
         if (QUAL) {
-          qc = s.q0;
+          qc = realign_chunk(s.q0, s.q1, s.head);
           s.q0 = s.q1;
           s.q1 = load_chunk(s.aq, s.ci + 2, s.nchunks);
         }
-        const int32_t pbase = (int32_t)(16 * s.ci) - (int32_t)s.head;
+        const int32_t pbase = (int32_t)(16 * s.ci);
 #pragma unroll 1
         for (int wi = 0; wi < 4; wi++) {
           const uint32_t wd = wi == 0 ? cur.x : (wi == 1 ? cur.y : (wi == 2 ? cur.z : cur.w));
@@ -339,8 +357,6 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
             if (c.qall) ok = 0;
           }
           const int32_t p0 = pbase + 4 * wi;
-          const int32_t before = -p0;
-          if (before > 0) ok = before >= 4 ? 0u : (ok & (0xFFFFFFFFu << (8 * before)));
           if constexpr (W == 5 && K2G_SCAN_WORD5) {
             const bool clean = ok == 0x01010101u && s.run + 1 >= c.l && p0 - s.last_amb > c.amb_span &&
                                p0 >= c.k - 1 && p0 + 3 < (int32_t)s.len;
@@ -405,6 +421,15 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
   const uint64_t rbase = pipe_gbase(pa, f0);
   const uint32_t cnt = pa.bcount[blk];
   const TableView &t = pa.a.table;
+  if (t.wide) {   // 40-bit cells (uniform over the block: no barrier is skipped by part of it)
+    for (uint32_t i = part * kPipeBlock + threadIdx.x; i < cnt; i += stride) {
+      const uint64_t key = pa.rkey[rbase + i];
+      const uint32_t slot = pa.rslot[rbase + i];
+      pa.gtax[rbase + slot] = table_get_wide(t, murmur3(key));
+      if (pa.gkey) pa.gkey[rbase + slot] = key;
+    }
+    return;
+  }
   if (threadIdx.x == 0) *s_cnt = 0;
   __syncthreads();
   for (uint32_t i0 = part * kPipeBlock + threadIdx.x; i0 < cnt; i0 += B * stride) {

@@ -71,7 +71,9 @@ struct Request {
   std::map<uint64_t, std::pair<uint64_t, std::vector<uint64_t>>> piece_runs;
   std::vector<uint64_t> runs;       // runs of fragments [0, runs_frags), in order
   uint64_t runs_frags = 0;
-  Clock::time_point t_submit, t_done;
+  // submit, first piece and last piece taken into a batch, done
+  Clock::time_point t_submit, t_first, t_last, t_done;
+  bool started = false;
   bool done = false;
   k2g_status status = K2G_OK;
   std::string error;
@@ -199,6 +201,12 @@ void form_batch(k2g_server *sv, Slot &s) {
       }
       break;
     }
+    const Clock::time_point now = Clock::now();
+    if (!r.started) {
+      r.started = true;
+      r.t_first = now;
+    }
+    r.t_last = now;
     s.pieces.push_back({&r, r.next, f - r.next});
     s.frags += f - r.next;
     s.bases += b;
@@ -466,6 +474,25 @@ extern "C" k2g_status k2g_server_fetch(k2g_server *sv, uint64_t ticket, uint32_t
   if (runs) par_copy(runs, r->runs.data(), r->runs.size() * 8);
   if (n_runs) *n_runs = r->runs.size();
   if (latency_s) *latency_s = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_server_timing(k2g_server *sv, uint64_t ticket, double *queued_s,
+                                        double *batching_s, double *running_s) {
+  if (!sv) return fail(K2G_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(sv->mu);
+  auto it = sv->reqs.find(ticket);
+  if (it == sv->reqs.end()) return fail(K2G_ERR_ARG, "unknown ticket");
+  const Request &r = *it->second;
+  if (!r.done) return fail(K2G_ERR_ARG, "request not finished");
+  auto secs = [](Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double>(b - a).count();
+  };
+  const Clock::time_point first = r.started ? r.t_first : r.t_done;
+  const Clock::time_point last = r.started ? r.t_last : r.t_done;
+  if (queued_s) *queued_s = secs(r.t_submit, first);
+  if (batching_s) *batching_s = secs(first, last);
+  if (running_s) *running_s = secs(last, r.t_done);
   return K2G_OK;
 }
 

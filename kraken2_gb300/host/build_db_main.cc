@@ -9,7 +9,7 @@
 // subblock start), each block's distinct minimizers inserted in the
 // reference's order.  -F (the reference's nondeterministic build) inserts
 // each sequence's minimizers unordered.  Protein libraries (-X) are scanned
-// as amino acids; 40-bit cells (-C 40) are refused.
+// as amino acids; -C 40 builds 40-bit cells (CompactHashCell40).
 #include <err.h>
 #include <getopt.h>
 #include <sysexits.h>
@@ -184,7 +184,6 @@ void parse_command_line(int argc, char **argv, Options &o) {
               << std::endl;
     usage();
   }
-  if (o.cht_cell_size != 32) errx(EX_USAGE, "40-bit cells (-C 40) are not supported");
 }
 
 // ReadIDToTaxonMap (src/build_db.cc:147-163): "<seqid> <taxid>" per line
@@ -289,8 +288,11 @@ int main(int argc, char **argv) {
   std::vector<uint64_t> parent(tax.nodes.size());
   for (size_t i = 0; i < parent.size(); i++) parent[i] = tax.nodes[i].parent_id;
   k2g_db *db = nullptr;
-  if (k2g_db_create(&idx, actual_capacity, 32 - (uint32_t)bits_for_taxid, (uint32_t)bits_for_taxid,
-                    parent.data(), parent.size(), 0, &db) != K2G_OK)
+  // CompactHashTable<Cell>(capacity, cell bits - value bits, value bits)
+  // (src/build_db.cc:86-90)
+  const uint32_t cell_bits = (uint32_t)o.cht_cell_size;
+  if (k2g_db_create(&idx, actual_capacity, cell_bits - (uint32_t)bits_for_taxid,
+                    (uint32_t)bits_for_taxid, parent.data(), parent.size(), 0, &db) != K2G_OK)
     errx(EX_SOFTWARE, "%s", k2g_last_error());
   std::cerr << "CHT created with " << bits_for_taxid << " bits reserved for taxid." << std::endl;
 

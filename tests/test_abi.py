@@ -91,11 +91,17 @@ def test_hash_capacity_mismatch(tmp_path):
     assert _open_status(d) == 3
 
 
-def test_forty_bit_cells_unsupported(tmp_path):
+def test_forty_bit_cells_checked(tmp_path):
+    """Key + value bits of 40 select packed 5-byte cells (GetKVStoreCellType,
+    src/kv_store.h:35-57): a 40-bit header over 4-byte cells is a capacity
+    mismatch; value bits beyond 31 are refused as unsupported."""
     d = _copy_db(tmp_path)
     p = os.path.join(d, "hash.k2d")
     raw = bytearray(open(p, "rb").read())
     struct.pack_into("<QQ", raw, 16, 24, 16)
+    open(p, "wb").write(raw)
+    assert _open_status(d) == 3
+    struct.pack_into("<QQ", raw, 16, 8, 32)
     open(p, "wb").write(raw)
     assert _open_status(d) == 7
 

@@ -53,11 +53,15 @@ def test_usage_and_errors_match_reference(case):
     assert r.stderr.decode() == case["stderr"]
 
 
-def test_wide_cells_refused():
-    base = ["-H", "h", "-m", "m", "-t", "t", "-n", "n", "-o", "o", "-k", "15", "-l", "12",
-            "-c", "9"]
-    r = subprocess.run([exe(), *base, "-C", "40"], capture_output=True)
-    assert r.returncode == 64 and b"not supported" in r.stderr
+def test_wide_cells_parse():
+    """-C 40 is accepted (40-bit cells; tables checked on the GPU in
+    test_gpu_cells40.py), any other cell size refused as the reference does."""
+    base = ["-H", "h", "-m", "m", "-t", "t", "-n", "/nonexistent", "-o", "o", "-k", "15",
+            "-l", "12", "-c", "9"]
+    r = subprocess.run([exe(), *base, "-C", "40"], capture_output=True, stdin=subprocess.DEVNULL)
+    assert r.returncode != 64, r.stderr.decode()
+    r = subprocess.run([exe(), *base, "-C", "36"], capture_output=True, stdin=subprocess.DEVNULL)
+    assert r.returncode == 64 and b"CHT cell size should be either 32 or 40 bits" in r.stderr
 
 
 @pytest.mark.parametrize("name,want", VARIANTS, ids=[v for v, _ in VARIANTS])

@@ -3,8 +3,9 @@ reference (tests/golden/cells40.json, made by tests/golden/make_cells40.py):
 the oracle's build restatement over packed 5-byte cells reproduces the
 reference's tables byte for byte -- including its 32-bit key reassembly,
 which with 7 value bits loses the top bit of 33-bit keys -- and classification
-against them reproduces the reference's lines and reports.  CPU only; the GPU
-path reads 32-bit cells."""
+against them reproduces the reference's lines and reports.  CPU only; the
+GPU path's builds and classification of the same tables are checked in
+test_gpu_cells40.py."""
 import hashlib
 import json
 import os

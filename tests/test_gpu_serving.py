@@ -113,3 +113,30 @@ def test_server_rejects_oversized_fragment_only():
     sv.fetch(t_empty, 0, 1)
     sv.close()
     db.close()
+
+
+def test_server_timing_parts_add_up_to_the_latency():
+    """k2g_server_timing splits each request's latency into time queued,
+    time between its first and last batch, and time running after that;
+    with a small budget a request spans several batches."""
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    b = batch_of("se150")
+    params = k2g.ClassifyParams(0.1, 2, 0, 0, 0)
+    ref = reference(db, b, params)
+    sv = k2g.Server(db, params, 2_000_000)   # a slot holds a few thousand reads
+    try:
+        n = b.n_frags
+        tickets = [(submit_range(sv, b, a, min(n, a + 700), 1), a, min(n, a + 700))
+                   for a in range(0, n, 700)]
+        for t, a, z in tickets:
+            assert sv.wait(t, 120)
+            q, bt, r = sv.timing(t)
+            assert q >= 0 and bt >= 0 and r >= 0
+            got = sv.fetch(t)
+            check(ref, a, z, got)
+            assert abs((q + bt + r) - got[4]) < 1e-6
+        with pytest.raises(k2g.K2GError):
+            sv.timing(tickets[0][0])   # fetched requests are released
+    finally:
+        sv.close()
+        db.close()
