@@ -38,6 +38,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+T_START = time.time()
+
+
+def stage(log, what: str):
+    """Progress line with the seconds since the benchmark started."""
+    log(f"[{time.time() - T_START:7.1f}s] {what}")
 FALLBACK_HBM_GBS = 6800.0
 SEED_TEMPLATE = "1" * 17 + "01" * 7
 TOGGLE = 0xe37e28c4271b5a2d
@@ -752,17 +758,20 @@ def build_library_db(k2g, genomes: np.ndarray, glen: int, taxa: np.ndarray, pare
     (db, build description)."""
     n_g = len(taxa)
     vb = _bits_for(len(parent))
+    import torch
     probe = k2g.Database.create(_small_opts(k2g), 64, 32 - vb, vb, parent)
-    sample = np.zeros(0, np.uint64)
+    sample = None   # distinct sampled minimizers so far (as int64, on the GPU)
     t0 = time.time()
     for g0 in range(0, n_g, batch_genomes):
         g1 = min(n_g, g0 + batch_genomes)
         off = np.arange(g1 - g0 + 1, dtype=np.uint64) * glen
         keys = probe.sample_minimizers(genomes[g0 * glen:g1 * glen], off, 64,
                                        keys_cap=(g1 - g0) * glen // 16)
-        sample = np.union1d(sample, keys)
+        t = torch.from_numpy(keys.view(np.int64)).to("cuda")
+        sample = torch.unique(t if sample is None else torch.cat([sample, t]))
     probe.close()
     estimate = int(len(sample)) * 1024 // 64 + 8192
+    del sample
     required = int(estimate / 0.7)
     capacity, min_hash = required, 0
     if max_bytes and max_bytes < required * 4:
@@ -803,6 +812,24 @@ class TableOracle:
             bases, None, off.astype(np.uint64), n, threads=os.cpu_count() or 1,
             confidence=params.confidence, min_hit_groups=params.min_hit_groups, paired=paired)
         return calls, hg, nr, runs, base
+
+    def classify_bounded(self, bases_of, off: np.ndarray, n_max: int, params, paired: bool,
+                         budget_s: float, chunk: int = 50_000):
+        """The oracle on fragments [0, n) in chunks of `chunk`, stopping at
+        n_max or once budget_s seconds have passed (n >= one chunk).
+        bases_of(a, z) returns the bases [a, z) as bytes.  Returns (outputs
+        over the first n fragments as classify gives them, n)."""
+        per = 2 if paired else 1
+        parts, done, runs_total, t0 = [], 0, 0, time.time()
+        while done < n_max and (done == 0 or time.time() - t0 < budget_s):
+            m = min(chunk, n_max - done)
+            a, z = int(off[done * per]), int(off[(done + m) * per])
+            o = (off[done * per:(done + m) * per + 1].astype(np.int64) - a).astype(np.uint64)
+            calls, hg, nr, runs, base = self.classify(bases_of(a, z), o, m, params, paired)
+            parts.append((calls, hg, nr, runs, base + np.uint64(runs_total)))
+            runs_total += len(runs)
+            done += m
+        return tuple(np.concatenate([p[k] for p in parts]) for k in range(5)), done
 
 
 def _host_runs(bufs, n):
@@ -1063,7 +1090,7 @@ def _uneven_dev(torch, G, pick, lens: np.ndarray, g, dev, subs=0.04, indel=0.01)
 
 
 def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
-                parity_uneven: int = 1_000_000) -> dict:
+                parity_uneven: int = 1_000_000, parity_budget_s: float = 90.0) -> dict:
     """The mid-size database (5,000-node taxonomy of depth <= 12; 2,000
     genomes of 2 Mb from a seeded ancestral-mutation tree at 0.5-5%
     divergence per edge; built on the GPU into a 2 GB table, the way
@@ -1085,7 +1112,7 @@ def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
     t0 = time.time()
     G = mutation_tree_genomes(torch, parent, glen, 41, dev)
     torch.cuda.synchronize(dev)
-    log(f"mutation tree: {len(parent)} genomes x {glen} bp in {time.time() - t0:.1f}s")
+    stage(log, f"mutation tree: {len(parent)} genomes x {glen} bp in {time.time() - t0:.1f}s")
     pick = torch.from_numpy(chosen.astype(np.int64)).to(dev)
     lib = G[pick].cpu().numpy().reshape(-1)
     db, binfo = build_library_db(k2g, lib, glen, chosen.astype(np.uint32), parent, 2_000_000_000, log)
@@ -1133,8 +1160,9 @@ def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
                   k2g.MODE_PIPELINED, st)
     torch.cuda.synchronize(dev)
     gpu = _host_runs(bufs, ns)
-    host = bases[:ns * 2 * L].cpu().numpy().tobytes()
-    oo = orc.classify(host, np.arange(2 * ns + 1, dtype=np.uint64) * L, ns, params, True)
+    oo, ns = orc.classify_bounded(lambda a, z: bases[a:z].cpu().numpy().tobytes(),
+                                  np.arange(2 * ns + 1, dtype=np.uint64) * L, ns, params, True,
+                                  parity_budget_s)
     out["paired_2x150"] = {
         "pairs": n_pairs, "confidence": 0.1, "fragment_len": "N(300, 50), mate 2 reverse-complemented",
         "substitutions": 0.01, "call_pairs": batch,
@@ -1149,7 +1177,7 @@ def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
         "plain_block_form": "one synchronous MODE_PLAIN launch per 10,000-pair reader batch",
         "batched_over_plain_block": round(t_plain_block / t_batched, 3),
         "parity": {"pairs": ns, **_parity(gpu, oo, ns)}}
-    log(f"paired: {out['paired_2x150']['mreads_min']} Mreads/min")
+    stage(log, f"paired: {out['paired_2x150']['mreads_min']} Mreads/min, parity on {ns} pairs")
     del bases, off, bufs
     torch.cuda.empty_cache()
 
@@ -1160,6 +1188,7 @@ def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
     rng.shuffle(lens)
     seqs, offs = _uneven_dev(torch, G, pick, lens, g, dev)
     del G
+    stage(log, "uneven reads generated")
     torch.cuda.empty_cache()
     n = len(lens)
     tot = int(offs[-1])
@@ -1183,19 +1212,31 @@ def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
     cls = k2g.length_class(tot, n)
     default = db.tuning(0, cls).as_dict()
     t_default = one_call(k2g.MODE_PIPELINED)
-    rd, res = _classify_dev(k2g, db, seqs, d_off, n, max_len, tot, params, bufs, runs_cap,
-                            k2g.MODE_PIPELINED, st)
-    chosen_t, _ = db.autotune(rd, params, res, trials=1, stream=st)
+    stage(log, f"uneven default call {t_default:.3f}s")
+    # a call of several seconds (reads sent to the one-thread-per-read slow
+    # path) would make the autotuner's and the plain form's calls run on
+    # far longer than the whole run's budget: they are then left out
+    slow = t_default > 5.0
+    chosen_t = db.tuning(0, cls)
+    if not slow:
+        rd, res = _classify_dev(k2g, db, seqs, d_off, n, max_len, tot, params, bufs, runs_cap,
+                                k2g.MODE_PIPELINED, st)
+        chosen_t, _ = db.autotune(rd, params, res, trials=1, stream=st)
+        stage(log, "uneven autotuned")
     t_batched = one_call(k2g.MODE_PIPELINED)
     calls_b = bufs["call"][:n].cpu().numpy().copy()
-    t_plain = one_call(k2g.MODE_PLAIN)
-    same = bool(np.array_equal(calls_b, bufs["call"][:n].cpu().numpy()))
+    t_plain, same = None, None
+    if not slow:
+        t_plain = one_call(k2g.MODE_PLAIN)
+        stage(log, "uneven plain form timed")
+        same = bool(np.array_equal(calls_b, bufs["call"][:n].cpu().numpy()))
     one_call(k2g.MODE_PIPELINED)
     # oracle parity on the first reads of the call (long and short mixed)
     ns = min(parity_uneven, n)
     gpu = _host_runs(bufs, ns)
-    host = seqs[:int(offs[ns])].cpu().numpy().tobytes()
-    oo = orc.classify(host, offs[:ns + 1].astype(np.uint64), ns, params, False)
+    oo, ns = orc.classify_bounded(lambda a, z: seqs[a:z].cpu().numpy().tobytes(),
+                                  offs[:ns + 1].astype(np.uint64), ns, params, False,
+                                  parity_budget_s, chunk=20_000)
     out["uneven_lengths"] = {
         "reads": n, "bases": tot,
         "lengths": "1M log-normal mean 5 kb (150 bp - 50 kb) + 5M x 150 bp, interleaved",
@@ -1204,11 +1245,13 @@ def mid_db_runs(log, n_pairs: int = 10_000_000, parity_pairs: int = 1_000_000,
         "mreads_min": round(n / t_batched * 60 / 1e6, 1), "gbases_per_s": round(tot / t_batched / 1e9, 2),
         "default_gbases_per_s": round(tot / t_default / 1e9, 2),
         "tuning": {"default": default, "chosen": chosen_t.as_dict(), "gain": round(t_default / t_batched, 3)},
-        "plain_mreads_min": round(n / t_plain * 60 / 1e6, 1),
-        "plain_form": "one MODE_PLAIN launch, one thread per read (no work stealing, no pieces)",
-        "batched_over_plain": round(t_plain / t_batched, 3), "plain_calls_identical": same,
+        "plain_mreads_min": round(n / t_plain * 60 / 1e6, 1) if t_plain else None,
+        "plain_form": "one MODE_PLAIN launch, one thread per read (no work stealing, no pieces)"
+                      if t_plain else "left out: the default call took over 5 s",
+        "batched_over_plain": round(t_plain / t_batched, 3) if t_plain else None,
+        "plain_calls_identical": same,
         "parity": {"reads": ns, "long_reads": int((rl[:ns] > 300).sum()), **_parity(gpu, oo, ns)}}
-    log(f"uneven: {out['uneven_lengths']['gbases_per_s']} Gbases/s")
+    stage(log, f"uneven: {out['uneven_lengths']['gbases_per_s']} Gbases/s, parity on {ns} reads")
     del seqs, bufs, d_off
     db.close()
     torch.cuda.empty_cache()
@@ -1296,6 +1339,88 @@ def e2e_run(wl: Workload, n_reads: int, steps: int):
     h2d = n_reads * L + (n_reads + 1) * 8
     d2h = n_reads * 12 + used * 8
     return t, h2d, d2h, call.numpy().view(np.uint32).copy()
+
+
+def fastq_bytes(reads: np.ndarray, L: int, first_id: int = 0) -> np.ndarray:
+    """Fixed-width FASTQ records "@r<10 digits>", the read, "+", quality 'I'
+    (317 bytes per 150 bp read) as one uint8 array."""
+    n = len(reads) // L
+    w = 12 + 1 + L + 3 + L + 1
+    a = np.empty((n, w), np.uint8)
+    a[:, 0] = ord("@")
+    a[:, 1] = ord("r")
+    ids = np.arange(first_id, first_id + n, dtype=np.int64)
+    for d in range(10):
+        a[:, 2 + d] = ord("0") + (ids // 10 ** (9 - d)) % 10
+    a[:, 12] = ord("\n")
+    a[:, 13:13 + L] = reads.reshape(n, L)
+    a[:, 13 + L] = ord("\n")
+    a[:, 14 + L] = ord("+")
+    a[:, 15 + L] = ord("\n")
+    a[:, 16 + L:16 + 2 * L] = ord("I")
+    a[:, 16 + 2 * L] = ord("\n")
+    return a.reshape(-1)
+
+
+def text_e2e_run(wl: Workload, n_reads: int, steps: int, chunk: int = 256 << 20):
+    """The text path end to end: FASTQ bytes of n_reads reads in pinned host
+    memory go through k2g_text_classify chunk by chunk (parsed, cut into
+    3 MiB reader blocks, classified and formatted on the device) and every
+    chunk's kraken lines come back (k2g_text_fetch) into pinned memory; the
+    copies both ways are inside the timing.  Checked against the calls of
+    the k2g_classify_host run on the same reads."""
+    torch, cfg, k2g = wl.torch, wl.cfg, wl.k2g
+    L = cfg.read_len
+    # taxonomy fields for the lines: external id = internal id, names "t<id>"
+    wl.db.set_names(np.arange(cfg.nodes, dtype=np.uint64), [b"t%d" % i for i in range(cfg.nodes)])
+    fq = fastq_bytes(wl.reads[:n_reads * L].cpu().numpy(), L)
+    text_in = torch.empty(len(fq), dtype=torch.uint8, pin_memory=True)
+    text_in.numpy()[:] = fq
+    del fq
+    out = torch.empty(n_reads * 96 + (64 << 20), dtype=torch.uint8, pin_memory=True)
+    params = k2g.ClassifyParams(cfg.confidence, cfg.min_hit_groups, 0, 0, 0)
+    tr = k2g.TextReader(wl.db, params, chunk_cap=chunk)
+    lib = k2g.lib()
+    base_in, base_out, total = text_in.data_ptr(), out.data_ptr(), text_in.numel()
+    times, out_len, frags = [], 0, 0
+    for _ in range(steps + 1):
+        tr.reset()
+        t0 = time.perf_counter()
+        pos, out_len, frags = 0, 0, 0
+        k2g.check(lib.k2g_text_prefetch(tr.h, base_in, min(chunk, total)))
+        while True:
+            n = min(chunk, total - pos)
+            if pos + n < total:   # the next chunk's copy overlaps this chunk's work
+                k2g.check(lib.k2g_text_prefetch(tr.h, base_in + pos + n, min(chunk, total - pos - n)))
+            res = k2g.TextResult()
+            k2g.check(lib.k2g_text_classify(tr.h, base_in + pos, n, int(pos + n >= total), None,
+                                            C.byref(res)))
+            if out_len + res.text_len > out.numel():
+                raise RuntimeError("kraken lines larger than the output buffer")
+            k2g.check(lib.k2g_text_fetch(tr.h, base_out + out_len, res.text_len))
+            out_len += res.text_len
+            frags += res.fragments
+            pos += n
+            if res.handoff:
+                raise RuntimeError("the text path handed the input back")
+            if pos >= total:
+                break
+        times.append(time.perf_counter() - t0)
+    tr.close()
+    t = float(np.median(times[1:]))
+    # the taxid column of the lines ("C\tr<10 digits>\t<taxid>\t..."), vectorised
+    a = out.numpy()[:out_len]
+    nl = np.flatnonzero(a == 10)
+    at = np.concatenate([[0], nl[:-1] + 1]).astype(np.int64) + 14
+    M = a[at[:, None] + np.arange(11)[None, :]].astype(np.uint64)
+    digit = (M >= 48) & (M <= 57)
+    ndig = np.argmin(digit, axis=1)
+    calls = np.zeros(len(at), np.uint64)
+    for j in range(11):
+        calls = np.where(j < ndig, calls * np.uint64(10) + (M[:, j] - np.uint64(48)), calls)
+    del text_in, out, a, M, digit
+    return {"s_per_step": t, "h2d_bytes_per_step": int(total), "d2h_bytes_per_step": int(out_len),
+            "fragments": frags, "calls": calls}
 
 
 def dist_setup(n_gpus: int):
@@ -1481,6 +1606,7 @@ def run_ours(args, log):
         end.record(wl.stream)
         torch.cuda.synchronize()
     launches = wl.k2g.kernel_launches() - launches0
+    stage(log, "timed steps done")
     ms_total = max_over_ranks(pg, start.elapsed_time(end))
     ms_step = ms_total / args.steps
     if int(runner.status.cpu()[0]):
@@ -1507,6 +1633,7 @@ def run_ours(args, log):
         pe.record(wl.stream)
         torch.cuda.synchronize()
         plain = cfg.n_reads / (ps.elapsed_time(pe) / 1e3)
+        stage(log, "plain form done")
 
     # --report-minimizer-data (-K): the same reads with add_kmer events and the
     # HyperLogLog++ taxon counters, one full pass timed end to end on the host
@@ -1572,20 +1699,40 @@ def run_ours(args, log):
         gpu_calls.append(pr.call[:n].cpu().numpy().view(np.uint32).copy())
     gpu_calls = np.concatenate(gpu_calls)
     mismatches = int((gpu_calls.astype(np.uint64) != ocalls).sum())
+    stage(log, "cpu baseline and parity done")
     del cells
 
     e2e_t, h2d, d2h, e2e_calls = e2e_run(wl, cfg.e2e_reads, max(2, min(args.steps, 5)))
+    stage(log, "e2e done")
+    te = text_e2e_run(wl, cfg.e2e_reads, max(2, min(args.steps, 3)))
+    text_e2e = {"value": round(te["fragments"] / te["s_per_step"] * 60 / 1e6, 3),
+                "unit": "Mreads/min",
+                "h2d_bytes_per_step": te["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": te["d2h_bytes_per_step"],
+                "reads_per_step": te["fragments"], "s_per_step": round(te["s_per_step"], 4),
+                "form": "FASTQ bytes in (pinned host), kraken lines out (pinned host): "
+                        "k2g_text_classify + k2g_text_fetch per 256 MiB chunk, the next "
+                        "chunk's copy in overlapped (k2g_text_prefetch)",
+                "calls_equal_classify_host": bool(np.array_equal(te["calls"],
+                                                                 e2e_calls.astype(np.uint64)))}
+    del te
+    stage(log, "text e2e done")
     serving = None if args.skip_serving else serving_run(wl, log)
+    stage(log, "serving done")
     long_reads = None if args.skip_serving else long_reads_run(wl, log)
     value_counts = value_counts_run(wl)
     small_calls = small_calls_run(wl)
+    stage(log, "long reads, value counts, small calls done")
     configs = None
     if not args.skip_configs:
         del runner
         torch.cuda.empty_cache()
         configs = {"small_db": small_db_run(log)}
+        stage(log, "small db done")
         configs.update(mid_db_runs(log))
+        stage(log, "mid db done")
         configs["build"] = build_run(log)
+        stage(log, "build done")
     e2e_rate = cfg.e2e_reads / e2e_t
 
     out = {
@@ -1631,6 +1778,7 @@ def run_ours(args, log):
         "e2e": {"value": round(e2e_rate * 60 / 1e6, 3), "unit": "Mreads/min",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "reads_per_step": cfg.e2e_reads, "s_per_step": round(e2e_t, 4)},
+        "e2e_text": text_e2e,
         "plain_vs_batched": ({"plain_mreads_min": round(plain * 60 / 1e6, 3),
                               "plain_form": "one synchronous launch per 3 MiB reader block",
                               "batched_over_plain": round(reads_s / plain, 3)} if plain else None),
@@ -1673,9 +1821,11 @@ class HostWorkload:
         self.src = ACGT[np.frombuffer(rng.bytes(n_src_b), np.uint8) & 3]
         self.opts = oracle.index_opts(cfg.k, cfg.l, spaced_mask(SEED_TEMPLATE), TOGGLE)
         self.cells = np.zeros(cfg.capacity, np.uint32)
+        stage(log, "host sources generated; filling the table")
         self.size = oracle.fill_table(self.cells, cfg.key_bits, cfg.value_bits, self.parent,
                                       self.opts, self.src, cfg.src_len, self.src_taxa, leaves,
                                       internal, int(cfg.capacity * cfg.load), 4, threads)
+        stage(log, "host table filled")
         L = cfg.read_len
         hit = rng.random(n_reads) < cfg.hit_frac
         gi = rng.integers(0, cfg.n_src, n_reads)
@@ -1711,6 +1861,7 @@ def run_reference(args, log):
     hw = HostWorkload(cfg, sample_cap, log=log)
     n = min(sample_cap, 200_000)
     dt = hw.classify(n, threads)
+    stage(log, f"first sample classified: {n} reads in {dt:.2f}s")
     n = int(min(sample_cap, n * args.cpu_seconds / 4 / max(dt, 1e-3)))
     for _ in range(args.warmup):
         hw.classify(min(n, 100_000), threads)

@@ -103,6 +103,15 @@ k2g_status k2g_db_create(const k2g_index_options *opts, uint64_t capacity,
 k2g_status k2g_db_close(k2g_db *db);
 k2g_status k2g_db_info_get(const k2g_db *db, k2g_db_info *out);
 
+/* Gives a database the taxonomy fields its kraken lines print, as taxo.k2d
+ * holds them (src/taxonomy.h TaxonomyNode external_id / name_offset and the
+ * name data): external_id and name_off have node_count entries; names holds
+ * NUL-terminated names, names_len bytes ending in NUL.  k2g_db_open sets
+ * them from the file; a table made by k2g_db_create has none until this is
+ * called. */
+k2g_status k2g_db_set_names(k2g_db *db, const uint64_t *external_id, const char *names,
+                            uint64_t names_len, const uint64_t *name_off);
+
 /* Copies the table back to the host and writes hash.k2d in the reference
  * layout -- CompactHashTable::WriteTable (src/compact_hash.h:344-352). */
 k2g_status k2g_db_write_hash(const k2g_db *db, const char *hash_k2d);
@@ -286,6 +295,24 @@ k2g_status k2g_counters_destroy(k2g_counters *c);
 k2g_status k2g_counters_add(k2g_counters *c, const k2g_reads *reads, const k2g_results *res,
                             void *stream);
 
+/* The counters' state, to combine the counters of several processes that
+ * classified different reader blocks (one per GPU) into one report -- the
+ * union the reference's threads form by merging their block sketches
+ * (src/hyperloglogplus.cc:573-651, merged by src/classify.cc:640-645):
+ * entries = the distinct (taxon, HLL++ encoding) pairs seen, n_entries of
+ * them, as opaque sorted 64-bit words; taxon_kmers = add_kmer calls per
+ * taxon; dense = 1 for a taxon some block's sketch of which went dense
+ * (node_count entries each).  With entries, taxon_kmers and dense all NULL
+ * only *n_entries is set.  Synchronises `stream`. */
+k2g_status k2g_counters_export(k2g_counters *c, uint64_t *entries, uint64_t cap,
+                               uint64_t *n_entries, uint64_t *taxon_kmers, uint8_t *dense,
+                               void *stream);
+/* Adds an exported state (of counters over the same taxonomy) to c: entries
+ * are united, counts added, dense flags or-ed, so c then finishes as one
+ * object that saw both sets of blocks would.  Synchronises `stream`. */
+k2g_status k2g_counters_import(k2g_counters *c, const uint64_t *entries, uint64_t n_entries,
+                               const uint64_t *taxon_kmers, const uint8_t *dense, void *stream);
+
 /* Per taxonomy node (node_count entries, host memory): taxon_kmers (may be
  * NULL) = add_kmer calls of the taxon, clade_kmers = of its subtree (the
  * report's minimizer column), clade_distinct = the HyperLogLog++ estimate of
@@ -317,6 +344,120 @@ k2g_status k2g_classify_host_blocks(const k2g_db *db, const char *bases, const c
                                     const k2g_classify_params *params, uint32_t *call,
                                     uint32_t *hit_groups, uint32_t *hitlist_len,
                                     uint64_t *runs, uint64_t *n_runs, uint64_t *taxon_reads);
+
+/* ---- output lines on the device: the kraken lines of a classified batch
+ * (src/classify.cc:908-991 -- TrimPairInfo :764-771, the call's external
+ * taxid or with -n its scientific name, mate lengths, AddHitlistString
+ * :950-991), formatted by GPU threads from the classification outputs and
+ * the reader's records, so only the text returns to the host. */
+
+/* A record's name: text[pos, pos + len).  A caller's own record array can be
+ * passed when each element starts with these two fields (ref_stride = its
+ * element size). */
+typedef struct {
+  uint64_t pos;
+  uint32_t len;
+} k2g_name_ref;
+
+typedef struct {
+  const uint32_t *call;          /* [n_frags] internal taxid, 0 = unclassified */
+  const uint32_t *hitlist_len;   /* [n_frags] hit-list runs per fragment      */
+  const uint64_t *runs;          /* the runs, fragment after fragment, as
+                                    k2g_classify_host returns them           */
+  uint64_t n_runs;
+  const char *text;              /* bytes holding the names                   */
+  uint64_t text_len;
+  const void *name_refs;         /* record r's name: the k2g_name_ref at
+                                    name_refs + r * ref_stride               */
+  uint64_t ref_stride;
+  const uint64_t *seq_off;       /* record r has seq_off[r+1] - seq_off[r] bases */
+  const uint64_t *seq_off2;      /* two-file pairs: mate 2 records, else NULL */
+  uint64_t n_frags;
+  int32_t paired;                /* fragment = a pair: names lose "/1" "/2"  */
+  int32_t interleaved;           /* pairs are records 2i, 2i+1 of seq_off    */
+  int32_t quick;                 /* -q: the hit list is "taxid:Q"           */
+  int32_t print_names;           /* -n: "name (taxid N)" instead of taxid   */
+} k2g_lines;
+
+/* Formats the n_frags kraken lines into text (host, text_cap bytes);
+ * *text_len receives their length.  K2G_ERR_CAPACITY (nothing written,
+ * *text_len = the length needed) when text_cap is too small.  Host buffers
+ * in, host text out; synchronous.  Needs a database opened from files (the
+ * taxonomy's external ids and names). */
+k2g_status k2g_format_lines_host(const k2g_db *db, const k2g_lines *in, char *text,
+                                 uint64_t text_cap, uint64_t *text_len);
+
+/* ---- the text path: FASTA/FASTQ bytes in, kraken lines out, parsed,
+ * classified and formatted on the device.  Replaces, for one input, the
+ * reader threads' loop of src/classify.cc:523-645 over BatchSequenceReader
+ * (src/seqreader.h:101-163, kseq records) and the line output of
+ * src/classify.cc:908-991.
+ *
+ * The input is handed over in chunks of any size up to chunk_cap, in order.
+ * Each call classifies the whole reader blocks (LoadBlock: records until
+ * their sequence bytes reach block_bytes; LoadBatch: block_records records)
+ * that the bytes so far complete, and keeps the rest for the next call; at
+ * the end of the input (at_eof) the last block is classified too.
+ *
+ * The device reads the strict form of FASTQ (four-line records: '@' header,
+ * one sequence line, '+' line, one quality line of the sequence's length)
+ * and FASTA ('>' header, then sequence lines none of which starts with '@'
+ * or '+').  Records are those the reference's reader gives.  Where an input
+ * leaves that form (or a record is larger than the buffers), the call sets
+ * handoff: every record before `consumed` (an offset into the whole input,
+ * the start of a reader block) has been classified, and the caller's own
+ * reader continues from there -- exactly, since a reader's state between
+ * records is only where the next header starts.  Blocks are numbered on from
+ * first_block (k2g_text_reset), for the -K counters. */
+typedef struct k2g_text k2g_text;
+
+typedef struct {
+  uint64_t chunk_cap;         /* most bytes one k2g_text_classify call takes (<= 2^30) */
+  uint64_t block_bytes;       /* LoadBlock: 3 MiB for single reads (or 0)   */
+  uint64_t block_records;     /* LoadBatch: records per block (or 0); exactly
+                                 one of the two is nonzero                 */
+  int32_t interleaved;        /* pairs are records 2i, 2i+1 (-S; params->paired) */
+  int32_t print_names;        /* -n                                         */
+  int32_t lines;              /* 1: format the kraken lines                 */
+} k2g_text_config;
+
+typedef struct {
+  uint64_t fragments;         /* classified by this call (a pair counts once) */
+  uint64_t bases;             /* their sequence bytes (mates together)      */
+  uint64_t classified;        /* of them with a call                        */
+  uint64_t blocks;            /* reader blocks they make                    */
+  uint64_t text_len;          /* bytes of their kraken lines (k2g_text_fetch) */
+  uint64_t consumed;          /* input bytes before the first record not yet
+                                 classified                                */
+  int32_t handoff;            /* 1: the caller reads on from `consumed`     */
+  int32_t pad_;
+} k2g_text_result;
+
+/* params as for k2g_classify (min_quality masks FASTQ bases); DNA databases
+ * opened from files (for lines).  Device buffers are sized from chunk_cap
+ * (about 50 bytes per chunk byte, 2 more with k2g_text_prefetch). */
+k2g_status k2g_text_create(const k2g_db *db, const k2g_classify_params *params,
+                           const k2g_text_config *cfg, k2g_text **out);
+/* Starts a new input: drops held bytes; blocks and fragments are numbered
+ * from first_block / first_fragment. */
+k2g_status k2g_text_reset(k2g_text *t, uint32_t first_block, uint64_t first_fragment);
+/* Classifies what chunk[0, len) completes (see above); counters (may be
+ * NULL) receive the add_kmer events of -K.  Synchronous. */
+k2g_status k2g_text_classify(k2g_text *t, const char *chunk, uint64_t len, int at_eof,
+                             k2g_counters *counters, k2g_text_result *res);
+/* Starts copying the chunk a later k2g_text_classify call will be given
+ * (same pointer and length) to the device on a second stream, so that copy
+ * overlaps the work of the calls before it.  chunk must stay unchanged until
+ * that call; pinned memory (k2g_host_alloc) makes the copy asynchronous.  At
+ * most two chunks are held ahead. */
+k2g_status k2g_text_prefetch(k2g_text *t, const char *chunk, uint64_t len);
+/* Copies the kraken lines of the last k2g_text_classify call (text_len
+ * bytes, input order) into text. */
+k2g_status k2g_text_fetch(k2g_text *t, char *text, uint64_t cap);
+/* Adds the calls per taxon since the last call of this function into
+ * taxon_reads (node_count entries). */
+k2g_status k2g_text_taxon_reads(k2g_text *t, uint64_t *taxon_reads);
+k2g_status k2g_text_destroy(k2g_text *t);
 
 /* ---- serving: a resident database answering classification requests
  * (no counterpart in the reference, which classifies one invocation's files).

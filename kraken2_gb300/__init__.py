@@ -45,7 +45,10 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_counters_destroy", "k2g_counters_add", "k2g_counters_finish",
            "k2g_classify_host_blocks", "k2g_server_create", "k2g_server_submit",
            "k2g_server_wait", "k2g_server_fetch", "k2g_server_destroy", "k2g_server_sizes",
-           "k2g_tuning_get", "k2g_tuning_set", "k2g_autotune", "k2g_server_timing"]
+           "k2g_tuning_get", "k2g_tuning_set", "k2g_autotune", "k2g_server_timing",
+           "k2g_format_lines_host", "k2g_text_create", "k2g_text_reset", "k2g_text_classify",
+           "k2g_text_fetch", "k2g_text_taxon_reads", "k2g_text_destroy", "k2g_db_set_names",
+           "k2g_counters_export", "k2g_counters_import", "k2g_text_prefetch"]
 
 
 class Tuning(C.Structure):
@@ -64,6 +67,29 @@ def length_class(total_bases: int, n_frags: int) -> int:
     """Batch class by bases per fragment, mates together (k2g.h)."""
     avg = total_bases / n_frags if n_frags else 0.0
     return 0 if avg <= 512 else (1 if avg <= 4096 else 2)
+
+
+class Lines(C.Structure):
+    """k2g_lines: inputs of k2g_format_lines_host (host pointers)."""
+    _fields_ = [("call", C.c_void_p), ("hitlist_len", C.c_void_p), ("runs", C.c_void_p),
+                ("n_runs", C.c_uint64), ("text", C.c_void_p), ("text_len", C.c_uint64),
+                ("name_refs", C.c_void_p), ("ref_stride", C.c_uint64), ("seq_off", C.c_void_p),
+                ("seq_off2", C.c_void_p), ("n_frags", C.c_uint64), ("paired", C.c_int32),
+                ("interleaved", C.c_int32), ("quick", C.c_int32), ("print_names", C.c_int32)]
+
+
+class TextConfig(C.Structure):
+    """k2g_text_config: how the text path cuts an input into reader blocks."""
+    _fields_ = [("chunk_cap", C.c_uint64), ("block_bytes", C.c_uint64),
+                ("block_records", C.c_uint64), ("interleaved", C.c_int32),
+                ("print_names", C.c_int32), ("lines", C.c_int32)]
+
+
+class TextResult(C.Structure):
+    """k2g_text_result: what one k2g_text_classify call did."""
+    _fields_ = [("fragments", C.c_uint64), ("bases", C.c_uint64), ("classified", C.c_uint64),
+                ("blocks", C.c_uint64), ("text_len", C.c_uint64), ("consumed", C.c_uint64),
+                ("handoff", C.c_int32), ("pad_", C.c_int32)]
 
 
 class K2GError(RuntimeError):
@@ -157,6 +183,18 @@ def lib():
             "k2g_server_fetch": [vp, u64, vp, vp, vp, vp, C.POINTER(u64), C.POINTER(C.c_double)],
             "k2g_server_destroy": [vp],
             "k2g_server_sizes": [vp, u64, C.POINTER(u64), C.POINTER(u64)],
+            "k2g_format_lines_host": [vp, C.POINTER(Lines), vp, u64, C.POINTER(u64)],
+            "k2g_text_create": [vp, C.POINTER(ClassifyParams), C.POINTER(TextConfig),
+                                C.POINTER(vp)],
+            "k2g_text_reset": [vp, C.c_uint32, u64],
+            "k2g_db_set_names": [vp, vp, vp, u64, vp],
+            "k2g_counters_export": [vp, vp, u64, C.POINTER(u64), vp, vp, vp],
+            "k2g_counters_import": [vp, vp, u64, vp, vp, vp],
+            "k2g_text_classify": [vp, vp, u64, i32, vp, C.POINTER(TextResult)],
+            "k2g_text_fetch": [vp, vp, u64],
+            "k2g_text_prefetch": [vp, vp, u64],
+            "k2g_text_taxon_reads": [vp, vp],
+            "k2g_text_destroy": [vp],
             "k2g_server_timing": [vp, u64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                   C.POINTER(C.c_double)],
             "k2g_tuning_get": [vp, i32, i32, C.POINTER(Tuning)],
@@ -211,6 +249,18 @@ class Database:
         check(lib().k2g_db_create(C.byref(opts), capacity, key_bits, value_bits,
                                   parent.ctypes.data, len(parent), device, C.byref(h)))
         return cls(h)
+
+    def set_names(self, external_id: np.ndarray, names: list):
+        """k2g_db_set_names: the external ids and scientific names (one bytes
+        object per node) that kraken lines print."""
+        ext = np.ascontiguousarray(external_id, dtype=np.uint64)
+        blob = b"".join(n + b"\0" for n in names)
+        off = np.zeros(len(names), np.uint64)
+        if len(names) > 1:
+            off[1:] = np.cumsum([len(n) + 1 for n in names[:-1]])
+        buf = np.frombuffer(blob, np.uint8)
+        check(lib().k2g_db_set_names(self.h, ext.ctypes.data, buf.ctypes.data, len(blob),
+                                     off.ctypes.data))
 
     def close(self):
         if self.h:
@@ -296,6 +346,39 @@ class Database:
                                  int(trials), C.byref(t), C.byref(ms), stream))
         return t, float(ms.value)
 
+    def format_lines(self, call: np.ndarray, hitlist_len: np.ndarray, runs: np.ndarray,
+                     names: list, seq_lens: np.ndarray, paired: bool = False,
+                     quick: bool = False, print_names: bool = False) -> bytes:
+        """k2g_format_lines_host: the kraken lines of a classified batch,
+        formatted on the device.  names: one bytes object per record;
+        seq_lens: length of every record (pairs: mate 1, mate 2 in turn,
+        records 2i and 2i + 1 of fragment i)."""
+        text = b"".join(names)
+        refs = np.zeros(len(names), np.dtype([("pos", "<u8"), ("len", "<u4"), ("pad", "<u4")]))
+        refs["len"] = [len(x) for x in names]
+        refs["pos"] = np.concatenate([[0], np.cumsum(refs["len"][:-1].astype(np.uint64))]) \
+            if len(names) else []
+        off = np.concatenate([[0], np.cumsum(np.asarray(seq_lens, np.uint64))]).astype(np.uint64)
+        call = np.ascontiguousarray(call, np.uint32)
+        hl = np.ascontiguousarray(hitlist_len, np.uint32)
+        runs = np.ascontiguousarray(runs, np.uint64)
+        tb = np.frombuffer(text + b"\0", np.uint8)
+        n = len(call)
+        lines = Lines(call.ctypes.data, hl.ctypes.data, runs.ctypes.data if len(runs) else None,
+                      len(runs), tb.ctypes.data, len(text), refs.ctypes.data, refs.itemsize,
+                      off.ctypes.data, None, n, int(paired), int(paired), int(quick),
+                      int(print_names))
+        cap = max(1024, 128 * n)
+        out = np.zeros(cap, np.uint8)
+        got = C.c_uint64(0)
+        st = lib().k2g_format_lines_host(self.h, C.byref(lines), out.ctypes.data, cap, C.byref(got))
+        if st == 6:   # K2G_ERR_CAPACITY: size reported
+            out = np.zeros(got.value, np.uint8)
+            st = lib().k2g_format_lines_host(self.h, C.byref(lines), out.ctypes.data, got.value,
+                                             C.byref(got))
+        check(st)
+        return out[:got.value].tobytes()
+
     def classify_static(self, reads: Reads, params: ClassifyParams, results: Results,
                         stream: int = 0):
         """k2g_classify_static: plain classification with no device allocation."""
@@ -335,6 +418,68 @@ class Database:
         return keys[:n.value]
 
 
+class TextReader:
+    """The text path (k2g_text_*): FASTA/FASTQ bytes in, kraken lines out,
+    parsed, classified and formatted on the device."""
+
+    SE_BLOCK_BYTES = 3 * 1024 * 1024   # LoadBlock of single reads (src/classify.cc:526)
+
+    def __init__(self, db: "Database", params: ClassifyParams, chunk_cap: int = 64 << 20,
+                 block_bytes: int = SE_BLOCK_BYTES, block_records: int = 0,
+                 interleaved: bool = False, print_names: bool = False, lines: bool = True):
+        self.db = db
+        self.h = C.c_void_p()
+        cfg = TextConfig(int(chunk_cap), int(block_bytes), int(block_records), int(interleaved),
+                         int(print_names), int(lines))
+        check(lib().k2g_text_create(db.h, C.byref(params), C.byref(cfg), C.byref(self.h)))
+
+    def reset(self, first_block: int = 0, first_fragment: int = 0):
+        check(lib().k2g_text_reset(self.h, int(first_block), int(first_fragment)))
+
+    def classify(self, chunk: bytes, at_eof: bool, counters: "Counters | None" = None
+                 ) -> tuple[TextResult, bytes]:
+        """k2g_text_classify + k2g_text_fetch: (result, kraken lines)."""
+        res = TextResult()
+        buf = np.frombuffer(chunk, np.uint8) if len(chunk) else np.zeros(1, np.uint8)
+        check(lib().k2g_text_classify(self.h, buf.ctypes.data, len(chunk), int(at_eof),
+                                      counters.h if counters else None, C.byref(res)))
+        out = np.zeros(max(1, res.text_len), np.uint8)
+        check(lib().k2g_text_fetch(self.h, out.ctypes.data, res.text_len))
+        return res, out[:res.text_len].tobytes()
+
+    def prefetch(self, chunk: np.ndarray):
+        """k2g_text_prefetch: copy a later chunk (a uint8 array that stays
+        alive and unchanged until classified) ahead on a second stream."""
+        check(lib().k2g_text_prefetch(self.h, chunk.ctypes.data, len(chunk)))
+
+    def classify_array(self, chunk: np.ndarray, at_eof: bool, counters: "Counters | None" = None
+                       ) -> tuple[TextResult, bytes]:
+        """classify() for a uint8 array (the pointer k2g_text_prefetch saw)."""
+        res = TextResult()
+        check(lib().k2g_text_classify(self.h, chunk.ctypes.data if len(chunk) else None,
+                                      len(chunk), int(at_eof), counters.h if counters else None,
+                                      C.byref(res)))
+        out = np.zeros(max(1, res.text_len), np.uint8)
+        check(lib().k2g_text_fetch(self.h, out.ctypes.data, res.text_len))
+        return res, out[:res.text_len].tobytes()
+
+    def taxon_reads(self, into: np.ndarray):
+        """Adds the calls per taxon since the last such call into `into` (uint64)."""
+        assert into.dtype == np.uint64 and into.flags.c_contiguous
+        check(lib().k2g_text_taxon_reads(self.h, into.ctypes.data))
+
+    def close(self):
+        if self.h:
+            lib().k2g_text_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Counters:
     """Taxon counters of -R/-K on the device (k2g_counters)."""
 
@@ -345,6 +490,27 @@ class Counters:
 
     def add(self, reads: Reads, results: Results, stream: int = 0):
         check(lib().k2g_counters_add(self.h, C.byref(reads), C.byref(results), stream))
+
+    def export(self, stream: int = 0) -> dict:
+        """k2g_counters_export: {"entries": uint64 sorted, "taxon_kmers": uint64
+        per node, "dense": uint8 per node} -- what another process imports."""
+        n = self.db.info().node_count
+        cnt = C.c_uint64(0)
+        check(lib().k2g_counters_export(self.h, None, 0, C.byref(cnt), None, None, stream))
+        ent = np.zeros(max(cnt.value, 1), np.uint64)
+        tk = np.zeros(n, np.uint64)
+        dn = np.zeros(n, np.uint8)
+        check(lib().k2g_counters_export(self.h, ent.ctypes.data, len(ent), C.byref(cnt),
+                                        tk.ctypes.data, dn.ctypes.data, stream))
+        return {"entries": ent[:cnt.value], "taxon_kmers": tk, "dense": dn}
+
+    def import_state(self, state: dict, stream: int = 0):
+        """k2g_counters_import of an exported (or merged) state."""
+        ent = np.ascontiguousarray(state["entries"], np.uint64)
+        tk = np.ascontiguousarray(state["taxon_kmers"], np.uint64)
+        dn = np.ascontiguousarray(state["dense"], np.uint8)
+        check(lib().k2g_counters_import(self.h, ent.ctypes.data if len(ent) else None, len(ent),
+                                        tk.ctypes.data, dn.ctypes.data, stream))
 
     def finish(self, stream: int = 0):
         """-> (taxon_kmers, clade_kmers, clade_distinct), uint64 per node."""

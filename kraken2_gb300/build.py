@@ -27,7 +27,7 @@ HOST_FLAGS = "-fPIC,-O3,-ffp-contract=off,-Wall"
 CU_SOURCES = ["kernels.cu", "host_classify.cu", "classify_w5.cu", "classify_misc.cu",
               "classify_static.cu", "counters.cu", "build_ordered.cu",
               "server.cu", "classify_split.cu", "inspect.cu", "build_gather.cu", "translated.cu",
-              "tuning.cu"]
+              "tuning.cu", "format.cu", "text.cu"]
 CC_SOURCES = ["db.cc"]
 # the drop-in executables (host C++ over the C ABI)
 HOST_SOURCES = ["classify_main.cc", "seq_reader.cc", "block_reader.cc", "report.cc"]

@@ -140,6 +140,9 @@ struct SmemStore {
 };
 
 // Global-memory flavour for the slow path: one contiguous region per thread.
+// Its map is sized for every token of the batch's longest fragment, so it
+// keeps a list of its occupied slots (mlist, when the region has room for
+// it): the resolve then visits a fragment's taxa, not the whole map.
 template <int KCAP, int GCAP>
 struct GlobalStore {
   static constexpr int kKeys = KCAP, kGroups = GCAP;
@@ -147,6 +150,7 @@ struct GlobalStore {
   uint16_t *groups;
   uint32_t *mkey;
   uint32_t *mcnt;
+  uint32_t *mlist;    // occupied slots in insertion order, or null
   int mcap;
   __device__ __forceinline__ uint64_t &key(int j) { return keys[j]; }
   __device__ __forceinline__ uint32_t &val(int j) { return reinterpret_cast<uint32_t *>(keys)[j * 2]; }
@@ -480,6 +484,16 @@ __device__ __forceinline__ void probe_segment(Store &st, const ClassifyArgs &a, 
 
 // Per-lane taxon -> count map (open addressing, key 0 = empty).  Returns
 // false when the map is too full; the fragment then takes the slow path.
+// Stores whose map may keep a list of its occupied slots.
+template <class Store>
+struct MapListed {
+  static constexpr bool value = false;
+};
+template <int KCAP, int GCAP>
+struct MapListed<GlobalStore<KCAP, GCAP>> {
+  static constexpr bool value = true;
+};
+
 template <class Store>
 __device__ __forceinline__ bool map_add(Store &st, uint32_t &distinct, uint32_t taxon,
                                         uint32_t n) {
@@ -492,11 +506,30 @@ __device__ __forceinline__ bool map_add(Store &st, uint32_t &distinct, uint32_t 
       if (4 * (distinct + 1) > 3 * (uint32_t)cap) return false;
       st.map_key(i) = taxon;
       st.map_cnt(i) = n;
+      if constexpr (MapListed<Store>::value) {
+        if (st.mlist) st.mlist[distinct] = (uint32_t)i;
+      }
       distinct++;
       return true;
     }
     i = (i + 1) & (cap - 1);
   }
+}
+
+// The slots of a map a resolve visits: all of them, or the listed ones.
+template <class Store>
+struct MapVisit {
+  int n;
+  const uint32_t *list;
+  __device__ __forceinline__ int slot(int j) const { return list ? (int)list[j] : j; }
+};
+
+template <class Store, class L>
+__device__ __forceinline__ MapVisit<Store> map_visit(Store &st, const L &s) {
+  if constexpr (MapListed<Store>::value) {
+    if (st.mlist) return MapVisit<Store>{(int)s.distinct, st.mlist};
+  }
+  return MapVisit<Store>{st.map_cap(), nullptr};
 }
 
 template <class Store>
@@ -584,14 +617,15 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
   // ResolveTree (src/classify.cc:710-762)
   const uint32_t required =
       (uint32_t)ceil(__dmul_rn(a.cls.confidence, (double)total));
-  const int cap = st.map_cap();
+  const MapVisit<Store> mv = map_visit(st, s);
   // The map's occupied slots: with no taxon the call is 0; with one taxon t
   // of count n, t's score is n and so is the score of each of its ancestors
   // (no other taxon lies below them), so the climb of ResolveTree either
   // stops at t (n >= required) or runs past the root: call = n >= required ?
   // t : 0.  Most reads hit one taxon or none, and skip the ancestor walks.
   uint32_t occupied = 0, t1 = 0, n1 = 0;
-  for (int i = 0; i < cap; i++) {
+  for (int j = 0; j < mv.n; j++) {
+    const int i = mv.slot(j);
     const uint32_t t = st.map_key(i);
     occupied += t ? 1u : 0u;
     if (t && !t1) {
@@ -604,7 +638,8 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
     call = n1 >= required ? t1 : 0u;
   } else if (occupied > 1) {
     uint32_t max_taxon = 0, max_score = 0;
-    for (int i = 0; i < cap; i++) {
+    for (int j = 0; j < mv.n; j++) {
+      const int i = mv.slot(j);
       uint32_t t = st.map_key(i);
       if (!t) continue;
       uint32_t score = 0;
@@ -620,7 +655,8 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
     call = max_taxon;
     while (call && max_score < required) {
       max_score = 0;
-      for (int i = 0; i < cap; i++) {
+      for (int j = 0; j < mv.n; j++) {
+        const int i = mv.slot(j);
         uint32_t t = st.map_key(i);
         if (t && is_ancestor(parent, call, t)) max_score += st.map_cnt(i);
       }
@@ -644,7 +680,7 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
   if (a.hitlist_len) a.hitlist_len[f] = s.n_runs;
   if (call && a.taxon_reads) atomicAdd(a.taxon_reads + call, 1ull);
   if (ClearMap && occupied)
-    for (int i = 0; i < cap; i++) st.map_key(i) = 0;
+    for (int j = 0; j < mv.n; j++) st.map_key(mv.slot(j)) = 0;
 }
 
 // The end of a piece: its runs are already in place (the last one is written

@@ -142,6 +142,9 @@ __global__ void classify_slow_kernel(ClassifyArgs a, int mcap) {
   st.mkey = reinterpret_cast<uint32_t *>(region + kSlowKCap + (kSlowGCap * 2 + 7) / 8);
   st.mcnt = st.mkey + mcap;
   st.mcap = mcap;
+  // the occupied-slot list, where the region has room for it
+  const uint64_t fixed = kSlowKCap + (kSlowGCap * 2 + 7) / 8 + (uint64_t)mcap;
+  st.mlist = a.scratch_stride >= fixed + (uint64_t)mcap / 2 ? st.mcnt + mcap : nullptr;
   for (int i = 0; i < mcap; i++) st.map_key(i) = 0;
   for (uint64_t li = tid; li < n_list; li += (uint64_t)gridDim.x * blockDim.x) {
     Lane<0> s;

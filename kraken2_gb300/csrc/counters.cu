@@ -381,6 +381,16 @@ __global__ void dense_hist_kernel(const uint32_t *regs, const uint32_t *clade_of
   if (threadIdx.x < kHist) hist[(uint64_t)clade_of_slot[blockIdx.x] * kHist + threadIdx.x] = h[threadIdx.x];
 }
 
+// Adds another process's per-taxon counts and dense flags.
+__global__ void import_kernel(uint64_t *nobs, uint8_t *dense, const uint64_t *in_nobs,
+                              const uint8_t *in_dense, uint64_t n) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    nobs[t] += in_nobs[t];
+    dense[t] |= in_dense[t];
+  }
+}
+
 }  // namespace
 }  // namespace k2g
 
@@ -734,6 +744,70 @@ extern "C" k2g_status k2g_counters_add(k2g_counters *c, const k2g_reads *reads,
     if (s != K2G_OK) return s;
   }
   K2G_CUDA_TRY(cudaStreamSynchronize(st));
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_counters_export(k2g_counters *c, uint64_t *entries, uint64_t cap,
+                                          uint64_t *n_entries, uint64_t *taxon_kmers,
+                                          uint8_t *dense, void *stream) {
+  if (!c || !n_entries) return fail(K2G_ERR_ARG, "null argument");
+  K2G_CUDA_TRY(cudaSetDevice(c->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  k2g_status s = compact_acc(c, st);
+  if (s != K2G_OK) return s;
+  *n_entries = c->acc_used;
+  if (!entries && !taxon_kmers && !dense) return K2G_OK;   // size query
+  if (entries) {
+    if (cap < c->acc_used) return fail(K2G_ERR_CAPACITY, "entries buffer smaller than n_entries");
+    if (c->acc_used)
+      K2G_CUDA_TRY(cudaMemcpyAsync(entries, c->d_acc, c->acc_used * 8, cudaMemcpyDeviceToHost, st));
+  }
+  if (taxon_kmers)
+    K2G_CUDA_TRY(cudaMemcpyAsync(taxon_kmers, c->d_nobs, c->node_count * 8, cudaMemcpyDeviceToHost, st));
+  if (dense) K2G_CUDA_TRY(cudaMemcpyAsync(dense, c->d_dense, c->node_count, cudaMemcpyDeviceToHost, st));
+  K2G_CUDA_TRY(cudaStreamSynchronize(st));
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_counters_import(k2g_counters *c, const uint64_t *entries,
+                                          uint64_t n_entries, const uint64_t *taxon_kmers,
+                                          const uint8_t *dense, void *stream) {
+  if (!c || !taxon_kmers || !dense || (n_entries && !entries)) return fail(K2G_ERR_ARG, "null argument");
+  K2G_CUDA_TRY(cudaSetDevice(c->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  // an entry is (encoding << tbits | preorder number of its taxon)
+  const uint64_t pmask = (1ull << c->tbits) - 1;
+  for (uint64_t i = 0; i < n_entries; i++)
+    if ((entries[i] & pmask) >= c->node_count || (entries[i] >> c->tbits) >> 32)
+      return fail(K2G_ERR_ARG, "entry of a taxon outside this taxonomy");
+  if (c->acc_used + n_entries >= (1ull << 32)) {
+    k2g_status s = compact_acc(c, st);
+    if (s != K2G_OK) return s;
+    if (c->acc_used + n_entries >= (1ull << 32)) return fail(K2G_ERR_BUDGET, "too many distinct minimizers");
+  }
+  const uint64_t n = c->node_count;
+  K2G_CUDA_TRY(reserve_keep(c->d_acc, c->acc_cap, c->acc_used + n_entries, c->acc_used, st));
+  uint64_t *d_nobs = nullptr;
+  uint8_t *d_dense = nullptr;
+  cudaError_t e = cudaMalloc(&d_nobs, n * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&d_dense, n);
+  if (e == cudaSuccess && n_entries)
+    e = cudaMemcpyAsync(c->d_acc + c->acc_used, entries, n_entries * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_nobs, taxon_kmers, n * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_dense, dense, n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    import_kernel<<<grid_for(c->device, n), 256, 0, st>>>(c->d_nobs, c->d_dense, d_nobs, d_dense, n);
+    note_launches();
+    e = cudaGetLastError();
+  }
+  unsigned long long fill = c->acc_used + n_entries;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_ctr, &fill, sizeof(fill), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (d_nobs) cudaFree(d_nobs);
+  if (d_dense) cudaFree(d_dense);
+  if (e != cudaSuccess) return cuda_fail(e, "k2g_counters_import");
+  c->acc_used += n_entries;   // sorted and de-duplicated with the rest at the next compaction
   return K2G_OK;
 }
 

@@ -140,6 +140,17 @@ k2g_status upload_parents(k2g_db *db, const uint64_t *parent, uint64_t n) {
   return K2G_OK;
 }
 
+k2g_status upload_names(k2g_db *db, const std::vector<uint64_t> &ext,
+                        const std::vector<uint64_t> &name_off, const std::vector<char> &names) {
+  K2G_CUDA_TRY(cudaMalloc(&db->d_ext, ext.size() * 8));
+  K2G_CUDA_TRY(cudaMemcpy(db->d_ext, ext.data(), ext.size() * 8, cudaMemcpyHostToDevice));
+  K2G_CUDA_TRY(cudaMalloc(&db->d_name_off, name_off.size() * 8));
+  K2G_CUDA_TRY(cudaMemcpy(db->d_name_off, name_off.data(), name_off.size() * 8, cudaMemcpyHostToDevice));
+  K2G_CUDA_TRY(cudaMalloc(&db->d_names, names.size()));
+  K2G_CUDA_TRY(cudaMemcpy(db->d_names, names.data(), names.size(), cudaMemcpyHostToDevice));
+  return K2G_OK;
+}
+
 k2g_status alloc_table(k2g_db *db, uint64_t capacity) {
   if (capacity == 0) return fail(K2G_ERR_FORMAT, "table capacity is zero");
   if (db->cell_bytes == 5) {
@@ -186,6 +197,9 @@ void destroy(k2g_db *db) {
   cudaSetDevice(db->device);
   if (db->d_cells) cudaFree(db->d_cells);
   if (db->d_wide) cudaFree(db->d_wide);
+  if (db->d_ext) cudaFree(db->d_ext);
+  if (db->d_name_off) cudaFree(db->d_name_off);
+  if (db->d_names) cudaFree(db->d_names);
   if (db->d_parent) cudaFree(db->d_parent);
   if (db->d_size) cudaFree(db->d_size);
   cudaSetDevice(cur);
@@ -233,8 +247,10 @@ extern "C" k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
     if (s != K2G_OK) return s;
   }
 
-  // taxo.k2d: only the parent array goes to the device.
-  std::vector<uint64_t> parent;
+  // taxo.k2d: the parent array, and for formatting output lines the
+  // external ids and scientific names.
+  std::vector<uint64_t> parent, ext, name_off;
+  std::vector<char> names;
   {
     int fd = open(taxo_k2d, O_RDONLY);
     if (fd < 0) return fail(K2G_ERR_IO, std::string("unable to open ") + taxo_k2d);
@@ -258,9 +274,26 @@ extern "C" k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
       close(fd);
       return fail(K2G_ERR_FORMAT, std::string("read exhausted taxonomy information in ") + taxo_k2d);
     }
+    // name data (NUL-terminated names, TaxonomyNode::name_offset into it)
+    if (hdr[1] > (1ull << 34)) {
+      close(fd);
+      return fail(K2G_ERR_FORMAT, "implausible taxonomy name data length");
+    }
+    names.resize(hdr[1] + 1);
+    if (!read_exact(fd, names.data(), hdr[1])) {
+      close(fd);
+      return fail(K2G_ERR_FORMAT, std::string("read exhausted taxonomy information in ") + taxo_k2d);
+    }
+    names[hdr[1]] = '\0';
     close(fd);
     parent.resize(n);
-    for (uint64_t i = 0; i < n; i++) parent[i] = nodes[i * 7];
+    ext.resize(n);
+    name_off.resize(n);
+    for (uint64_t i = 0; i < n; i++) {
+      parent[i] = nodes[i * 7];                      // TaxonomyNode::parent_id
+      name_off[i] = std::min<uint64_t>(nodes[i * 7 + 3], hdr[1]);   // name_offset
+      ext[i] = nodes[i * 7 + 5];                     // external_id
+    }
     k2g_status s = validate_parents(parent.data(), n);
     if (s != K2G_OK) return s;
   }
@@ -297,6 +330,7 @@ extern "C" k2g_status k2g_db_open(const char *hash_k2d, const char *taxo_k2d,
   cudaError_t ce = cudaSetDevice(device);
   if (ce != cudaSuccess) { close(fd); return cuda_fail(ce, "cudaSetDevice"); }
   k2g_status s = upload_parents(db.get(), parent.data(), parent.size());
+  if (s == K2G_OK) s = upload_names(db.get(), ext, name_off, names);
   if (s == K2G_OK) s = alloc_table(db.get(), hdr[0]);
   if (s != K2G_OK) { close(fd); destroy(db.release()); return s; }
   if (db->cell_bytes == 5) {
@@ -395,6 +429,25 @@ extern "C" k2g_status k2g_db_create(const k2g_index_options *opts, uint64_t capa
   db->size = 0;
   *out = db.release();
   return K2G_OK;
+}
+
+extern "C" k2g_status k2g_db_set_names(k2g_db *db, const uint64_t *external_id, const char *names,
+                                      uint64_t names_len, const uint64_t *name_off) {
+  if (!db || !external_id || !names || !name_off) return fail(K2G_ERR_ARG, "null argument");
+  if (!names_len || names[names_len - 1] != '\0')
+    return fail(K2G_ERR_ARG, "names must end with a NUL byte");
+  for (uint64_t i = 0; i < db->node_count; i++)
+    if (name_off[i] >= names_len) return fail(K2G_ERR_ARG, "name offset outside the names");
+  K2G_CUDA_TRY(cudaSetDevice(db->device));
+  if (db->d_ext) cudaFree(db->d_ext);
+  if (db->d_name_off) cudaFree(db->d_name_off);
+  if (db->d_names) cudaFree(db->d_names);
+  db->d_ext = nullptr;
+  db->d_name_off = nullptr;
+  db->d_names = nullptr;
+  return upload_names(db, std::vector<uint64_t>(external_id, external_id + db->node_count),
+                      std::vector<uint64_t>(name_off, name_off + db->node_count),
+                      std::vector<char>(names, names + names_len));
 }
 
 extern "C" k2g_status k2g_db_close(k2g_db *db) {

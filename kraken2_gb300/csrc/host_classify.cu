@@ -85,6 +85,23 @@ __global__ void rebase_kernel(uint64_t *off, uint64_t n, uint64_t base) {
   if (i < n) off[i] -= base;
 }
 
+__global__ void add_block_base_kernel(uint64_t *out, const uint64_t *sums, uint64_t n) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] += sums[i / kScanBlock];
+}
+
+k2g_status exclusive_scan_u32(const uint32_t *d_in, uint64_t n, uint64_t *d_out, uint64_t *d_sums,
+                              uint64_t *d_total, cudaStream_t st) {
+  if (!n) return K2G_OK;
+  uint64_t nb = (n + kScanBlock - 1) / kScanBlock;
+  scan_blocks_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(d_in, d_out, d_sums, n);
+  scan_sums_kernel<<<1, kScanBlock, 0, st>>>(d_sums, nb, d_total);
+  add_block_base_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_out, d_sums, n);
+  note_launches(3);
+  K2G_CUDA_TRY(cudaGetLastError());
+  return K2G_OK;
+}
+
 k2g_status compact_runs(const uint64_t *d_sparse, const uint64_t *d_seq_off, int per,
                         const uint32_t *d_len, uint64_t n, uint64_t *d_excl, uint64_t *d_sums,
                         uint64_t *d_total, uint64_t *d_dense, cudaStream_t st) {

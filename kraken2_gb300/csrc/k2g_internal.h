@@ -104,6 +104,11 @@ struct k2g_db {
   // padded to a multiple of 4; d_cells is then null
   unsigned long long *d_wide = nullptr;
   uint32_t cell_bytes = 4;        // 4, or 5 for CompactHashCell40 files
+  // taxonomy text for output lines (databases opened from files only):
+  // external id and scientific name (NUL-terminated at d_names + d_name_off[t])
+  uint64_t *d_ext = nullptr;
+  uint64_t *d_name_off = nullptr;
+  char *d_names = nullptr;
   uint32_t *d_parent = nullptr;   // node_count entries
   uint64_t *d_size = nullptr;     // device-side size counter used by builds
   k2g::DivMagic div{};

@@ -412,7 +412,8 @@ static SlowPlan slow_plan(uint64_t max_len, bool paired) {
   const uint64_t tokens = per * std::max<uint64_t>(max_len, 1) + 2;
   p.mcap = 64;
   while ((uint64_t)p.mcap < 2 * tokens + 2) p.mcap <<= 1;
-  p.stride = kSlowKCap + (kSlowGCap * 2 + 7) / 8 + (size_t)p.mcap;
+  // keys, groups, the map's keys and counts, and its occupied-slot list
+  p.stride = kSlowKCap + (kSlowGCap * 2 + 7) / 8 + (size_t)p.mcap + (size_t)p.mcap / 2;
   uint64_t n = (1ull << 30) / (p.stride * 8);
   n = std::max<uint64_t>(128, std::min<uint64_t>(n, 8192));
   p.threads = n / 128 * 128;

@@ -5,20 +5,28 @@
 //
 // Input is read in the reference's blocks (3 MiB of sequence single-end,
 // 10,000 records per file for pairs in two files, 20,000 records for
-// interleaved pairs) because the -K counters depend on them; blocks are
-// gathered into batches of about 64 M bases for the GPU.  Reading,
-// classification and output run as a three-thread pipeline over a pool of
-// batches; output is formatted on up to -p threads and written in input
-// order, so every output file is byte for byte what one thread would write.
+// interleaved pairs) because the -K counters depend on them.  A regular file
+// of single reads or interleaved pairs, without -C/-U, goes through the
+// library's text path: raw chunks of the file are parsed, cut into blocks,
+// classified and formatted on the GPU (k2g_text_*), and only the kraken lines
+// come back.  Other inputs, and the rest of a file from the first record the
+// text path does not take, are parsed on the host and gathered into batches
+// of about 64 M bases for the GPU.  Reading, classification and output run
+// as a three-thread pipeline over a pool of batches; output is written in
+// input order, so every output file is byte for byte what one thread would
+// write.
 #include <err.h>
 #include <getopt.h>
+#include <sys/stat.h>
 #include <sys/time.h>
 #include <sysexits.h>
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <charconv>
 #include <condition_variable>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -41,6 +49,7 @@ constexpr size_t kBlockBytes = 3 * 1024 * 1024;      // src/classify.cc:526
 constexpr size_t kFragmentsPerBatch = 10000;          // src/classify.cc:32
 constexpr uint64_t kGpuBatchBases = 64ull << 20;      // bases gathered per GPU call
 constexpr int kBatchesInFlight = 4;                   // reading, classifying, writing, spare
+constexpr uint64_t kTextChunk = 64ull << 20;          // raw bytes per text-path chunk
 
 struct Options {
   std::string index_filename, taxonomy_filename, options_filename;
@@ -162,6 +171,9 @@ void open_pair(const std::string &fmt, FILE *&f1, FILE *&f2) {
 }
 
 void initialize_outputs(const Options &o, Outputs &out) {
+  // the reading thread and (for text-path chunks) the writing thread open them
+  static std::mutex mu;
+  std::lock_guard<std::mutex> l(mu);
   if (out.initialized) return;
   if (!o.classified_output_filename.empty()) {
     if (o.paired_end_processing) open_pair(o.classified_output_filename, out.c1, out.c2);
@@ -214,8 +226,22 @@ class Channel {
   bool closed_ = false;
 };
 
+// One input read through the text path: the chunks in flight and where the
+// host reader takes over if the text path hands the input back.
+struct TextFile {
+  k2g_text *t = nullptr;
+  uint64_t start = 0;                 // file offset of the input's first byte
+  uint32_t first_block = 0;
+  std::mutex mu;
+  std::condition_variable cv;
+  uint64_t submitted = 0, processed = 0, blocks = 0;
+  std::atomic<bool> handoff{false};
+  uint64_t resume = 0;                // file offset the host reader continues from
+};
+
 // Fragments of one GPU call: whole reader blocks of one input, parsed into
-// arenas, and their results.
+// arenas, and their results; or (tf set) one raw chunk of a text-path input
+// and its kraken lines.
 struct Batch {
   k2host::RecordSet m1;               // single reads, first mates, or interleaved pairs
   k2host::RecordSet m2;               // second mates read from a second file
@@ -227,13 +253,28 @@ struct Batch {
   uint64_t runs_cap = 0;
   std::vector<uint64_t> run_start;    // first run of each fragment
   uint64_t silent_from = UINT64_MAX;  // fragments from here on are counted, not written
+  // text path
+  TextFile *tf = nullptr;
+  char *raw = nullptr;                // pinned, kTextChunk bytes once used
+  uint64_t raw_len = 0;
+  bool at_eof = false;
+  std::vector<char> text;             // kraken lines of the chunk
+  Stats text_stats;
 
+  ~Batch() {
+    if (raw) k2g_host_free(raw);
+  }
   uint64_t frags() const { return block.size(); }
   void clear() {
     m1.clear();
     m2.clear();
     block.clear();
     silent_from = UINT64_MAX;
+    tf = nullptr;
+    raw_len = 0;
+    at_eof = false;
+    text.clear();
+    text_stats = Stats{};
   }
 };
 
@@ -266,7 +307,7 @@ void append_record(std::string &s, const k2host::RecordSet &set, size_t i, const
 
 // Output text of a range of fragments, formatted by one worker.
 struct Piece {
-  std::string ko, c1, c2, u1, u2;
+  std::string c1, c2, u1, u2;
   Stats stats;
 };
 
@@ -301,14 +342,15 @@ class Pipeline {
 
   // Hands a batch on (an empty one goes back to the pool).
   void submit(Batch *b) {
-    if (b->frags()) full_.push(b);
+    if (b->frags() || b->tf) full_.push(b);
     else free_.push(b);
   }
 
  private:
   void gpu_loop() {
     while (Batch *b = full_.pop()) {
-      classify(*b);
+      if (b->tf) classify_text(*b);
+      else classify(*b);
       done_.push(b);
     }
     done_.close();
@@ -316,10 +358,45 @@ class Pipeline {
 
   void writer_loop() {
     while (Batch *b = done_.pop()) {
-      write(*b);
+      if (b->tf) write_text(*b);
+      else write(*b);
       b->clear();
       free_.push(b);
     }
+  }
+
+  // A text-path chunk: parsed, classified and formatted by the library; a
+  // hand-off stops the input's later chunks.
+  void classify_text(Batch &b) {
+    TextFile &tf = *b.tf;
+    if (!tf.handoff.load()) {
+      k2g_text_result r{};
+      if (k2g_text_classify(tf.t, b.raw, b.raw_len, b.at_eof ? 1 : 0, counters_, &r) != K2G_OK)
+        errx(EX_SOFTWARE, "classification failed: %s", k2g_last_error());
+      b.text.resize(r.text_len);
+      if (r.text_len && k2g_text_fetch(tf.t, b.text.data(), r.text_len) != K2G_OK)
+        errx(EX_SOFTWARE, "classification failed: %s", k2g_last_error());
+      b.text_stats.total_sequences = r.fragments;
+      b.text_stats.total_bases = r.bases;
+      b.text_stats.total_classified = r.classified;
+      std::lock_guard<std::mutex> l(tf.mu);
+      tf.blocks += r.blocks;
+      if (r.handoff) {
+        tf.resume = tf.start + r.consumed;
+        tf.handoff = true;
+      }
+    }
+    std::lock_guard<std::mutex> l(tf.mu);
+    tf.processed++;
+    tf.cv.notify_all();
+  }
+
+  void write_text(Batch &b) {
+    if (b.text_stats.total_sequences) initialize_outputs(o_, out_);
+    if (out_.kraken && !b.text.empty()) fwrite(b.text.data(), 1, b.text.size(), out_.kraken);
+    stats_.total_sequences += b.text_stats.total_sequences;
+    stats_.total_bases += b.text_stats.total_bases;
+    stats_.total_classified += b.text_stats.total_classified;
   }
 
   void classify(Batch &b) {
@@ -363,11 +440,47 @@ class Pipeline {
   size_t idx1(size_t i) const { return paired_ && !two_files_ ? 2 * i : i; }
   size_t idx2(size_t i) const { return two_files_ ? i : 2 * i + 1; }
 
+  // The kraken lines of the batch's written fragments, formatted on the
+  // GPU (k2g_format_lines_host) from the calls, hit lists and the reader's
+  // records.
+  void gpu_lines(const Batch &b, uint64_t n_written) {
+    static_assert(offsetof(k2host::RecordRef, text) == offsetof(k2g_name_ref, pos) &&
+                      offsetof(k2host::RecordRef, name_len) == offsetof(k2g_name_ref, len) &&
+                      sizeof(k2host::RecordRef) >= sizeof(k2g_name_ref),
+                  "a reader record starts with a k2g_name_ref");
+    k2g_lines in{};
+    in.call = b.call.data();
+    in.hitlist_len = b.hlen.data();
+    in.runs = b.runs.get();
+    in.n_runs = b.run_start[n_written];
+    in.text = b.m1.text.data();
+    in.text_len = b.m1.text.size();
+    in.name_refs = b.m1.recs.data();
+    in.ref_stride = sizeof(k2host::RecordRef);
+    in.seq_off = b.m1.seq_off.data();
+    in.seq_off2 = two_files_ ? b.m2.seq_off.data() : nullptr;
+    in.n_frags = n_written;
+    in.paired = paired_ ? 1 : 0;
+    in.interleaved = paired_ && !two_files_ ? 1 : 0;
+    in.quick = o_.quick_mode ? 1 : 0;
+    in.print_names = o_.print_scientific_name ? 1 : 0;
+    uint64_t len = 0;
+    k2g_status s = k2g_format_lines_host(db_, &in, text_.data(), text_.size(), &len);
+    if (s == K2G_ERR_CAPACITY) {
+      text_.resize(len + len / 4);
+      s = k2g_format_lines_host(db_, &in, text_.data(), text_.size(), &len);
+    }
+    if (s != K2G_OK) errx(EX_SOFTWARE, "formatting output failed: %s", k2g_last_error());
+    fwrite(text_.data(), 1, len, out_.kraken);
+  }
+
   void write(Batch &b) {
     const uint64_t n = b.frags();
     b.run_start.resize(n + 1);
     b.run_start[0] = 0;
     for (uint64_t i = 0; i < n; i++) b.run_start[i + 1] = b.run_start[i] + b.hlen[i];
+    if (out_.kraken) gpu_lines(b, std::min<uint64_t>(n, b.silent_from));
+    // statistics and the classified/unclassified sequence files on the host:
     // about 20,000 fragments per piece, at most -p pieces at a time
     const uint64_t workers = (uint64_t)std::max(1, o_.num_threads);
     const uint64_t pieces = std::max<uint64_t>(1, std::min<uint64_t>(workers, (n + 19999) / 20000));
@@ -378,7 +491,6 @@ class Pipeline {
     format(b, 0, n / pieces, out[0]);
     for (auto &t : th) t.join();
     for (Piece &pc : out) {
-      if (out_.kraken) fwrite(pc.ko.data(), 1, pc.ko.size(), out_.kraken);
       if (out_.c1) fwrite(pc.c1.data(), 1, pc.c1.size(), out_.c1);
       if (out_.c2) fwrite(pc.c2.data(), 1, pc.c2.size(), out_.c2);
       if (out_.u1) fwrite(pc.u1.data(), 1, pc.u1.size(), out_.u1);
@@ -391,8 +503,6 @@ class Pipeline {
 
   void format(const Batch &b, uint64_t f0, uint64_t f1, Piece &pc) const {
     const k2host::RecordSet &s1 = b.m1, &s2 = set2(b);
-    std::string &ko = pc.ko;
-    if (out_.kraken) ko.reserve((f1 - f0) * 64);
     for (uint64_t i = f0; i < f1; i++) {
       const size_t a = idx1(i), z = idx2(i);
       const uint32_t c = b.call[i];
@@ -402,61 +512,6 @@ class Pipeline {
       pc.stats.total_bases += len1 + len2;
       if (c) pc.stats.total_classified++;
       if (i >= b.silent_from) continue;
-      if (out_.kraken) {
-        // kraken line (src/classify.cc:908-945)
-        ko += c ? "C\t" : "U\t";
-        size_t name_len = s1.recs[a].name_len;
-        const char *name = s1.name(a);
-        // TrimPairInfo (src/classify.cc:764-771): drop a trailing "/1" or "/2"
-        if (paired_ && name_len > 2 && name[name_len - 2] == '/' &&
-            (name[name_len - 1] == '1' || name[name_len - 1] == '2'))
-          name_len -= 2;
-        ko.append(name, name_len);
-        ko.push_back('\t');
-        if (o_.print_scientific_name) {
-          ko += c ? tax_.name(c) : "unclassified";
-          ko += " (taxid ";
-          append_u64(ko, ext);
-          ko.push_back(')');
-        } else {
-          append_u64(ko, ext);
-        }
-        ko.push_back('\t');
-        append_u64(ko, len1);
-        if (paired_) {
-          ko.push_back('|');
-          append_u64(ko, len2);
-        }
-        ko.push_back('\t');
-        if (o_.quick_mode) {
-          append_u64(ko, ext);
-          ko += ":Q";
-        } else if (!b.hlen[i]) {
-          ko += "0:0";
-        } else {
-          // AddHitlistString (src/classify.cc:950-991)
-          const uint64_t *runs = b.runs.get() + b.run_start[i];
-          const uint32_t hl = b.hlen[i];
-          for (uint32_t j = 0; j < hl; j++) {
-            const uint32_t code = (uint32_t)(runs[j] >> 32), cnt = (uint32_t)runs[j];
-            if (j) ko.push_back(' ');
-            if (code == K2G_CODE_MATE_BORDER) {
-              ko += "|:|";
-            } else if (code == K2G_CODE_FRAME_BORDER) {
-              ko += "-:-";
-            } else if (code == K2G_CODE_AMBIGUOUS) {
-              ko += "A:";
-              append_u64(ko, cnt);
-              if (j + 1 == hl) ko.push_back(' ');
-            } else {
-              append_u64(ko, tax_.nodes[code].external_id);
-              ko.push_back(':');
-              append_u64(ko, cnt);
-            }
-          }
-        }
-        ko.push_back('\n');
-      }
       // classified / unclassified sequences (src/classify.cc:587-602)
       if (c) {
         if (out_.c1) {
@@ -472,6 +527,7 @@ class Pipeline {
     }
   }
 
+  std::vector<char> text_ = std::vector<char>(64u << 20);   // kraken lines of one batch
   const Options &o_;
   k2g_db *db_;
   const k2host::TaxonomyFile &tax_;
@@ -496,9 +552,83 @@ class Pipeline {
 // written: the output queue waits for the empty block's id
 // (src/classify.cc:647-673).  So reading ends at the -p-th empty load, and
 // the fragments read after the first are silent.
+// Reads a regular file from fd's offset through the text path: raw chunks
+// (read on the pool's threads) go down the pipeline, where the library
+// classifies the whole reader blocks each completes.  Returns true when the
+// whole input was taken; false when the text path handed it back, with fd's
+// offset set to the start of the first reader block it did not take.
+bool process_text(int fd, k2g_text *t, Pipeline &pl, uint32_t &block_id,
+                  k2host::RunCounts &rc, k2host::WorkerPool &pool) {
+  struct stat sb;
+  if (fstat(fd, &sb) != 0) return false;
+  const off_t at = lseek(fd, 0, SEEK_CUR);
+  if (at < 0) return false;
+  const uint64_t size = (uint64_t)sb.st_size;
+  TextFile tf;
+  tf.t = t;
+  tf.start = (uint64_t)at;
+  tf.first_block = block_id;
+  if (k2g_text_reset(t, block_id, 0) != K2G_OK)
+    errx(EX_SOFTWARE, "classification failed: %s", k2g_last_error());
+  uint64_t off = tf.start;
+  bool eof = false;
+  while (!eof && !tf.handoff.load()) {
+    Batch *b = pl.take();
+    if (!b->raw && k2g_host_alloc(reinterpret_cast<void **>(&b->raw), kTextChunk) != K2G_OK)
+      errx(EX_OSERR, "pinned host allocation failed: %s", k2g_last_error());
+    const uint64_t want = std::min<uint64_t>(kTextChunk, size > off ? size - off : 0);
+    // pieces of the chunk read in parallel straight into the pinned buffer
+    const uint64_t piece = std::max<uint64_t>(4u << 20, (want + pool.size() - 1) / pool.size());
+    const uint64_t pieces = want ? (want + piece - 1) / piece : 0;
+    std::atomic<bool> short_read{false};
+    pool.run(pieces, [&](size_t i) {
+      uint64_t a = i * piece;
+      const uint64_t z = std::min(want, a + piece);
+      while (a < z) {
+        const ssize_t got = pread(fd, b->raw + a, z - a, (off_t)(off + a));
+        if (got <= 0) {
+          short_read = true;
+          return;
+        }
+        a += (uint64_t)got;
+      }
+    });
+    if (short_read.load()) errx(EX_IOERR, "read of the input failed");
+    b->raw_len = want;
+    off += want;
+    eof = off >= size;
+    b->at_eof = eof;
+    b->tf = &tf;
+    {
+      std::lock_guard<std::mutex> l(tf.mu);
+      tf.submitted++;
+    }
+    pl.submit(b);
+  }
+  {
+    std::unique_lock<std::mutex> l(tf.mu);
+    tf.cv.wait(l, [&] { return tf.processed == tf.submitted; });
+  }
+  block_id = tf.first_block + (uint32_t)tf.blocks;
+  if (k2g_text_taxon_reads(t, rc.taxon_reads.data()) != K2G_OK)
+    errx(EX_SOFTWARE, "classification failed: %s", k2g_last_error());
+  if (!tf.handoff.load()) return true;
+  lseek(fd, (off_t)tf.resume, SEEK_SET);
+  return false;
+}
+
 void process_files(const char *f1, const char *f2, const Options &o, Pipeline &pl,
-                   Outputs &out, uint32_t &block_id, k2host::WorkerPool &pool) {
-  k2host::BlockReader reader1(k2host::open_input(f1), &pool);
+                   Outputs &out, uint32_t &block_id, k2host::WorkerPool &pool,
+                   k2g_text *text, k2host::RunCounts &rc) {
+  int fd1 = k2host::open_input(f1);
+  if (text && f1 && !f2 && fd1 >= 0) {
+    struct stat sb;
+    if (fstat(fd1, &sb) == 0 && S_ISREG(sb.st_mode) && process_text(fd1, text, pl, block_id, rc, pool)) {
+      close(fd1);
+      return;
+    }
+  }
+  k2host::BlockReader reader1(fd1, &pool);
   k2host::BlockReader reader2(f2 ? k2host::open_input(f2) : -1, &pool);
   const bool two_files = o.paired_end_processing && !o.single_file_pairs;
   const bool interleaved = o.paired_end_processing && o.single_file_pairs;
@@ -620,13 +750,30 @@ int main(int argc, char **argv) {
   Pipeline pl(o, db, tax, counters, rc, out);
   k2host::WorkerPool pool(o.num_threads);
   uint32_t block_id = 0;
+  // the text path, for regular files of single reads or interleaved pairs
+  // without -C/-U (K2G_TEXT_PATH=0 turns it off)
+  k2g_text *text = nullptr;
+  const char *tp = getenv("K2G_TEXT_PATH");
+  if ((!tp || strcmp(tp, "0") != 0) && !(o.paired_end_processing && !o.single_file_pairs) &&
+      o.classified_output_filename.empty() && o.unclassified_output_filename.empty()) {
+    k2g_classify_params p{o.confidence_threshold, o.minimum_hit_groups, o.quick_mode ? 1 : 0,
+                          o.paired_end_processing ? 1 : 0, o.minimum_quality_score};
+    k2g_text_config cfg{};
+    cfg.chunk_cap = kTextChunk;
+    if (o.paired_end_processing) cfg.block_records = kFragmentsPerBatch * 2;
+    else cfg.block_bytes = kBlockBytes;
+    cfg.interleaved = o.paired_end_processing ? 1 : 0;
+    cfg.print_names = o.print_scientific_name ? 1 : 0;
+    cfg.lines = o.kraken_output_filename == "-" ? 0 : 1;
+    if (k2g_text_create(db, &p, &cfg, &text) != K2G_OK) text = nullptr;   // host reading only
+  }
 
   timeval tv1, tv2;
   gettimeofday(&tv1, nullptr);
   if (o.filenames.empty()) {
     if (o.paired_end_processing && !o.single_file_pairs)
       errx(EX_USAGE, "paired end processing used with no files specified");
-    process_files(nullptr, nullptr, o, pl, out, block_id, pool);
+    process_files(nullptr, nullptr, o, pl, out, block_id, pool, text, rc);
   } else {
     for (size_t i = 0; i < o.filenames.size(); i++) {
       if (o.paired_end_processing && !o.single_file_pairs) {
@@ -635,14 +782,15 @@ int main(int argc, char **argv) {
           errx(EX_USAGE, "paired end processing used with unpaired file");
         }
         process_files(o.filenames[i].c_str(), o.filenames[i + 1].c_str(), o, pl, out, block_id,
-                      pool);
+                      pool, nullptr, rc);
         i++;
       } else {
-        process_files(o.filenames[i].c_str(), nullptr, o, pl, out, block_id, pool);
+        process_files(o.filenames[i].c_str(), nullptr, o, pl, out, block_id, pool, text, rc);
       }
     }
   }
   const Stats stats = pl.finish();
+  if (text) k2g_text_destroy(text);
   for (FILE *f : {out.kraken, out.c1, out.c2, out.u1, out.u2})
     if (f) fflush(f);
   gettimeofday(&tv2, nullptr);

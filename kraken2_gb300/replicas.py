@@ -4,8 +4,10 @@ Classification shards by reads with no exchange during the work: rank r
 classifies a contiguous range of fragments, cut on reader-block boundaries
 so each block's -K counters stay on one rank.  At the end the ranks combine
 their results on the host side of rank 0: calls and hit lists are gathered in
-rank order (= input order), per-taxon read counts are summed, and times are
-the maximum over ranks.  torch.distributed is only the transport here.
+rank order (= input order), per-taxon read counts are summed, the -K
+counters' states are united (merge_counter_states; rank 0 imports the union
+and finishes the report's columns), and times are the maximum over ranks.
+torch.distributed is only the transport here.
 """
 from __future__ import annotations
 
@@ -52,3 +54,26 @@ def gather_in_order(pg, rank: int, world: int, local: np.ndarray) -> np.ndarray 
     parts = [None] * world if rank == 0 else None
     pg.gather_object(local, parts, dst=0)
     return np.concatenate(parts) if rank == 0 else None
+
+
+def merge_counter_states(states: list) -> dict:
+    """The union of -K counter states (k2g_counters_export of each rank):
+    distinct (taxon, encoding) entries united, add_kmer counts added, dense
+    flags or-ed -- the state one k2g_counters object would hold had it seen
+    every rank's reader blocks (the reference merges its threads' block
+    sketches into one, src/hyperloglogplus.cc:573-651)."""
+    if not states:
+        raise ValueError("no states")
+    ent = np.unique(np.concatenate([np.asarray(s["entries"], np.uint64) for s in states]))
+    tk = np.sum([np.asarray(s["taxon_kmers"], np.uint64) for s in states], axis=0, dtype=np.uint64)
+    dn = np.bitwise_or.reduce([np.asarray(s["dense"], np.uint8) for s in states], axis=0)
+    return {"entries": ent, "taxon_kmers": tk, "dense": dn.astype(np.uint8)}
+
+
+def gather_counter_states(pg, rank: int, world: int, state: dict) -> dict | None:
+    """Every rank's counter state united on rank 0 (None elsewhere)."""
+    if pg is None:
+        return state
+    parts = [None] * world if rank == 0 else None
+    pg.gather_object(state, parts, dst=0)
+    return merge_counter_states(parts) if rank == 0 else None

@@ -1,6 +1,7 @@
 """C-ABI surface checks that need no GPU: the library builds and loads, it
 exports every entry point include/k2g.h declares, and malformed database
 files are rejected with a status (never an abort) before any device work."""
+import ctypes as C
 import os
 import re
 import shutil
@@ -155,3 +156,20 @@ def test_fast_mod_exact(d):
     for n in ns:
         n &= (1 << 64) - 1
         assert _fast_mod(n, d) == n % d, (n, d)
+
+
+def test_text_path_and_names_refuse_null_arguments():
+    """k2g_text_* and k2g_db_set_names check their arguments before any
+    device work: a null handle or output is K2G_ERR_ARG."""
+    L = k2g.lib()
+    res = k2g.TextResult()
+    cfg = k2g.TextConfig(1 << 20, 3 << 20, 0, 0, 0, 1)
+    p = k2g.ClassifyParams(0.0, 0, 0, 0, 0)
+    out = C.c_void_p()
+    assert L.k2g_text_create(None, C.byref(p), C.byref(cfg), C.byref(out)) == 1
+    assert L.k2g_text_classify(None, None, 0, 1, None, C.byref(res)) == 1
+    assert L.k2g_text_fetch(None, None, 0) == 1
+    assert L.k2g_text_reset(None, 0, 0) == 1
+    assert L.k2g_text_taxon_reads(None, None) == 1
+    assert L.k2g_text_destroy(None) == 0
+    assert L.k2g_db_set_names(None, None, None, 0, None) == 1

@@ -62,8 +62,13 @@ def _gunzip(path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("text_path", ["1", "0"], ids=["text_path", "host_reader"])
 @pytest.mark.parametrize("tag,run_", RUNS, ids=[t for t, _ in RUNS])
-def test_golden_run_outputs_identical(tag, run_, tmp_path):
+def test_golden_run_outputs_identical(tag, run_, text_path, tmp_path):
+    """Every golden run, byte for byte: through the GPU text path where the
+    run allows it (regular files of single reads or interleaved pairs, no
+    -C/-U; damaged inputs are handed back to the host reader part way), and
+    with the host reader alone (K2G_TEXT_PATH=0)."""
     db = os.path.join(GOLDEN, run_["db"])
     inputs = readsets.write_set(run_["reads"], str(tmp_path / "in"))
     args = list(run_["args"])
@@ -77,7 +82,7 @@ def test_golden_run_outputs_identical(tag, run_, tmp_path):
             cu[flag] = args[i + 1]
             args[i + 1] = str(tmp_path / (tag + args[i + 1]))
     r = run(["-H", f"{db}/hash.k2d", "-t", f"{db}/taxo.k2d", "-o", f"{db}/opts.k2d", "-p", "4"]
-            + args + inputs)
+            + args + inputs, env=dict(os.environ, K2G_TEXT_PATH=text_path))
     assert r.returncode == 0, r.stderr.decode()
     want = _gunzip(os.path.join(GOLDEN, "runs", tag + ".out.gz"))
     assert r.stdout == want

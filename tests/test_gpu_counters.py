@@ -117,6 +117,62 @@ def test_counters_over_several_calls():
     db.close()
 
 
+@pytest.mark.parametrize("tag", ["blk_se", "se150_default", "long_default"])
+def test_counters_of_ranks_merge_into_one_report(tag):
+    """Reader blocks shared out over three counters objects (the ranks of
+    the replica layout), their exported states united by
+    replicas.merge_counter_states and imported into a fresh object: the
+    report columns equal one object's over every block, and the golden
+    report."""
+    from kraken2_gb300 import replicas
+    run = manifest()["runs"][tag]
+    params, _ = parse_args(run["args"])
+    db = k2g.Database.open(os.path.join(GOLDEN, run["db"]))
+    b = batch_of(run["reads"], params["min_quality"])
+    st = torch().cuda.current_stream().cuda_stream
+    cuts = [0] + [i for i in range(1, b.n_frags) if b.blocks[i] != b.blocks[i - 1]] + [b.n_frags]
+    ranks = 3
+    objs = [k2g.Counters(db) for _ in range(ranks)]
+    tr = np.zeros(db.info().node_count, np.uint64)
+    # with one block, split at a fragment instead (both halves are then blocks of their own
+    # for the ranks, so compare with the single object fed the same calls)
+    if len(cuts) == 2:
+        cuts = [0, b.n_frags // 3, 2 * b.n_frags // 3, b.n_frags]
+    single = k2g.Counters(db)
+    for j, (f0, f1) in enumerate(zip(cuts[:-1], cuts[1:])):
+        for c in (objs[j % ranks], single):
+            reads, res, tr_i, keep = classify_with_events(db, b, params, k2g.MODE_PIPELINED, f0, f1)
+            c.add(reads, res, st)
+        tr += tr_i
+    states = [c.export(st) for c in objs]
+    merged = replicas.merge_counter_states(states)
+    fresh = k2g.Counters(db)
+    fresh.import_state(merged, st)
+    tk_m, ck_m, cd_m = fresh.finish()
+    tk_s, ck_s, cd_s = single.finish()
+    assert np.array_equal(tk_m, tk_s) and np.array_equal(ck_m, ck_s) and np.array_equal(cd_m, cd_s)
+    if len(cuts) - 1 == len(set(b.blocks.tolist())):   # the calls were the reader blocks
+        check_report(tag, run["db"], tr, ck_m, cd_m)
+    # importing into an object that holds blocks of its own adds to them
+    objs[0].import_state(replicas.merge_counter_states(states[1:]), st)
+    assert [np.array_equal(x, y) for x, y in zip(objs[0].finish(), (tk_s, ck_s, cd_s))] == [True] * 3
+    for c in objs + [single, fresh]:
+        c.close()
+    db.close()
+
+
+def test_counters_import_refuses_foreign_entries():
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    n = db.info().node_count
+    c = k2g.Counters(db)
+    bad = {"entries": np.array([0xFFFFFFFFFFFFFFFF], np.uint64),   # no (encoding, taxon) pair
+           "taxon_kmers": np.zeros(n, np.uint64), "dense": np.zeros(n, np.uint8)}
+    with pytest.raises(k2g.K2GError):
+        c.import_state(bad)
+    c.close()
+    db.close()
+
+
 # ---- crafted events: the sparse/dense switch and the event markers -------
 
 def hll_encode_np(keys):

@@ -123,7 +123,7 @@ def test_server_timing_parts_add_up_to_the_latency():
     b = batch_of("se150")
     params = k2g.ClassifyParams(0.1, 2, 0, 0, 0)
     ref = reference(db, b, params)
-    sv = k2g.Server(db, params, 2_000_000)   # a slot holds a few thousand reads
+    sv = k2g.Server(db, params, 2 * 20 * 70_000)   # a slot holds ~500 reads of 150 bp
     try:
         n = b.n_frags
         tickets = [(submit_range(sv, b, a, min(n, a + 700), 1), a, min(n, a + 700))

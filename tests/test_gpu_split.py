@@ -223,3 +223,53 @@ def test_pieces_under_other_scanner_options(k, l, mask, revcom, min_hash):
         assert split.runs_of(i) == want, i
     assert (calls > 0).mean() > 0.5
     db.close()
+
+
+def stitched_long_reads(seed: int, n: int = 40) -> Batch:
+    """Reads of 2-20 kb stitched from 36-base stretches of many db_a
+    genomes: each piece of such a read hits more taxa than a lane's taxon
+    map holds, so whole fragments go to the slow path, whose map is sized
+    for the batch's longest read (2^16 slots here) -- the resolve must visit
+    only a fragment's own taxa."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import reads as golden_reads
+    g = golden_reads.genomes_of("db_a")
+    rng = np.random.default_rng(seed)
+    reads = []
+    for r in range(n):
+        target = int(rng.integers(150, 2000)) if r % 5 == 0 else int(rng.integers(2000, 20_000))
+        buf = bytearray()
+        while len(buf) < target:
+            s = np.asarray(g[int(rng.integers(0, len(g)))][1], dtype=np.uint8)
+            p = int(rng.integers(0, len(s) - 36))
+            buf += s[p:p + 36].tobytes()
+        reads.append(bytes(buf[:target]))
+    bases = b"".join(reads)
+    off = np.concatenate([[0], np.cumsum([len(x) for x in reads])]).astype(np.uint64)
+    return Batch(bases, None, off, n, False, [f"s{i}" for i in range(n)],
+                 [(len(x),) for x in reads], np.zeros(n, np.uint32))
+
+
+@pytest.mark.parametrize("mode", [k2g.MODE_PIPELINED, k2g.MODE_PERSISTENT, k2g.MODE_PLAIN],
+                         ids=["pipelined", "persistent", "plain"])
+def test_long_reads_over_many_taxa_match_the_oracle(mode):
+    params = dict(confidence=0.05, min_hit_groups=2)
+    db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
+    b = stitched_long_reads(7)
+    got = classify_batch(db, b, params, mode=mode)
+    assert got.status == 0
+    g = golden_db("db_a")
+    o = oracle.Oracle(g.hash.cells, g.hash.capacity, g.hash.key_bits, g.hash.value_bits,
+                      g.taxo.parent, oracle.index_opts(g.opts.k, g.opts.l, g.opts.spaced_seed_mask,
+                                                       g.opts.toggle_mask))
+    calls, hg, nr, runs, base = o.classify(b.bases, None, b.seq_off, b.n_frags, threads=4, **params)
+    assert np.array_equal(got.call[:b.n_frags], calls.astype(np.uint32))
+    assert np.array_equal(got.hit_groups[:b.n_frags], hg.astype(np.uint32))
+    for i in range(b.n_frags):
+        want = [(int(r["code"]), int(r["count"])) for r in runs[int(base[i]):int(base[i]) + int(nr[i])]]
+        assert got.runs_of(i) == want, i
+    counts = np.bincount(calls.astype(np.int64), minlength=len(g.taxo.parent)).astype(np.uint64)
+    counts[0] = 0
+    assert np.array_equal(got.taxon_reads, counts)
+    db.close()

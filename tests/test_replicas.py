@@ -87,3 +87,58 @@ def test_two_gloo_ranks_equal_one_process(tmp_path):
     counts[0] = 0
     assert np.array_equal(np.load(tmp_path / "counts.npy"), counts)
     assert float((tmp_path / "max.txt").read_text()) == float(world)
+
+
+def test_merge_counter_states_is_the_union():
+    """Entries united (sorted, distinct), add_kmer counts added, dense flags
+    or-ed; the order of the states does not matter."""
+    rng = np.random.default_rng(3)
+    n = 50
+    states = []
+    for r in range(3):
+        states.append({"entries": np.unique(rng.integers(0, 1 << 20, 400).astype(np.uint64)),
+                       "taxon_kmers": rng.integers(0, 100, n).astype(np.uint64),
+                       "dense": (rng.random(n) < 0.1).astype(np.uint8)})
+    m = replicas.merge_counter_states(states)
+    assert np.array_equal(m["entries"], np.unique(np.concatenate([s["entries"] for s in states])))
+    assert np.array_equal(m["taxon_kmers"], sum(s["taxon_kmers"] for s in states))
+    assert np.array_equal(m["dense"], np.maximum.reduce([s["dense"] for s in states]))
+    m2 = replicas.merge_counter_states(states[::-1])
+    assert all(np.array_equal(m[k], m2[k]) for k in m)
+    one = replicas.merge_counter_states(states[:1])
+    assert np.array_equal(one["entries"], states[0]["entries"])
+
+
+def _state_rank_main(rank, world, port, out_dir):
+    import torch.distributed as dist
+    from kraken2_gb300 import replicas as rp
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    rng = np.random.default_rng(100 + rank)
+    st = {"entries": np.unique(rng.integers(0, 1 << 30, 5000).astype(np.uint64)),
+          "taxon_kmers": rng.integers(0, 1000, 64).astype(np.uint64),
+          "dense": (rng.random(64) < 0.2).astype(np.uint8)}
+    merged = rp.gather_counter_states(dist, rank, world, st)
+    if rank == 0:
+        np.savez(os.path.join(out_dir, "merged.npz"), **merged)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_counter_states_gathered_over_gloo_ranks(tmp_path):
+    """Two gloo ranks send their -K counter states to rank 0, which holds
+    the union one process would have made of both."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    world = 2
+    mp.spawn(_state_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    got = np.load(tmp_path / "merged.npz")
+    states = []
+    for rank in range(world):
+        rng = np.random.default_rng(100 + rank)
+        states.append({"entries": np.unique(rng.integers(0, 1 << 30, 5000).astype(np.uint64)),
+                       "taxon_kmers": rng.integers(0, 1000, 64).astype(np.uint64),
+                       "dense": (rng.random(64) < 0.2).astype(np.uint8)})
+    want = replicas.merge_counter_states(states)
+    for k in want:
+        assert np.array_equal(got[k], want[k]), k
