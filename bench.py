@@ -1579,6 +1579,20 @@ def run_ours(args, log):
     mode = {"plain": wl.k2g.MODE_PLAIN, "persistent": wl.k2g.MODE_PERSISTENT,
             "pipelined": wl.k2g.MODE_PIPELINED}[args.mode]
     runner = DeviceRunner(wl, mode)
+    if args.text_only:
+        # for ncu: setup, then the text path's end-to-end run (FASTQ in, lines out)
+        te = text_e2e_run(wl, cfg.e2e_reads, 1)
+        log(f"text path: {te['fragments'] / te['s_per_step'] * 60 / 1e6:.1f} Mreads/min")
+        return None
+    if args.roles:
+        # for ncu: calls of 400,000 reads are one sub-batch each, so the beats
+        # of a call run the scan, probe and resolve roles one at a time
+        rr = DeviceRunner(wl, wl.k2g.MODE_PIPELINED, batch=400_000)
+        for i in range(3):
+            rr.classify(i * 400_000, 400_000)
+        torch.cuda.synchronize()
+        log("role calls done")
+        return None
     if args.profile:
         # for ncu: setup, then exactly two classification steps
         runner.step()
@@ -1902,6 +1916,11 @@ def main():
                     help="skip the -K (minimizer data) measurement")
     ap.add_argument("--profile", action="store_true",
                     help="setup plus two classification steps only (for ncu captures)")
+    ap.add_argument("--text-only", action="store_true",
+                    help="setup plus the text path end to end (for ncu captures)")
+    ap.add_argument("--roles", action="store_true",
+                    help="setup plus three calls of 400,000 reads, each beat one role alone "
+                         "(for ncu captures)")
     ap.add_argument("--long-reads", action="store_true",
                     help="setup plus the long-read mix in HBM only (for ncu captures)")
     ap.add_argument("--kmer-only", action="store_true",

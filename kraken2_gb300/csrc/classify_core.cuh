@@ -63,16 +63,16 @@ struct Window {
 // token stream starts afresh -- the k-mers ending at lo - 1 and lo are both
 // unambiguous and have different minimizers, so the token at lo is a new
 // lookup (or a min-hash skip) and no REPEAT carries a taxon over the cut.
-// The pieces' counts, hit groups and runs then simply add up.
-constexpr int kPieceMap = 16;
+// The pieces' counts, hit groups and runs then simply add up.  A piece
+// keeps no taxon map: the merge counts each taxon from the runs (a taxon's
+// k-mer count is the sum of its runs' counts), so a piece never overflows.
 struct SplitPiece {
   uint64_t frag;          // fragment index in the view
   uint64_t last_min;      // minimizer of the k-mer ending at lo - 1
   uint32_t lo, hi;        // hi == 0: unused slot
   uint32_t index;         // piece number within its fragment
   // results
-  uint32_t hit_groups, tokens, n_runs, n_map, status;   // status 1: map overflow
-  uint32_t map_taxon[kPieceMap], map_count[kPieceMap];
+  uint32_t hit_groups, tokens, n_runs;
 };
 
 // Everything a classify kernel needs, passed by value.
@@ -599,7 +599,8 @@ __device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const Clas
     } else {
       taxon = s.cur_taxon;
     }
-    if (taxon && !map_add(st, s.distinct, taxon, len)) return false;
+    // (a piece's taxa are counted from its runs by the merge)
+    if (taxon && s.piece == ~0ull && !map_add(st, s.distinct, taxon, len)) return false;
     emit_run(s, a, taxon, len);
     s.total_tokens += len;
   }
@@ -684,10 +685,11 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
 }
 
 // The end of a piece: its runs are already in place (the last one is written
-// here); counts, hit groups and the taxon map go to the piece record for the
-// merge (classify_split.cu), and the lane's map is cleared.
+// here); counts and hit groups go to the piece record for the merge
+// (classify_split.cu).  The lane's map was not used.
 template <class L, class Store>
 __device__ __forceinline__ void finish_piece(L &s, Store &st, const ClassifyArgs &a) {
+  (void)st;
   if (s.run_cnt) {
     uint64_t at = s.run_base + s.n_runs;
     if (at < a.runs_cap) a.runs[at] = ((uint64_t)s.run_code << 32) | s.run_cnt;
@@ -699,16 +701,6 @@ __device__ __forceinline__ void finish_piece(L &s, Store &st, const ClassifyArgs
   pc.hit_groups = s.hit_groups;
   pc.tokens = s.total_tokens;
   pc.n_runs = s.n_runs;
-  uint32_t n = 0;
-  for (int i = 0; i < st.map_cap(); i++) {
-    const uint32_t t = st.map_key(i);
-    if (!t) continue;
-    pc.map_taxon[n] = t;
-    pc.map_count[n] = st.map_cnt(i);
-    n++;
-    st.map_key(i) = 0;
-  }
-  pc.n_map = n;
 }
 
 }  // namespace k2g

@@ -11,14 +11,19 @@ namespace k2g {
 
 constexpr int kKCap = 40;     // keys per lane per segment
 constexpr int kGCap = 48;     // groups per lane per segment
-constexpr int kMCap = 16;     // taxon map slots per lane
+// Taxon map slots per lane (a power of two; a fragment with more than 3/4 of
+// this many taxa goes to the slow path).  16 keeps the kernel at its
+// register-limited 12 warps per SM.
+#ifndef K2G_FAST_MAP_SLOTS
+#define K2G_FAST_MAP_SLOTS 16
+#endif
+constexpr int kMCap = K2G_FAST_MAP_SLOTS;
 constexpr int kWarpsPerBlock = 2;
 using FastStore = SmemStore<kKCap, kGCap, kMCap>;
 
 constexpr int kSlowKCap = 256, kSlowGCap = 320;
 using SlowStore = GlobalStore<kSlowKCap, kSlowGCap>;
 
-static_assert(kMCap <= kPieceMap, "a piece record holds a lane's whole taxon map");
 
 // Gives idle lanes work; returns true when the lane holds a fragment (or a
 // piece) afterwards.  Persistent lanes take indices from a global counter
@@ -102,11 +107,9 @@ classify_kernel(ClassifyArgs a, int persistent) {
       bool ok = replay_segment(s, st, a, ng);
       s.key_ordinal += nk;
       if (!ok) {
-        // taxon map overflow: hand the fragment to the slow path (a piece
-        // marks its record; the merge hands its fragment on)
-        if (s.piece != ~0ull) {
-          a.pieces[s.piece].status = 1;
-        } else {
+        // taxon map overflow (never for a piece): hand the fragment to the
+        // slow path
+        {
           unsigned long long at = atomicAdd(a.defer_count, 1ull);
           if (at < a.defer_cap) a.defer_list[at] = s.frag;
           else atomicOr(a.status, STATUS_DEFER_OVERFLOW);

@@ -175,23 +175,18 @@ __global__ void split_merge_kernel(ClassifyArgs a, SplitBufs b) {
        sid += (uint64_t)gridDim.x * blockDim.x) {
     const SplitFrag sf = b.frags[sid];
     if (!sf.n) continue;
-    bool bad = false;
-    for (uint32_t j = 0; j < sf.n; j++) bad = bad || b.pieces[sf.first + j].status != 0;
-    if (bad) {   // a piece's taxon map overflowed: the slow path takes the fragment
-      const unsigned long long at = atomicAdd(a.defer_count, 1ull);
-      if (at < a.defer_cap) a.defer_list[at] = sf.frag;
-      else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
-      continue;
-    }
-    // at least twice the taxon entries of all pieces (ResolveTree walks the
-    // whole map, so it is no larger than that); at most 32 per piece, which
-    // fits the fragment's 64 entries per piece of the merge buffer
-    uint32_t entries = 0;
-    for (uint32_t j = 0; j < sf.n; j++) entries += b.pieces[sf.first + j].n_map;
+    // The fragment's taxa are counted from its pieces' runs into a map of
+    // its 64 entries per piece of the merge buffer (the largest power of two
+    // that fits; ResolveTree walks the whole map, so it is no larger than
+    // the runs need: at least twice the pieces' runs, at least 16).  A
+    // fragment with more taxa than 3/4 of that goes to the slow path.
+    uint32_t runs_total = 0;
+    for (uint32_t j = 0; j < sf.n; j++) runs_total += b.pieces[sf.first + j].n_runs;
     int cap = 16;
-    while ((uint32_t)cap < 2 * entries) cap *= 2;
+    while ((uint64_t)cap < 2ull * runs_total && (uint64_t)cap * 2 <= 64ull * sf.n) cap *= 2;
     MergeMap st{b.map_key + sf.first * 64, b.map_cnt + sf.first * 64, cap};
     for (int i = 0; i < cap; i++) st.mkey[i] = 0;
+    bool over = false;
     MergeLane s{};
     s.frag = sf.frag;
     s.run_base = a.seq_off[sf.frag] + 2 * (sf.frag + a.frag_off);
@@ -205,7 +200,6 @@ __global__ void split_merge_kernel(ClassifyArgs a, SplitBufs b) {
       const SplitPiece &pc = b.pieces[sf.first + j];
       s.total_tokens += pc.tokens;
       s.hit_groups += pc.hit_groups;
-      for (uint32_t e = 0; e < pc.n_map; e++) map_add(st, distinct, pc.map_taxon[e], pc.map_count[e]);
       const uint64_t r0 = s.run_base + (pc.lo - (k - 1));
       const uint32_t nr =
           r0 >= a.runs_cap ? 0u : (uint32_t)min((uint64_t)pc.n_runs, a.runs_cap - r0);
@@ -220,6 +214,8 @@ __global__ void split_merge_kernel(ClassifyArgs a, SplitBufs b) {
         for (uint32_t i = 0; i < kBatch; i++) {
           if (r + i >= nr) break;
           const uint32_t code = (uint32_t)(x[i] >> 32), cnt = (uint32_t)x[i];
+          // a taxon's k-mers (not ambiguous runs; single-end pieces have no border)
+          if (code && code != K2G_CODE_AMBIGUOUS && !over) over = !map_add(st, distinct, code, cnt);
           if (have && code == lc) {
             ln += cnt;
           } else {
@@ -238,6 +234,12 @@ __global__ void split_merge_kernel(ClassifyArgs a, SplitBufs b) {
       w++;
     }
     s.n_runs = (uint32_t)w;
+    if (over) {   // too many taxa for the merge map: the slow path redoes the fragment
+      const unsigned long long at = atomicAdd(a.defer_count, 1ull);
+      if (at < a.defer_cap) a.defer_list[at] = sf.frag;
+      else atomicOr(a.status, STATUS_DEFER_OVERFLOW);
+      continue;
+    }
     finish_fragment(s, st, a);
   }
 }

@@ -55,9 +55,9 @@ cudaError_t split_plan(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaS
 // The same for the fragments of the view's in_list (b.mark must be zeroed).
 cudaError_t split_plan_list(const ClassifyArgs &v, const SplitBufs &b, uint64_t list_cap, int sms,
                            cudaStream_t st);
-// Merges the pieces of every split fragment and writes its outputs; a
-// fragment one of whose pieces overflowed its taxon map goes to the view's
-// slow-path list instead.
+// Merges the pieces of every split fragment and writes its outputs, counting
+// its taxa from the pieces' runs; a fragment with more taxa than its merge
+// map holds goes to the view's slow-path list instead.
 cudaError_t split_merge(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st);
 
 }  // namespace k2g

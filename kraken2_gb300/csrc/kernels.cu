@@ -521,7 +521,7 @@ static k2g_status run_classify(const k2g_db *db, const ClassifyArgs &a0, int mod
   // kernel.
   // Long single-end fragments of that list are cut into pieces first (see
   // classify_split.h); the fused kernel then skips them, and the merge hands
-  // a fragment whose piece overflowed its taxon map to the slow kernel.
+  // a fragment with more taxa than its merge map holds to the slow kernel.
   // Persistent mode cuts long single-end fragments into pieces first, so
   // no lane walks a long read alone; quick mode stops inside a fragment
   // and pairs carry a mate border, so those stay whole.

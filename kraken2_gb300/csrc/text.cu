@@ -70,6 +70,7 @@ struct ParseInfo {
   unsigned long long bases;       // sequence bytes of the kept fragments
   unsigned long long valid;       // records before the first line outside the form
   unsigned long long classified;  // kept fragments with a call
+  unsigned long long all;         // the input ends with the last valid record
 };
 
 struct Window {
@@ -237,12 +238,13 @@ struct CutArgs {
   const uint32_t *rec_line;
   uint64_t *block_start;          // [block_cap + 1]
   uint64_t block_cap;
+  const uint32_t *rnext;          // LoadBlock: the record after the block starting at r
   ParseInfo *info;
 };
 
-// One thread: how many records are valid and complete, and which whole
-// reader blocks they form (LoadBlock / LoadBatch, src/seqreader.h:101-163).
-__global__ void cut_kernel(CutArgs a) {
+// One thread: how many records are valid and complete, and the sequence end
+// of the last of them.
+__global__ void valid_kernel(CutArgs a) {
   if (blockIdx.x || threadIdx.x) return;
   const Window &wd = a.wd;
   const unsigned long long fb = a.info->first_bad;
@@ -256,44 +258,61 @@ __global__ void cut_kernel(CutArgs a) {
     limit = fb == kNone ? complete : (a.hdr_rank[fb] ? a.hdr_rank[fb] - 1 : 0);
   }
   const uint64_t valid = complete < limit ? complete : limit;
-  const bool all = fb == kNone && wd.at_eof;   // the input ends with record `valid`
-  // the sequence end of the last valid record
   a.seq_off[valid] = valid < a.n_hdr ? a.line_pos[a.rec_line[valid]] : a.contrib_total;
+  a.info->valid = valid;
+  a.info->all = fb == kNone && wd.at_eof;   // the input ends with record `valid`
+}
+
+constexpr uint32_t kNoEnd = 0xFFFFFFFFu;
+
+// LoadBlock, per valid record r: the block that starts at r ends with the
+// first record that brings its sequence bytes to block_bytes; rnext[r] is
+// the record after it (kNoEnd when the valid records run out first).
+__global__ void block_end_kernel(const uint64_t *seq_off, uint64_t block_bytes,
+                                 const ParseInfo *info, uint32_t *rnext) {
+  const uint64_t valid = info->valid;
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < valid;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b0 = seq_off[r];
+    if (seq_off[valid] - b0 < block_bytes) {
+      rnext[r] = kNoEnd;
+      continue;
+    }
+    uint64_t lo = r, hi = valid - 1;   // smallest e with seq_off[e + 1] - b0 >= bytes
+    while (lo < hi) {
+      const uint64_t mid = lo + (hi - lo) / 2;
+      if (seq_off[mid + 1] - b0 >= block_bytes) hi = mid;
+      else lo = mid + 1;
+    }
+    rnext[r] = (uint32_t)(lo + 1);
+  }
+}
+
+// One thread: the whole reader blocks (LoadBlock / LoadBatch,
+// src/seqreader.h:101-163) from record 0, following rnext for LoadBlock.
+__global__ void cut_kernel(CutArgs a) {
+  if (blockIdx.x || threadIdx.x) return;
+  const Window &wd = a.wd;
+  const uint64_t valid = a.info->valid;
+  const bool all = a.info->all != 0;
   uint64_t take = 0, nb = 0;
   a.block_start[0] = 0;
-  if (a.block_records) {
-    while (take < valid && nb < a.block_cap) {
-      uint64_t end = take + a.block_records;
-      if (end > valid) {
-        if (!all) break;
-        end = valid;
-      }
-      take = end;
-      a.block_start[++nb] = take;
+  while (take < valid && nb < a.block_cap) {
+    uint64_t end;
+    if (a.block_records) {
+      end = take + a.block_records;
+      if (end > valid) end = kNoEnd;
+    } else {
+      end = a.rnext[take];
     }
-  } else {
-    while (take < valid && nb < a.block_cap) {
-      // the block ends with the first record that brings its bytes to block_bytes
-      const uint64_t b0 = a.seq_off[take];
-      uint64_t end;
-      if (a.seq_off[valid] - b0 < a.block_bytes) {
-        if (!all) break;
-        end = valid;
-      } else {
-        uint64_t lo = take, hi = valid - 1;   // smallest r with seq_off[r + 1] - b0 >= bytes
-        while (lo < hi) {
-          const uint64_t mid = lo + (hi - lo) / 2;
-          if (a.seq_off[mid + 1] - b0 >= a.block_bytes) hi = mid;
-          else lo = mid + 1;
-        }
-        end = lo + 1;
-      }
-      take = end;
-      a.block_start[++nb] = take;
+    if (end == kNoEnd) {   // an unfinished block: kept only when the input ends with it
+      if (!all) break;
+      end = valid;
     }
+    take = end;
+    a.block_start[++nb] = take;
   }
   const uint64_t frags = a.interleaved ? take / 2 : take;   // an odd last record has no mate
-  a.info->valid = valid;
   a.info->n_take = take;
   a.info->n_frags = frags;
   a.info->n_blocks = nb;
@@ -405,7 +424,7 @@ struct k2g_text {
   bool handed_off = false;
   uint32_t next_block = 0;
   uint64_t next_frag = 0;
-  DBuf<uint32_t> tile_cnt, nl, contrib, hflag, rec_line, block, call, hlen, status;
+  DBuf<uint32_t> tile_cnt, nl, contrib, hflag, rec_line, block, call, hlen, status, rnext;
   DBuf<uint64_t> tile_off, sums, total, line_pos, hdr_rank, seq_off, block_start, runs;
   DBuf<k2g_name_ref> refs;
   DBuf<char> bases;
@@ -451,6 +470,7 @@ k2g_status text_alloc(k2g_text *t) {
   K2G_CUDA_TRY(t->rec_line.need(t->rec_cap + 1));
   K2G_CUDA_TRY(t->seq_off.need(t->rec_cap + 2));
   K2G_CUDA_TRY(t->block.need(t->rec_cap));
+  K2G_CUDA_TRY(t->rnext.need(t->rec_cap));
   K2G_CUDA_TRY(t->block_start.need(t->block_cap + 2));
   K2G_CUDA_TRY(t->bases.need(W + 16));
   K2G_CUDA_TRY(t->call.need(t->rec_cap));
@@ -473,7 +493,7 @@ void text_free(k2g_text *t) {
   if (t->st) cudaStreamSynchronize(t->st);
   for (auto &b : t->win) b.free();
   t->tile_cnt.free(); t->nl.free(); t->contrib.free(); t->hflag.free(); t->rec_line.free();
-  t->block.free(); t->call.free(); t->hlen.free(); t->status.free();
+  t->block.free(); t->rnext.free(); t->call.free(); t->hlen.free(); t->status.free();
   t->tile_off.free(); t->sums.free(); t->total.free(); t->line_pos.free(); t->hdr_rank.free();
   t->seq_off.free(); t->block_start.free(); t->runs.free(); t->refs.free(); t->bases.free();
   t->taxon_reads.free(); t->hit_keys.free(); t->hit_order.free(); t->hits_used.free();
@@ -643,8 +663,16 @@ extern "C" k2g_status k2g_text_classify(k2g_text *t, const char *chunk, uint64_t
   }
   CutArgs ca{wd, t->hflag.p, t->line_pos.p, t->hdr_rank.p, n_hdr, contrib_total,
              t->cfg.block_bytes, t->cfg.block_records, t->cfg.interleaved ? 1 : 0,
-             t->seq_off.p, t->rec_line.p, t->block_start.p, t->block_cap, t->info.p};
+             t->seq_off.p, t->rec_line.p, t->block_start.p, t->block_cap, t->rnext.p,
+             t->info.p};
+  valid_kernel<<<1, 1, 0, st>>>(ca);
+  if (!t->cfg.block_records) {
+    block_end_kernel<<<grid_for(t, n_hdr, 256), 256, 0, st>>>(t->seq_off.p, t->cfg.block_bytes,
+                                                               t->info.p, t->rnext.p);
+    note_launches();
+  }
   cut_kernel<<<1, 1, 0, st>>>(ca);
+  note_launches();
   frag_kernel<<<grid_for(t, n_hdr, 256), 256, 0, st>>>(t->seq_off.p, t->block_start.p,
                                                         t->next_block, t->cfg.interleaved ? 1 : 0,
                                                         t->block.p, t->info.p);
