@@ -454,6 +454,12 @@ k2g_status k2g_text_prefetch(k2g_text *t, const char *chunk, uint64_t len);
 /* Copies the kraken lines of the last k2g_text_classify call (text_len
  * bytes, input order) into text. */
 k2g_status k2g_text_fetch(k2g_text *t, char *text, uint64_t cap);
+/* The same copy started on a stream of its own, so it overlaps the next
+ * k2g_text_classify call (pinned memory from k2g_host_alloc makes it
+ * asynchronous); text is complete after k2g_text_wait.  The lines of a call
+ * stay on the device until the call after next, so fetch before then. */
+k2g_status k2g_text_fetch_async(k2g_text *t, char *text, uint64_t cap);
+k2g_status k2g_text_wait(k2g_text *t);
 /* Adds the calls per taxon since the last call of this function into
  * taxon_reads (node_count entries). */
 k2g_status k2g_text_taxon_reads(k2g_text *t, uint64_t *taxon_reads);

@@ -48,7 +48,8 @@ EXPORTS = ["k2g_last_error", "k2g_version", "k2g_db_open", "k2g_db_create", "k2g
            "k2g_tuning_get", "k2g_tuning_set", "k2g_autotune", "k2g_server_timing",
            "k2g_format_lines_host", "k2g_text_create", "k2g_text_reset", "k2g_text_classify",
            "k2g_text_fetch", "k2g_text_taxon_reads", "k2g_text_destroy", "k2g_db_set_names",
-           "k2g_counters_export", "k2g_counters_import", "k2g_text_prefetch"]
+           "k2g_counters_export", "k2g_counters_import", "k2g_text_prefetch",
+           "k2g_text_fetch_async", "k2g_text_wait"]
 
 
 class Tuning(C.Structure):
@@ -193,6 +194,8 @@ def lib():
             "k2g_text_classify": [vp, vp, u64, i32, vp, C.POINTER(TextResult)],
             "k2g_text_fetch": [vp, vp, u64],
             "k2g_text_prefetch": [vp, vp, u64],
+            "k2g_text_fetch_async": [vp, vp, u64],
+            "k2g_text_wait": [vp],
             "k2g_text_taxon_reads": [vp, vp],
             "k2g_text_destroy": [vp],
             "k2g_server_timing": [vp, u64, C.POINTER(C.c_double), C.POINTER(C.c_double),

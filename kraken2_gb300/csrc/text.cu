@@ -92,36 +92,33 @@ __device__ __forceinline__ uint32_t line_bytes(const char *w, uint64_t s, uint64
   return (uint32_t)(n - (n > 1 && w[e - 1] == '\r'));
 }
 
-// '\n' bytes among the 4 bytes of w that lie below `lim` bytes from its start.
-__device__ __forceinline__ uint32_t nl_in_word(uint32_t w, int64_t lim) {
-  if (lim <= 0) return 0;
-  uint32_t m = __vcmpeq4(w, 0x0a0a0a0au);
-  if (lim < 4) m &= (1u << (8 * lim)) - 1;
-  return (uint32_t)__popc(m) >> 3;
-}
-
-// Thread t of a tile block looks at window bytes [tile + 64 t, +64).
-__device__ __forceinline__ uint32_t count_mine(const char *win, uint64_t len, uint64_t base,
-                                               uint4 (&v)[4]) {
-  uint32_t c = 0;
+// Bit j of the result is set when window byte base + j (j < 64) is a '\n'
+// below len: thread t of a tile block looks at bytes [tile + 64 t, +64).
+__device__ __forceinline__ uint64_t nl_mask(const char *win, uint64_t len, uint64_t base) {
   if (base >= len) return 0;
   const uint4 *p = reinterpret_cast<const uint4 *>(win + base);
+  uint64_t mask = 0;
 #pragma unroll
   for (int q = 0; q < 4; q++) {
-    v[q] = p[q];
-    const int64_t rem = (int64_t)len - (int64_t)(base + 16 * q);
-    c += nl_in_word(v[q].x, rem) + nl_in_word(v[q].y, rem - 4) + nl_in_word(v[q].z, rem - 8) +
-         nl_in_word(v[q].w, rem - 12);
+    const uint4 v = p[q];
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const uint32_t m = __vcmpeq4(w[i], 0x0a0a0a0au);   // 0xff in each matching byte
+      const uint32_t bits = ((m >> 7) & 1u) | ((m >> 14) & 2u) | ((m >> 21) & 4u) | ((m >> 28) & 8u);
+      mask |= (uint64_t)bits << (16 * q + 4 * i);
+    }
   }
-  return c;
+  const uint64_t rem = len - base;
+  if (rem < 64) mask &= (1ull << rem) - 1;
+  return mask;
 }
 
 __global__ void __launch_bounds__(kTileThreads) nl_count_kernel(const char *win, uint64_t len,
                                                                 uint32_t *tile_cnt) {
   __shared__ uint32_t warp_sum[kTileThreads / 32];
-  uint4 v[4];
   const uint64_t base = blockIdx.x * (uint64_t)kTile + threadIdx.x * 64ull;
-  uint32_t c = count_mine(win, len, base, v);
+  uint32_t c = (uint32_t)__popcll(nl_mask(win, len, base));
   c = __reduce_add_sync(0xffffffffu, c);
   if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = c;
   __syncthreads();
@@ -136,9 +133,9 @@ __global__ void __launch_bounds__(kTileThreads) nl_write_kernel(const char *win,
                                                                 const uint64_t *tile_off,
                                                                 uint32_t *nl, uint64_t nl_cap) {
   __shared__ uint32_t warp_tot[kTileThreads / 32];
-  uint4 v[4];
   const uint64_t base = blockIdx.x * (uint64_t)kTile + threadIdx.x * 64ull;
-  const uint32_t c = count_mine(win, len, base, v);
+  uint64_t mask = nl_mask(win, len, base);
+  const uint32_t c = (uint32_t)__popcll(mask);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t x = c;
 #pragma unroll
@@ -150,15 +147,9 @@ __global__ void __launch_bounds__(kTileThreads) nl_write_kernel(const char *win,
   __syncthreads();
   uint32_t before = x - c;
   for (int i = 0; i < w; i++) before += warp_tot[i];
-  if (!c) return;
   uint64_t out = tile_off[blockIdx.x] + before;
-  const unsigned char *b = reinterpret_cast<const unsigned char *>(v);
-  for (int j = 0; j < 64 && base + j < len; j++) {
-    if (b[j] == '\n') {
-      if (out < nl_cap) nl[out] = (uint32_t)(base + j);
-      out++;
-    }
-  }
+  for (; mask; mask &= mask - 1, out++)
+    if (out < nl_cap) nl[out] = (uint32_t)(base + (uint64_t)(__ffsll((long long)mask) - 1));
 }
 
 // Per line: header flag, sequence bytes, and the strict-form check.
@@ -433,7 +424,10 @@ struct k2g_text {
   DBuf<uint32_t> hit_taxa;
   DBuf<uint32_t> line_len;
   DBuf<uint64_t> line_off;
-  DBuf<char> text;
+  DBuf<char> text[2];             // kraken lines of the last two calls
+  int text_cur = 0;               // the buffer of the last call
+  cudaStream_t fetch_st = nullptr;
+  cudaEvent_t text_free[2] = {nullptr, nullptr};   // the last copy out of each buffer
   DBuf<unsigned int> bad;
   DBuf<ParseInfo> info;
   ParseInfo *h_info = nullptr;    // pinned
@@ -485,6 +479,8 @@ k2g_status text_alloc(k2g_text *t) {
   K2G_CUDA_TRY(t->info.need(1));
   K2G_CUDA_TRY(t->hits_used.need(1));
   K2G_CUDA_TRY(cudaStreamCreateWithFlags(&t->copy_st, cudaStreamNonBlocking));
+  K2G_CUDA_TRY(cudaStreamCreateWithFlags(&t->fetch_st, cudaStreamNonBlocking));
+  for (auto &e : t->text_free) K2G_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &a : t->ahead) K2G_CUDA_TRY(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
   return K2G_OK;
 }
@@ -497,9 +493,14 @@ void text_free(k2g_text *t) {
   t->tile_off.free(); t->sums.free(); t->total.free(); t->line_pos.free(); t->hdr_rank.free();
   t->seq_off.free(); t->block_start.free(); t->runs.free(); t->refs.free(); t->bases.free();
   t->taxon_reads.free(); t->hit_keys.free(); t->hit_order.free(); t->hits_used.free();
-  t->hit_taxa.free(); t->line_len.free(); t->line_off.free(); t->text.free(); t->bad.free();
+  t->hit_taxa.free(); t->line_len.free(); t->line_off.free(); t->bad.free();
   t->info.free();
   if (t->copy_st) cudaStreamSynchronize(t->copy_st);
+  if (t->fetch_st) cudaStreamSynchronize(t->fetch_st);
+  for (auto &b : t->text) b.free();
+  for (auto &e : t->text_free)
+    if (e) cudaEventDestroy(e);
+  if (t->fetch_st) cudaStreamDestroy(t->fetch_st);
   for (auto &a : t->ahead) {
     a.buf.free();
     if (a.done) cudaEventDestroy(a.done);
@@ -759,8 +760,12 @@ extern "C" k2g_status k2g_text_classify(k2g_text *t, const char *chunk, uint64_t
       if (s != K2G_OK) return s;
       K2G_CUDA_TRY(cudaMemcpyAsync(&text_total, d_tot, 8, cudaMemcpyDeviceToHost, st));
       K2G_CUDA_TRY(cudaStreamSynchronize(st));
-      K2G_CUDA_TRY(t->text.need(text_total + 1));
-      lines::line_write_kernel<<<g, 256, 0, st>>>(v, t->line_off.p, t->text.p);
+      // the other buffer than the last call's, once its copy out is done
+      const int c = t->text_cur ^ 1;
+      K2G_CUDA_TRY(cudaEventSynchronize(t->text_free[c]));
+      K2G_CUDA_TRY(t->text[c].need(text_total + 1));
+      t->text_cur = c;
+      lines::line_write_kernel<<<g, 256, 0, st>>>(v, t->line_off.p, t->text[c].p);
       note_launches();
       K2G_CUDA_TRY(cudaGetLastError());
     }
@@ -815,13 +820,33 @@ extern "C" k2g_status k2g_text_prefetch(k2g_text *t, const char *chunk, uint64_t
   return K2G_OK;
 }
 
-extern "C" k2g_status k2g_text_fetch(k2g_text *t, char *text, uint64_t cap) {
+// Starts copying the last call's lines out on the fetch stream.
+static k2g_status fetch_start(k2g_text *t, char *text, uint64_t cap) {
   if (!t || (t->text_len && !text)) return fail(K2G_ERR_ARG, "null argument");
   if (cap < t->text_len) return fail(K2G_ERR_CAPACITY, "text buffer smaller than text_len");
   if (!t->text_len) return K2G_OK;
   K2G_CUDA_TRY(cudaSetDevice(t->db->device));
-  K2G_CUDA_TRY(cudaMemcpyAsync(text, t->text.p, t->text_len, cudaMemcpyDeviceToHost, t->st));
-  K2G_CUDA_TRY(cudaStreamSynchronize(t->st));
+  const int c = t->text_cur;
+  K2G_CUDA_TRY(cudaMemcpyAsync(text, t->text[c].p, t->text_len, cudaMemcpyDeviceToHost, t->fetch_st));
+  K2G_CUDA_TRY(cudaEventRecord(t->text_free[c], t->fetch_st));
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_text_fetch(k2g_text *t, char *text, uint64_t cap) {
+  k2g_status s = fetch_start(t, text, cap);
+  if (s != K2G_OK || !t->text_len) return s;
+  K2G_CUDA_TRY(cudaStreamSynchronize(t->fetch_st));
+  return K2G_OK;
+}
+
+extern "C" k2g_status k2g_text_fetch_async(k2g_text *t, char *text, uint64_t cap) {
+  return fetch_start(t, text, cap);
+}
+
+extern "C" k2g_status k2g_text_wait(k2g_text *t) {
+  if (!t) return fail(K2G_ERR_ARG, "null argument");
+  K2G_CUDA_TRY(cudaSetDevice(t->db->device));
+  K2G_CUDA_TRY(cudaStreamSynchronize(t->fetch_st));
   return K2G_OK;
 }
 

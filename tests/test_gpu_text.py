@@ -310,3 +310,41 @@ def test_drop_in_text_path_equals_host_reader(tmp_path):
         assert r.returncode == 0, r.stderr
         outs[tp] = (r.stdout, rep.read_bytes())
     assert outs["1"] == outs["0"]
+
+
+@pytest.mark.parametrize("tag", ["se150_default", "long_default", "pe100_interleaved"])
+def test_lines_fetched_asynchronously(tag):
+    """k2g_text_fetch_async copies each call's lines out while the next call
+    runs (the lines of a call stay on the device until the call after next);
+    after k2g_text_wait the concatenated text is the reference's output."""
+    import ctypes as C
+    run = manifest()["runs"][tag]
+    params, flags = parse_args(run["args"])
+    (data,) = read_files(run["reads"])
+    inter = params["paired"]
+    rec_max = 2 * max(len(x) for x in data.split(b"\n")) + 256
+    chunk = max(20_000, 4 * rec_max + 12_000)
+    cut = dict(block_records=40, block_bytes=0) if inter else dict(block_bytes=3000)
+    tr = k2g.TextReader(gpu_db(run["db"]), cparams(params), chunk_cap=chunk, interleaved=inter,
+                        print_names=flags["names"], **cut)
+    lib = k2g.lib()
+    arr = np.frombuffer(data, np.uint8)
+    out = np.zeros(len(data) * 4 + (1 << 20), np.uint8)
+    try:
+        tr.reset()
+        pos, used = 0, 0
+        while True:
+            piece = arr[pos:pos + chunk]
+            pos += len(piece)
+            res = k2g.TextResult()
+            k2g.check(lib.k2g_text_classify(tr.h, piece.ctypes.data, len(piece),
+                                            int(pos >= len(data)), None, C.byref(res)))
+            assert not res.handoff
+            k2g.check(lib.k2g_text_fetch_async(tr.h, out.ctypes.data + used, res.text_len))
+            used += res.text_len
+            if pos >= len(data):
+                break
+        k2g.check(lib.k2g_text_wait(tr.h))
+    finally:
+        tr.close()
+    assert out[:used].tobytes() == "".join(golden_output(tag)).encode()
