@@ -205,6 +205,12 @@ CASES = {
         for n, s, _ in rs),
     "fasta_crlf_single": lambda rng, rs: b"".join(b">" + n + b"\r\n" + s + b"\r\n" for n, s, _ in rs),
     "fasta_no_final_newline": lambda rng, rs: b"\n".join(b">" + n + b"\n" + s for n, s, _ in rs),
+    # records without sequence (a header followed by a header), and blank
+    # lines inside a record's sequence
+    "fasta_empty_records_blank_lines": lambda rng, rs: b"".join(
+        (b">" + n + b"\n") if i % 7 == 3 else
+        (b">" + n + b"\n" + s[:len(s) // 2] + b"\n\n" + s[len(s) // 2:] + b"\n")
+        for i, (n, s, _) in enumerate(rs)),
 }
 
 
