@@ -58,22 +58,11 @@ struct Sector {
 #ifndef K2G_TABLE_EVICT_FIRST
 #define K2G_TABLE_EVICT_FIRST 1
 #endif
-// 1: the load asks L2 to fetch the sector's whole 128-byte line (a random
-// request costs about the same whatever its size up to a line), so a walk
-// that continues into the next sector of the line may find it in L2
-#ifndef K2G_TABLE_L2_LINE
-#define K2G_TABLE_L2_LINE 0
-#endif
 
 __device__ __forceinline__ Sector load_sector(const uint32_t *cells, uint64_t base) {
   const uint32_t *p = cells + base;
   Sector s;
-#if K2G_TABLE_EVICT_FIRST && K2G_TABLE_L2_LINE
-  asm("ld.global.nc.L1::no_allocate.L2::evict_first.L2::128B.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(s.lo.x), "=r"(s.lo.y), "=r"(s.lo.z), "=r"(s.lo.w),
-                 "=r"(s.hi.x), "=r"(s.hi.y), "=r"(s.hi.z), "=r"(s.hi.w)
-               : "l"(p));
-#elif K2G_TABLE_EVICT_FIRST
+#if K2G_TABLE_EVICT_FIRST
   asm("ld.global.nc.L1::no_allocate.L2::evict_first.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(s.lo.x), "=r"(s.lo.y), "=r"(s.lo.z), "=r"(s.lo.w),
                  "=r"(s.hi.x), "=r"(s.hi.y), "=r"(s.hi.z), "=r"(s.hi.w)

@@ -403,9 +403,7 @@ namespace k2g {
 // Probe blocks per scan block (StepArgs::split, a tuning value, 1..4): each
 // takes every split-th run of kPipeBlock keys of the scan block's range.
 constexpr uint32_t kMaxProbeSplit = 4;
-#ifndef K2G_PROBE_PARK
-#define K2G_PROBE_PARK 1
-#endif
+
 
 // Probe that resolves every key's home sector in the main loop and parks
 // the keys whose walk continues (about one in five at load 0.7) in a shared
@@ -454,12 +452,6 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
         uint32_t v = 0;
         uint64_t next = 0, walked = 0;
         bool done = probe_first(t, hc[b], idx[b], sec[b], &v, &next, &walked);
-#if !K2G_PROBE_PARK
-        if (!done) {   // continue at once (the next sector may be in L2 already)
-          v = probe_continue(t, hc[b], next, walked);
-          done = true;
-        }
-#endif
         if (!done) {
           const uint32_t at = atomicAdd(s_cnt, 1u);
           if (at < kCap) {
