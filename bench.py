@@ -1488,7 +1488,7 @@ def random_sector_rate(wl, n_loads: int = 1 << 30) -> dict:
 #   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
 #       --clock-control none -k regex:pipe_step -s <beats of the first call> -c <beats of one call>
 # Traffic grows in proportion to the reads, so it scales to a full call.
-DRAM_BYTES_PER_READ = 7713.0
+DRAM_BYTES_PER_READ = 7752.0
 
 
 def value_counts_run(wl: Workload, reps: int = 5) -> dict:

@@ -607,6 +607,52 @@ __device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const Clas
   return true;
 }
 
+// ResolveTree (src/classify.cc:710-762) over a map with two or more taxa:
+// the highest-scoring taxon (score = counts of the taxon and its ancestors
+// in the map; ties meet at their LCA), then climbing until the counts of its
+// subtree reach `required`.
+// 1: kept out of line, so the hot loops of the step kernel's three roles
+// take less instruction cache (a read with two or more taxa is the rarer case)
+#ifndef K2G_COLD_RESOLVE_CALL
+#define K2G_COLD_RESOLVE_CALL 0
+#endif
+#if K2G_COLD_RESOLVE_CALL
+#define K2G_COLD_RESOLVE __device__ __noinline__
+#else
+#define K2G_COLD_RESOLVE __device__ __forceinline__
+#endif
+template <class Store>
+K2G_COLD_RESOLVE uint32_t resolve_tree_multi(Store st, MapVisit<Store> mv, const uint32_t *parent,
+                                     uint32_t required) {
+  uint32_t max_taxon = 0, max_score = 0;
+  for (int j = 0; j < mv.n; j++) {
+    const int i = mv.slot(j);
+    uint32_t t = st.map_key(i);
+    if (!t) continue;
+    uint32_t score = 0;
+    for (uint32_t x = t; x; x = __ldg(parent + x)) score += map_get(st, x);
+    if (score > max_score) {
+      max_score = score;
+      max_taxon = t;
+    } else if (score == max_score) {
+      max_taxon = lca(parent, max_taxon, t);
+    }
+  }
+  max_score = map_get(st, max_taxon);
+  uint32_t call = max_taxon;
+  while (call && max_score < required) {
+    max_score = 0;
+    for (int j = 0; j < mv.n; j++) {
+      const int i = mv.slot(j);
+      uint32_t t = st.map_key(i);
+      if (t && is_ancestor(parent, call, t)) max_score += st.map_cnt(i);
+    }
+    if (max_score >= required) break;
+    call = __ldg(parent + call);
+  }
+  return call;
+}
+
 // ---- resolve and write -------------------------------------------------
 // ClearMap: leave the lane's map empty for its next fragment (a lane that
 // resolves only one fragment skips it).
@@ -638,32 +684,7 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
   if (occupied == 1) {
     call = n1 >= required ? t1 : 0u;
   } else if (occupied > 1) {
-    uint32_t max_taxon = 0, max_score = 0;
-    for (int j = 0; j < mv.n; j++) {
-      const int i = mv.slot(j);
-      uint32_t t = st.map_key(i);
-      if (!t) continue;
-      uint32_t score = 0;
-      for (uint32_t x = t; x; x = __ldg(parent + x)) score += map_get(st, x);
-      if (score > max_score) {
-        max_score = score;
-        max_taxon = t;
-      } else if (score == max_score) {
-        max_taxon = lca(parent, max_taxon, t);
-      }
-    }
-    max_score = map_get(st, max_taxon);
-    call = max_taxon;
-    while (call && max_score < required) {
-      max_score = 0;
-      for (int j = 0; j < mv.n; j++) {
-        const int i = mv.slot(j);
-        uint32_t t = st.map_key(i);
-        if (t && is_ancestor(parent, call, t)) max_score += st.map_cnt(i);
-      }
-      if (max_score >= required) break;
-      call = __ldg(parent + call);
-    }
+    call = resolve_tree_multi(st, mv, parent, required);
   }
   if (call && (int32_t)s.hit_groups < a.cls.min_hit_groups) call = 0;
   // close the last run
