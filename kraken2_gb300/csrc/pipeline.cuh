@@ -111,7 +111,7 @@ __device__ __forceinline__ void pipe_scan_base(ScanLane<W> &s, const PipeArgs &p
   const bool is_new = nonamb && (m != s.last_min);
   s.last_min = nonamb ? m : s.last_min;
   bool skip = false;
-  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
   const bool is_key = is_new && !skip;
   const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
   const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
@@ -139,7 +139,7 @@ __device__ __forceinline__ void pipe_scan_emit(ScanLane<5> &s, const PipeArgs &p
   const bool is_new = nonamb && (m != s.last_min);
   s.last_min = nonamb ? m : s.last_min;
   bool skip = false;
-  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
   const bool is_key = is_new && !skip;
   const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
   const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
@@ -222,7 +222,7 @@ __device__ __forceinline__ void pipe_scan_emit_clean(ScanLane<5> &s, const PipeA
   const bool is_new = m != s.last_min;
   s.last_min = m;
   bool skip = false;
-  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
+  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
   const bool newg = is_new || s.gkind == G_AMBIG || s.gkind == G_NONE;
   const bool close = newg && (s.gkind != G_NONE);
   if (close) pa.gstream[s.gbase + s.ng] = make_group(s.gkind, s.glen);
@@ -411,6 +411,20 @@ constexpr uint32_t kMaxProbeSplit = 4;
 // their second-sector loads overlap instead of running as a divergent tail
 // of each warp (measured 11% faster per beat at 40 GB).  Probe blocks have
 // the step kernel's shared memory to themselves.
+// The probe of a 40-bit table: one lookup per record (probe_wide).
+__device__ __forceinline__ void pipe_probe_wide(
+    const unsigned long long *wide, uint64_t capacity, uint32_t key_shift, uint32_t value_bits,
+    uint32_t value_mask, DivMagic div, const uint64_t *rkey, const uint32_t *rslot, uint32_t *gtax,
+    uint64_t *gkey, uint32_t i0, uint32_t cnt, uint32_t stride) {
+  for (uint32_t i = i0; i < cnt; i += stride) {
+    const uint64_t key = rkey[i], hc = murmur3(key);
+    const uint32_t slot = rslot[i];
+    gtax[slot] = probe_wide(wide, capacity, key_shift, value_bits, value_mask, hc,
+                            fast_mod(hc, div));
+    if (gkey) gkey[slot] = key;
+  }
+}
+
 __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk, uint32_t part,
                                                 uint32_t split, unsigned char *smem) {
   constexpr int B = 4;
@@ -423,12 +437,10 @@ __device__ __forceinline__ void pipe_probe_body(const PipeArgs &pa, uint32_t blk
   const uint32_t cnt = pa.bcount[blk];
   const TableView &t = pa.a.table;
   if (t.wide) {   // 40-bit cells (uniform over the block: no barrier is skipped by part of it)
-    for (uint32_t i = part * kPipeBlock + threadIdx.x; i < cnt; i += stride) {
-      const uint64_t key = pa.rkey[rbase + i];
-      const uint32_t slot = pa.rslot[rbase + i];
-      pa.gtax[rbase + slot] = table_get_wide(t, murmur3(key));
-      if (pa.gkey) pa.gkey[rbase + slot] = key;
-    }
+    pipe_probe_wide(t.wide, t.capacity, t.key_shift,
+                    t.value_bits, t.value_mask, t.div, pa.rkey + rbase, pa.rslot + rbase,
+                    pa.gtax + rbase, pa.gkey ? pa.gkey + rbase : nullptr,
+                    part * kPipeBlock + threadIdx.x, cnt, stride);
     return;
   }
   if (threadIdx.x == 0) *s_cnt = 0;
@@ -502,14 +514,26 @@ struct ResolveLane {
   uint64_t run_base;
 };
 
+// Where a warp's add_kmer events go (the fields of PipeArgs they need,
+// passed by value to the out-of-line writer).
+struct HitSink {
+  const uint16_t *gstream;
+  const uint32_t *gtax;
+  const uint64_t *gkey;
+  uint64_t *hit_keys, *hit_order, hits_cap, frag_base;
+  uint32_t *hit_taxa, *status;
+  unsigned long long *hits_used;
+};
+
 // add_kmer events of the fragments this warp completed (src/classify.cc:
 // 869-873): every lookup group with a nonzero taxon, in token order, up to
 // and including the group that ended a quick-mode search -- n_ev of them,
 // which is the fragment's hit-group count.  One atomic per warp reserves the
-// warp's range; all 32 lanes take part (n_ev = 0 for idle lanes).
-__device__ __forceinline__ void pipe_emit_hits(const PipeArgs &pa, uint64_t f, uint64_t gb,
-                                               uint32_t ng, uint32_t n_ev) {
-  const ClassifyArgs &a = pa.a;
+// warp's range; all 32 lanes take part (n_ev = 0 for idle lanes).  (Kept
+// inline: out of line it measured 0.5 % slower on the 40 GB step, which
+// writes no events.)
+__device__ __forceinline__ void pipe_emit_hits(HitSink hs, uint64_t f, uint64_t gb, uint32_t ng,
+                                               uint32_t n_ev) {
   const unsigned lane = threadIdx.x & 31;
   uint32_t incl = n_ev;
 #pragma unroll
@@ -519,23 +543,23 @@ __device__ __forceinline__ void pipe_emit_hits(const PipeArgs &pa, uint64_t f, u
   }
   const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
   unsigned long long base = 0;
-  if (lane == 31 && total) base = atomicAdd(a.hits_used, (unsigned long long)total);
+  if (lane == 31 && total) base = atomicAdd(hs.hits_used, (unsigned long long)total);
   base = __shfl_sync(0xffffffffu, base, 31) + (incl - n_ev);
   if (!n_ev) return;
-  if (base + n_ev > a.hits_cap) {
-    atomicOr(a.status, STATUS_HITS_OVERFLOW);
+  if (base + n_ev > hs.hits_cap) {
+    atomicOr(hs.status, STATUS_HITS_OVERFLOW);
     return;
   }
-  const uint64_t order0 = (a.frag_base + f) << 32;
+  const uint64_t order0 = (hs.frag_base + f) << 32;
   uint32_t k = 0, ordinal = 0;
   for (uint32_t g = 0; g < ng && k < n_ev; g++) {
-    const uint32_t kind = pa.gstream[gb + g] >> kGroupLenBits;
+    const uint32_t kind = hs.gstream[gb + g] >> kGroupLenBits;
     if (kind != G_KEY) continue;
-    const uint32_t taxon = pa.gtax[gb + g];
+    const uint32_t taxon = hs.gtax[gb + g];
     if (taxon) {
-      a.hit_keys[base + k] = pa.gkey[gb + g];
-      a.hit_taxa[base + k] = taxon;
-      a.hit_order[base + k] = order0 | ordinal;
+      hs.hit_keys[base + k] = hs.gkey[gb + g];
+      hs.hit_taxa[base + k] = taxon;
+      hs.hit_order[base + k] = order0 | ordinal;
       k++;
     }
     ordinal++;
@@ -605,7 +629,10 @@ __device__ __forceinline__ void pipe_resolve_body(const PipeArgs &pa, uint32_t b
       n_ev = s.hit_groups;
     }
   }
-  if (a.hit_keys) pipe_emit_hits(pa, f, gb, ng, n_ev);
+  if (a.hit_keys)
+    pipe_emit_hits(HitSink{pa.gstream, pa.gtax, pa.gkey, a.hit_keys, a.hit_order, a.hits_cap,
+                           a.frag_base, a.hit_taxa, a.status, a.hits_used},
+                   f, gb, ng, n_ev);
 }
 
 }  // namespace k2g
