@@ -654,6 +654,15 @@ K2G_COLD_RESOLVE uint32_t resolve_tree_multi(Store st, MapVisit<Store> mv, const
   return call;
 }
 
+// Unrolling of the loops over a lane's taxon map: code size against loop
+// overhead in the step kernel's hot loops (4 measured 1 % faster than the
+// full 16 and 0.6 % faster than none on the 40 GB / 150 bp step).
+#ifndef K2G_MAP_UNROLL
+#define K2G_MAP_UNROLL 4
+#endif
+#define K2G_DO_PRAGMA(x) _Pragma(#x)
+#define K2G_UNROLL(n) K2G_DO_PRAGMA(unroll n)
+
 // ---- resolve and write -------------------------------------------------
 // ClearMap: leave the lane's map empty for its next fragment (a lane that
 // resolves only one fragment skips it).
@@ -672,6 +681,7 @@ __device__ __forceinline__ void finish_fragment(L &s, Store &st, const ClassifyA
   // stops at t (n >= required) or runs past the root: call = n >= required ?
   // t : 0.  Most reads hit one taxon or none, and skip the ancestor walks.
   uint32_t occupied = 0, t1 = 0, n1 = 0;
+  K2G_UNROLL(K2G_MAP_UNROLL)
   for (int j = 0; j < mv.n; j++) {
     const int i = mv.slot(j);
     const uint32_t t = st.map_key(i);

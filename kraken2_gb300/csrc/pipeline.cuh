@@ -579,6 +579,7 @@ __device__ __forceinline__ void pipe_resolve_body(const PipeArgs &pa, uint32_t b
   uint32_t ng = 0, n_ev = 0;
   if (f < a.n_frags) {
     ResolveMap st{s_mkey, s_mcnt, (int)threadIdx.x};
+    K2G_UNROLL(K2G_MAP_UNROLL)
     for (int i = 0; i < ResolveMap::kMapResolve; i++) st.map_key(i) = 0;
     ResolveLane s;
     s.frag = f;
