@@ -352,7 +352,7 @@ __device__ __forceinline__ void scan_base(Lane<W> &s, Store &st, const ScanConst
   const bool is_new = nonamb && (m != s.last_min);
   s.last_min = nonamb ? m : s.last_min;
   bool skip = false;
-  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
+  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
   const bool is_key = is_new && !skip;
   const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
   const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)

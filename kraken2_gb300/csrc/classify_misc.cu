@@ -16,12 +16,12 @@ template cudaError_t launch_slow<false, true>(const ClassifyArgs &, int, unsigne
 template cudaError_t launch_slow<true, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 template cudaError_t launch_slow<false, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 template cudaError_t launch_slow<true, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
-template cudaError_t launch_pipe_step<1, false, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<1, true, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<7, false, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<7, true, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<0, false, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<0, true, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<0, false, false>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<0, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<1, false, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<1, true, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<7, false, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<7, true, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<0, false, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<0, true, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<0, false, false, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<0, true, false, false>(const StepArgs &, cudaStream_t);
 }  // namespace k2g

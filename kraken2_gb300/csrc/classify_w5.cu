@@ -6,6 +6,8 @@
 namespace k2g {
 template cudaError_t launch_fast<5, false, true>(const ClassifyArgs &, int, int, cudaStream_t);
 template cudaError_t launch_fast<5, true, true>(const ClassifyArgs &, int, int, cudaStream_t);
-template cudaError_t launch_pipe_step<5, false, true>(const StepArgs &, cudaStream_t);
-template cudaError_t launch_pipe_step<5, true, true>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<5, false, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<5, false, true, true>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<5, true, true, false>(const StepArgs &, cudaStream_t);
+template cudaError_t launch_pipe_step<5, true, true, true>(const StepArgs &, cudaStream_t);
 }  // namespace k2g

@@ -17,13 +17,6 @@ __device__ __forceinline__ uint64_t murmur3(uint64_t k) {
   return k;
 }
 
-// The scanner's min-hash test (a -M database: minimizers hashing below the
-// threshold are skipped).  Out of line: the hash is needed only by such
-// databases, and its inlined copies in every token of the scan's hot loops
-// took instruction cache (1.4 % of the 40 GB / 150 bp step).
-static __device__ __noinline__ bool below_min_hash(uint64_t m, uint64_t min_hash) {
-  return murmur3(m) < min_hash;
-}
 
 // n % d through the invariant-divisor magic (see DivMagic).
 __device__ __forceinline__ uint64_t fast_mod(uint64_t n, const DivMagic &m) {

@@ -28,16 +28,18 @@ extern template cudaError_t launch_slow<false, true>(const ClassifyArgs &, int, 
 extern template cudaError_t launch_slow<true, true>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 extern template cudaError_t launch_slow<false, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
 extern template cudaError_t launch_slow<true, false>(const ClassifyArgs &, int, unsigned, unsigned, cudaStream_t);
-extern template cudaError_t launch_pipe_step<5, false, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<5, true, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<1, false, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<1, true, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<7, false, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<7, true, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<0, false, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<0, true, true>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<0, false, false>(const StepArgs &, cudaStream_t);
-extern template cudaError_t launch_pipe_step<0, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<5, false, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<5, false, true, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<5, true, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<5, true, true, true>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<1, false, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<1, true, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<7, false, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<7, true, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, false, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, true, true, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, false, false, false>(const StepArgs &, cudaStream_t);
+extern template cudaError_t launch_pipe_step<0, true, false, false>(const StepArgs &, cudaStream_t);
 }  // namespace k2g
 
 namespace k2g {
@@ -379,12 +381,15 @@ static cudaError_t dispatch_pipe_step(const StepArgs &sa, cudaStream_t st) {
   const ClassifyArgs &a = sa.scan.a;
   const bool q = a.quals != nullptr && a.cls.min_quality > 0;
   if (a.scan.revcom_version == 0)
-    return q ? launch_pipe_step<0, true, false>(sa, st) : launch_pipe_step<0, false, false>(sa, st);
+    return q ? launch_pipe_step<0, true, false, false>(sa, st) : launch_pipe_step<0, false, false, false>(sa, st);
   switch (a.scan.w) {
-    case 5: return q ? launch_pipe_step<5, true, true>(sa, st) : launch_pipe_step<5, false, true>(sa, st);
-    case 1: return q ? launch_pipe_step<1, true, true>(sa, st) : launch_pipe_step<1, false, true>(sa, st);
-    case 7: return q ? launch_pipe_step<7, true, true>(sa, st) : launch_pipe_step<7, false, true>(sa, st);
-    default: return q ? launch_pipe_step<0, true, true>(sa, st) : launch_pipe_step<0, false, true>(sa, st);
+    case 5:
+      if (a.scan.min_hash)
+        return q ? launch_pipe_step<5, true, true, true>(sa, st) : launch_pipe_step<5, false, true, true>(sa, st);
+      return q ? launch_pipe_step<5, true, true, false>(sa, st) : launch_pipe_step<5, false, true, false>(sa, st);
+    case 1: return q ? launch_pipe_step<1, true, true, false>(sa, st) : launch_pipe_step<1, false, true, false>(sa, st);
+    case 7: return q ? launch_pipe_step<7, true, true, false>(sa, st) : launch_pipe_step<7, false, true, false>(sa, st);
+    default: return q ? launch_pipe_step<0, true, true, false>(sa, st) : launch_pipe_step<0, false, true, false>(sa, st);
   }
 }
 

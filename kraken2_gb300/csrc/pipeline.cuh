@@ -111,7 +111,7 @@ __device__ __forceinline__ void pipe_scan_base(ScanLane<W> &s, const PipeArgs &p
   const bool is_new = nonamb && (m != s.last_min);
   s.last_min = nonamb ? m : s.last_min;
   bool skip = false;
-  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
+  if (c.min_hash) skip = is_new && (murmur3(m) < c.min_hash);
   const bool is_key = is_new && !skip;
   const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
   const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
@@ -131,6 +131,7 @@ __device__ __forceinline__ void pipe_scan_base(ScanLane<W> &s, const PipeArgs &p
 
 // The part of pipe_scan_base after the window minimum: token kind, groups,
 // keys.  m is the minimizer (toggle already removed).
+template <bool MH>
 __device__ __forceinline__ void pipe_scan_emit(ScanLane<5> &s, const PipeArgs &pa, const ScanConst &c,
                                                int32_t p, bool amb, uint64_t m, uint64_t *skey,
                                                uint32_t *sslot, int &nst) {
@@ -139,7 +140,7 @@ __device__ __forceinline__ void pipe_scan_emit(ScanLane<5> &s, const PipeArgs &p
   const bool is_new = nonamb && (m != s.last_min);
   s.last_min = nonamb ? m : s.last_min;
   bool skip = false;
-  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
+  if constexpr (MH) skip = is_new && (murmur3(m) < c.min_hash);
   const bool is_key = is_new && !skip;
   const uint32_t tkind = amb ? G_AMBIG : (is_new ? (skip ? G_SKIP : G_KEY) : G_CONT);
   const bool cont = (tkind == G_AMBIG) ? (s.gkind == G_AMBIG)
@@ -165,7 +166,7 @@ __device__ __forceinline__ uint64_t min64(uint64_t a, uint64_t b) { return a < b
 // a word costs 10 minimum operations instead of 16 and no window shifts.
 // win.r[0..3] hold the previous word's suffix minima (all ~0 at a mate start,
 // like an empty window).
-template <bool RC1>
+template <bool RC1, bool MH>
 __device__ __forceinline__ void pipe_scan_word5(ScanLane<5> &s, const PipeArgs &pa, const ScanConst &c,
                                                 int32_t p0, uint32_t ok, uint32_t codes,
                                                 uint64_t *skey, uint32_t *sslot, int &nst) {
@@ -190,10 +191,10 @@ __device__ __forceinline__ void pipe_scan_word5(ScanLane<5> &s, const PipeArgs &
   s.win.r[2] = min64(cand[2], cand[3]);
   s.win.r[1] = min64(cand[1], s.win.r[2]);
   s.win.r[0] = min64(cand[0], s.win.r[1]);
-  pipe_scan_emit(s, pa, c, p0, amb[0], m0 ^ c.toggle, skey, sslot, nst);
-  pipe_scan_emit(s, pa, c, p0 + 1, amb[1], m1 ^ c.toggle, skey, sslot, nst);
-  pipe_scan_emit(s, pa, c, p0 + 2, amb[2], m2 ^ c.toggle, skey, sslot, nst);
-  pipe_scan_emit(s, pa, c, p0 + 3, amb[3], m3 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit<MH>(s, pa, c, p0, amb[0], m0 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit<MH>(s, pa, c, p0 + 1, amb[1], m1 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit<MH>(s, pa, c, p0 + 2, amb[2], m2 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit<MH>(s, pa, c, p0 + 3, amb[3], m3 ^ c.toggle, skey, sslot, nst);
 }
 
 // Chunk ci of a mate realigned to its first base: bytes [16 ci, 16 ci + 16)
@@ -216,13 +217,14 @@ __device__ __forceinline__ uint4 realign_chunk(uint4 a, uint4 b, uint32_t head) 
 // The token of a k-mer that is unambiguous and emitted (pipe_scan_emit with
 // emit true and amb false): a new minimizer opens a KEY (or SKIP) group, a
 // repeat continues the open group unless that group is ambiguous.
+template <bool MH>
 __device__ __forceinline__ void pipe_scan_emit_clean(ScanLane<5> &s, const PipeArgs &pa,
                                                      const ScanConst &c, uint64_t m,
                                                      uint64_t *skey, uint32_t *sslot, int &nst) {
   const bool is_new = m != s.last_min;
   s.last_min = m;
   bool skip = false;
-  if (c.min_hash) skip = is_new && below_min_hash(m, c.min_hash);
+  if constexpr (MH) skip = is_new && (murmur3(m) < c.min_hash);
   const bool newg = is_new || s.gkind == G_AMBIG || s.gkind == G_NONE;
   const bool close = newg && (s.gkind != G_NONE);
   if (close) pa.gstream[s.gbase + s.ng] = make_group(s.gkind, s.glen);
@@ -243,7 +245,7 @@ __device__ __forceinline__ void pipe_scan_emit_clean(ScanLane<5> &s, const PipeA
 // Every candidate is then valid and no k-mer is ambiguous, so the run and
 // ambiguity bookkeeping and the emit bounds drop out; the state left behind
 // is the one pipe_scan_word5 leaves.
-template <bool RC1>
+template <bool RC1, bool MH>
 __device__ __forceinline__ void pipe_scan_word5_clean(ScanLane<5> &s, const PipeArgs &pa,
                                                       const ScanConst &c, uint32_t codes,
                                                       uint64_t *skey, uint32_t *sslot, int &nst) {
@@ -264,10 +266,10 @@ __device__ __forceinline__ void pipe_scan_word5_clean(ScanLane<5> &s, const Pipe
   s.win.r[2] = min64(cand[2], cand[3]);
   s.win.r[1] = min64(cand[1], s.win.r[2]);
   s.win.r[0] = min64(cand[0], s.win.r[1]);
-  pipe_scan_emit_clean(s, pa, c, m0 ^ c.toggle, skey, sslot, nst);
-  pipe_scan_emit_clean(s, pa, c, m1 ^ c.toggle, skey, sslot, nst);
-  pipe_scan_emit_clean(s, pa, c, m2 ^ c.toggle, skey, sslot, nst);
-  pipe_scan_emit_clean(s, pa, c, m3 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean<MH>(s, pa, c, m0 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean<MH>(s, pa, c, m1 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean<MH>(s, pa, c, m2 ^ c.toggle, skey, sslot, nst);
+  pipe_scan_emit_clean<MH>(s, pa, c, m3 ^ c.toggle, skey, sslot, nst);
 }
 
 #ifndef K2G_SCAN_WORD5
@@ -276,7 +278,9 @@ __device__ __forceinline__ void pipe_scan_word5_clean(ScanLane<5> &s, const Pipe
 
 constexpr size_t kScanSmem = (size_t)kStage * kPipeBlock * 12 + 16;
 
-template <int W, bool QUAL, bool RC1>
+// MH: the table skips minimizers hashing below a threshold (a -M database);
+// a compile-time choice, so the hash's code is in the hot loop only when used.
+template <int W, bool QUAL, bool RC1, bool MH>
 __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk, unsigned char *smem) {
   uint64_t *s_key = reinterpret_cast<uint64_t *>(smem);
   uint32_t *s_slot = reinterpret_cast<uint32_t *>(smem + (size_t)kStage * kPipeBlock * 8);
@@ -360,8 +364,8 @@ __device__ __forceinline__ void pipe_scan_body(const PipeArgs &pa, uint32_t blk,
           if constexpr (W == 5 && K2G_SCAN_WORD5) {
             const bool clean = ok == 0x01010101u && s.run + 1 >= c.l && p0 - s.last_amb > c.amb_span &&
                                p0 >= c.k - 1 && p0 + 3 < (int32_t)s.len;
-            if (clean) pipe_scan_word5_clean<RC1>(s, pa, c, codes, skey, sslot, nst);
-            else pipe_scan_word5<RC1>(s, pa, c, p0, ok, codes, skey, sslot, nst);
+            if (clean) pipe_scan_word5_clean<RC1, MH>(s, pa, c, codes, skey, sslot, nst);
+            else pipe_scan_word5<RC1, MH>(s, pa, c, p0, ok, codes, skey, sslot, nst);
           } else {
 #pragma unroll
             for (int b = 0; b < 4; b++) {
@@ -656,14 +660,14 @@ struct StepArgs {
 #define K2G_PIPE_MIN_BLOCKS 7
 #endif
 
-template <int W, bool QUAL, bool RC1>
+template <int W, bool QUAL, bool RC1, bool MH>
 __global__ void __launch_bounds__(kPipeBlock, K2G_PIPE_MIN_BLOCKS)
 pipe_step_kernel(StepArgs sa) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t roles = 2 + sa.split;
   const uint32_t role = blockIdx.x % roles, blk = blockIdx.x / roles;
   if (role == 0) {
-    if (blk < sa.n_scan) pipe_scan_body<W, QUAL, RC1>(sa.scan, blk, smem);
+    if (blk < sa.n_scan) pipe_scan_body<W, QUAL, RC1, MH>(sa.scan, blk, smem);
   } else if (role <= sa.split) {
     if (blk < sa.n_probe) pipe_probe_body(sa.probe, blk, role - 1, sa.split, smem);
   } else {
@@ -671,13 +675,13 @@ pipe_step_kernel(StepArgs sa) {
   }
 }
 
-template <int W, bool QUAL, bool RC1>
+template <int W, bool QUAL, bool RC1, bool MH>
 cudaError_t launch_pipe_step(const StepArgs &sa, cudaStream_t st) {
   const uint32_t most = max(sa.n_scan, max(sa.n_probe, sa.n_resolve));
   if (!most) return cudaSuccess;
   const size_t smem = kScanSmem > (size_t)ResolveMap::kMapResolve * kPipeBlock * 8
                           ? kScanSmem : (size_t)ResolveMap::kMapResolve * kPipeBlock * 8;
-  pipe_step_kernel<W, QUAL, RC1><<<(2 + sa.split) * most, kPipeBlock, smem, st>>>(sa);
+  pipe_step_kernel<W, QUAL, RC1, MH><<<(2 + sa.split) * most, kPipeBlock, smem, st>>>(sa);
   note_launches();
   return cudaGetLastError();
 }
