@@ -611,20 +611,9 @@ __device__ __forceinline__ bool replay_segment(Lane<W> &s, Store &st, const Clas
 // the highest-scoring taxon (score = counts of the taxon and its ancestors
 // in the map; ties meet at their LCA), then climbing until the counts of its
 // subtree reach `required`.
-// 1: kept out of line, so the hot loops of the step kernel's three roles
-// take less instruction cache (a read with two or more taxa is the rarer
-// case); measured 1 % faster on the 40 GB / 150 bp step
-#ifndef K2G_COLD_RESOLVE_CALL
-#define K2G_COLD_RESOLVE_CALL 1
-#endif
-#if K2G_COLD_RESOLVE_CALL
-#define K2G_COLD_RESOLVE __device__ __noinline__
-#else
-#define K2G_COLD_RESOLVE __device__ __forceinline__
-#endif
 template <class Store>
-K2G_COLD_RESOLVE uint32_t resolve_tree_multi(Store st, MapVisit<Store> mv, const uint32_t *parent,
-                                     uint32_t required) {
+__device__ __forceinline__ uint32_t resolve_tree_multi(Store &st, const MapVisit<Store> &mv,
+                                                       const uint32_t *parent, uint32_t required) {
   uint32_t max_taxon = 0, max_score = 0;
   for (int j = 0; j < mv.n; j++) {
     const int i = mv.slot(j);
@@ -653,6 +642,11 @@ K2G_COLD_RESOLVE uint32_t resolve_tree_multi(Store st, MapVisit<Store> mv, const
   }
   return call;
 }
+
+// (Inline on purpose.  As a function call it saved at most 0.25 % on the
+// 40 GB / 150 bp step, where reads with two or more taxa are rare, and cost
+// 11 % on paired 2 x 150 bp reads and 2.6 times on an uneven-length call over
+// a mutation-tree table, where they are common.)
 
 // Unrolling of the loops over a lane's taxon map: code size against loop
 // overhead in the step kernel's hot loops (4 measured 1 % faster than the

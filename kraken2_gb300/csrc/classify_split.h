@@ -18,7 +18,6 @@ namespace k2g {
 // fragment of at least twice this many bases is cut into pieces of about
 // this length, so a read of L bases is classified by about L / piece_len
 // lanes.  Bounds keep a cut's search window inside its own piece.
-constexpr uint32_t kPieceLenDefault = 1024;
 constexpr uint32_t kPieceLenMin = 256, kPieceLenMax = 8192;
 constexpr uint32_t kCutSearch = 256;      // a cut is looked for within this many positions
 constexpr uint32_t kMaxEventPiece = 60000; // longest piece when hit events are requested

@@ -506,7 +506,6 @@ struct ResolveMap {
   __device__ __forceinline__ uint32_t &map_cnt(int s) { return mcnt[s * kPipeBlock + tid]; }
   __host__ __device__ static constexpr int map_cap() { return kMapResolve; }
 };
-
 struct ResolveLane {
   uint64_t frag;
   uint32_t cur_taxon;

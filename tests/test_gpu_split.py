@@ -18,10 +18,18 @@ from kraken_io import GOLDEN, Batch, batch_of, golden_db
 pytestmark = pytest.mark.gpu
 
 K = 35
-PIECE = 1024
+PIECE = 512     # the default nominal piece length (k2g_tuning::piece_len)
 
 
-def long_reads(seed: int, n: int = 60, quals: bool = False) -> Batch:
+def use_piece(db, piece: int) -> None:
+    """Sets the nominal piece length of every single-end batch class."""
+    for c in range(k2g.LEN_CLASSES):
+        t = db.tuning(0, c)
+        t.piece_len = piece
+        db.set_tuning(0, c, t)
+
+
+def long_reads(seed: int, n: int = 60, quals: bool = False, piece: int = PIECE) -> Batch:
     rng = np.random.default_rng(seed)
     src = batch_of("se150")
     pieces = [src.bases[int(src.seq_off[i]):int(src.seq_off[i + 1])] for i in range(src.n_frags)]
@@ -33,8 +41,8 @@ def long_reads(seed: int, n: int = 60, quals: bool = False) -> Batch:
             buf += pieces[int(rng.integers(0, len(pieces)))]
         buf = buf[:target]
         kind = r % 5
-        for j in range(1, target // PIECE + 1):
-            c = K - 1 + j * PIECE
+        for j in range(1, target // piece + 1):
+            c = K - 1 + j * piece
             if c >= target:
                 break
             at = min(c + int(rng.integers(-60, 300)), target - 2)
@@ -74,14 +82,16 @@ def same(a, b, n):
         assert a.runs_of(i) == b.runs_of(i), i
 
 
+@pytest.mark.parametrize("piece", [512, 1024])
 @pytest.mark.parametrize("seed,params", [
     (1, dict(confidence=0.0, min_hit_groups=0)),
     (2, dict(confidence=0.3, min_hit_groups=2)),
     (3, dict(confidence=0.1, min_hit_groups=2, min_quality=15)),
 ])
-def test_pieces_equal_whole_fragments_and_oracle(seed, params):
+def test_pieces_equal_whole_fragments_and_oracle(seed, params, piece):
     db = k2g.Database.open(os.path.join(GOLDEN, "db_a"))
-    b = long_reads(seed, quals="min_quality" in params)
+    use_piece(db, piece)
+    b = long_reads(seed, quals="min_quality" in params, piece=piece)
     split = classify_batch(db, b, params, mode=k2g.MODE_PERSISTENT)
     whole = classify_batch(db, b, params, mode=k2g.MODE_PLAIN)
     same(split, whole, b.n_frags)

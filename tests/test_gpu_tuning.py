@@ -123,7 +123,7 @@ def test_tuning_values_out_of_range_are_refused():
         for p in (0, 1):
             assert [fresh.tuning(p, c).pipeline for c in range(k2g.LEN_CLASSES)] == [1, 0, 0]
             assert fresh.tuning(p, 0).as_dict() == {"pipeline": 1, "probe_split": 2,
-                                                     "sub_batch_mb": 256, "piece_len": 1024,
+                                                     "sub_batch_mb": 256, "piece_len": 512,
                                                      "graphs": 0}
     finally:
         fresh.close()
