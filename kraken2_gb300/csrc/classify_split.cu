@@ -61,89 +61,138 @@ __device__ uint32_t find_cut(const ScanConst &sc, bool rc1, const uint8_t *seq,
   return 0;
 }
 
-// A long single-end fragment gets a contiguous range of piece slots (one
-// per nominal cut, plus one) and is cut near every b.piece_len positions.
+// Nominal cuts of a fragment of len bases: at k - 1 + j * piece for j = 1
+// .. n_cuts, the last piece keeping at least half a piece; 0 for a fragment
+// shorter than two pieces.
+__device__ __forceinline__ uint32_t nominal_cuts(uint64_t len, uint32_t k, uint32_t piece) {
+  if (len < 2ull * piece) return 0;
+  return (uint32_t)((len - (k - 1) - piece / 2) / piece);
+}
+
+// Planning runs in three steps, so that no thread walks all the cuts of a
+// long fragment alone (a 50 kb read has about 100 cuts at 512-base pieces):
+//  1. per fragment: a contiguous range of piece slots (one per nominal cut,
+//     plus one) and a fragment record; slot j - 1 becomes the job of cut j
+//     (frag, index = j; the slots are zero before);
+//  2. per job: the cut search, its position into hi (0: none) and the
+//     minimizer before it into last_min;
+//  3. per fragment record: the found cuts compacted in order into pieces,
+//     the slots left over made unused (hi = 0).
 // A fragment without room, or without a single usable cut, is left whole.
-__device__ void plan_fragment(const ClassifyArgs &a, const SplitBufs &b, const ScanConst &sc,
-                              uint64_t f) {
-  const bool rc1 = a.scan.revcom_version != 0;
-  const bool qual = a.quals != nullptr && a.cls.min_quality > 0;
-  const int thr = 33 + a.cls.min_quality;
-  const bool qall = thr > 127;
-  const uint32_t k = (uint32_t)sc.k;
-  const uint64_t o0 = a.seq_off[f], len = a.seq_off[f + 1] - o0;
-  const uint32_t piece = b.piece_len;
-  if (len < 2ull * piece) return;
-  // nominal cuts at k - 1 + j * piece, the last piece keeping half that
-  const uint32_t n_cuts = (uint32_t)((len - (k - 1) - piece / 2) / piece);
+__device__ void plan_reserve(const ClassifyArgs &a, const SplitBufs &b, uint32_t k, uint64_t f) {
+  const uint64_t len = a.seq_off[f + 1] - a.seq_off[f];
+  const uint32_t n_cuts = nominal_cuts(len, k, b.piece_len);
   if (!n_cuts) return;
   const unsigned long long base = atomicAdd(b.ctr, (unsigned long long)n_cuts + 1);
   if (base + n_cuts + 1 > b.pieces_cap) return;
   const unsigned long long sid = atomicAdd(b.ctr + 1, 1ull);
   if (sid >= b.frags_cap) return;
-  const uint8_t *seq = a.bases + o0;
-  const uint8_t *qs = qual ? a.quals + o0 : nullptr;
-  // with hit events a piece's key ordinals are index << 16 | local: keep
-  // the pieces below 2^15 and each below 2^16 bases (so below 2^16 keys)
-  const bool events = a.hit_keys != nullptr;
-  bool whole = events && n_cuts + 1 >= (1u << 15);
-  uint32_t lo = k - 1, idx = 0;
-  uint64_t lm = 0;
-  for (uint32_t j = 1; j <= n_cuts && !whole; j++) {
-    const uint32_t c = k - 1 + j * piece;
-    const uint32_t end = (uint32_t)min((uint64_t)c + kCutSearch, len);
-    uint64_t mp = 0;
-    const uint32_t p = find_cut(sc, rc1, seq, qs, thr, qall, c, end, mp);
-    if (!p) continue;
-    if (events && p - lo >= kMaxEventPiece) whole = true;
-    SplitPiece &pc = b.pieces[base + idx];
+  b.frags[sid] = SplitFrag{f, base, 0};
+  // with hit events a piece's key ordinals are index << 16 | local: a
+  // fragment of 2^15 pieces or more stays whole, and needs no search
+  if (a.hit_keys != nullptr && n_cuts + 1 >= (1u << 15)) return;
+  for (uint32_t j = 1; j <= n_cuts; j++) {
+    SplitPiece &pc = b.pieces[base + j - 1];
     pc.frag = f;
-    pc.last_min = lm;
-    pc.lo = lo;
-    pc.hi = p;
-    pc.index = idx;
-    idx++;
-    lo = p;
-    lm = mp;
+    pc.index = j;
   }
-  if (events && len - lo >= kMaxEventPiece) whole = true;
-  SplitFrag sf{f, base, 0};
-  if (whole) {   // slots already written are voided
-    for (uint32_t j = 0; j < idx; j++) b.pieces[base + j].hi = 0;
-    idx = 0;
-  }
-  if (idx) {
-    SplitPiece &pc = b.pieces[base + idx];
-    pc.frag = f;
-    pc.last_min = lm;
-    pc.lo = lo;
-    pc.hi = (uint32_t)len;
-    pc.index = idx;
-    sf.n = idx + 1;
-    b.mark[f] = 1;
-  }
-  b.frags[sid] = sf;
 }
 
 // One thread per fragment of the view (marks are cleared here).
 __global__ void split_plan_kernel(ClassifyArgs a, SplitBufs b) {
-  const ScanConst sc = scan_const(a);
+  const uint32_t k = (uint32_t)a.scan.k;
   for (uint64_t f = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; f < a.n_frags;
        f += (uint64_t)gridDim.x * blockDim.x) {
     b.mark[f] = 0;
-    plan_fragment(a, b, sc, f);
+    plan_reserve(a, b, k, f);
   }
 }
 
 // One thread per entry of the view's in_list (the fragments the pipeline
 // deferred); marks must be cleared before.
 __global__ void split_plan_list_kernel(ClassifyArgs a, SplitBufs b) {
-  const ScanConst sc = scan_const(a);
+  const uint32_t k = (uint32_t)a.scan.k;
   const uint64_t n = min((uint64_t)*a.in_count, a.in_cap);
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t f = a.in_list[i];
-    if (f < a.n_frags) plan_fragment(a, b, sc, f);
+    if (f < a.n_frags) plan_reserve(a, b, k, f);
+  }
+}
+
+// One thread per cut job.
+__global__ void split_cut_kernel(ClassifyArgs a, SplitBufs b) {
+  const ScanConst sc = scan_const(a);
+  const bool rc1 = a.scan.revcom_version != 0;
+  const bool qual = a.quals != nullptr && a.cls.min_quality > 0;
+  const int thr = 33 + a.cls.min_quality;
+  const bool qall = thr > 127;
+  const uint32_t k = (uint32_t)sc.k, piece = b.piece_len;
+  const uint64_t n_slots = min((uint64_t)*b.ctr, b.pieces_cap);
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n_slots;
+       s += (uint64_t)gridDim.x * blockDim.x) {
+    SplitPiece &job = b.pieces[s];
+    const uint32_t j = job.index;
+    const uint64_t f = job.frag;
+    if (!j || f >= a.n_frags) continue;
+    const uint64_t o0 = a.seq_off[f], len = a.seq_off[f + 1] - o0;
+    if (j > nominal_cuts(len, k, piece)) continue;
+    const uint32_t c = k - 1 + j * piece;
+    const uint32_t end = (uint32_t)min((uint64_t)c + kCutSearch, len);
+    uint64_t mp = 0;
+    job.hi = find_cut(sc, rc1, a.bases + o0, qual ? a.quals + o0 : nullptr, thr, qall, c, end, mp);
+    job.last_min = mp;
+  }
+}
+
+// One thread per fragment record: the pieces of the fragment in order.  A
+// piece is written at or before the slot its cut was read from, so the
+// compaction runs in place.
+__global__ void split_compact_kernel(ClassifyArgs a, SplitBufs b) {
+  const uint32_t k = (uint32_t)a.scan.k;
+  const bool events = a.hit_keys != nullptr;
+  const uint64_t n_split = min((uint64_t)b.ctr[1], b.frags_cap);
+  for (uint64_t sid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; sid < n_split;
+       sid += (uint64_t)gridDim.x * blockDim.x) {
+    SplitFrag sf = b.frags[sid];
+    const uint64_t f = sf.frag, base = sf.first;
+    const uint64_t len = a.seq_off[f + 1] - a.seq_off[f];
+    const uint32_t n_cuts = nominal_cuts(len, k, b.piece_len);
+    // (pieces below 2^15, each below 2^16 bases, with hit events)
+    bool whole = events && n_cuts + 1 >= (1u << 15);
+    uint32_t lo = k - 1, idx = 0;
+    uint64_t lm = 0;
+    for (uint32_t j = 1; j <= n_cuts && !whole; j++) {
+      const SplitPiece job = b.pieces[base + j - 1];
+      const uint32_t p = job.hi;
+      if (!p) continue;
+      if (events && p - lo >= kMaxEventPiece) whole = true;
+      SplitPiece &pc = b.pieces[base + idx];
+      pc.frag = f;
+      pc.last_min = lm;
+      pc.lo = lo;
+      pc.hi = p;
+      pc.index = idx;
+      idx++;
+      lo = p;
+      lm = job.last_min;
+    }
+    if (events && len - lo >= kMaxEventPiece) whole = true;
+    if (whole) idx = 0;
+    if (idx) {
+      SplitPiece &pc = b.pieces[base + idx];
+      pc.frag = f;
+      pc.last_min = lm;
+      pc.lo = lo;
+      pc.hi = (uint32_t)len;
+      pc.index = idx;
+      sf.n = idx + 1;
+      b.mark[f] = 1;
+    }
+    // the slots after the fragment's last piece (all of them when it stays
+    // whole) hold no piece
+    for (uint32_t j = idx ? idx + 1 : 0; j <= n_cuts; j++) b.pieces[base + j].hi = 0;
+    b.frags[sid] = sf;
   }
 }
 
@@ -251,17 +300,27 @@ unsigned grid_of(uint64_t n, int sms) {
 
 }  // namespace
 
+// Steps 2 and 3 of a plan.
+static cudaError_t split_cuts(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st) {
+  split_cut_kernel<<<grid_of(b.pieces_cap, sms), 128, 0, st>>>(v, b);
+  split_compact_kernel<<<grid_of(b.frags_cap, sms), 128, 0, st>>>(v, b);
+  note_launches(2);
+  return cudaGetLastError();
+}
+
 cudaError_t split_plan(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st) {
   split_plan_kernel<<<grid_of(v.n_frags, sms), 128, 0, st>>>(v, b);
   note_launches();
-  return cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
+  return e != cudaSuccess ? e : split_cuts(v, b, sms, st);
 }
 
 cudaError_t split_plan_list(const ClassifyArgs &v, const SplitBufs &b, uint64_t list_cap, int sms,
                            cudaStream_t st) {
   split_plan_list_kernel<<<grid_of(list_cap, sms), 128, 0, st>>>(v, b);
   note_launches();
-  return cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
+  return e != cudaSuccess ? e : split_cuts(v, b, sms, st);
 }
 
 cudaError_t split_merge(const ClassifyArgs &v, const SplitBufs &b, int sms, cudaStream_t st) {
