@@ -216,7 +216,9 @@ k2g_status k2g_classify(const k2g_db *db, const k2g_reads *reads,
  * prefetch distance at src/compact_hash.h:380-392).  Each table keeps one
  * set of values per (single-end or paired, length class) of a batch; every
  * k2g_classify call uses the set of its batch's class.  The values change
- * only how the work is scheduled, never a result. */
+ * only how the work is scheduled, never a result.  A table starts with
+ * pipeline 1 for short batches and 0 otherwise, probe_split 2,
+ * sub_batch_mb 256, piece_len 512 and graphs 0 in every class. */
 typedef struct {
   /* 1: K2G_MODE_PIPELINED runs scan / probe / resolve beats over
    * sub-batches; 0: it runs the fused work-stealing kernel instead */
