@@ -1650,8 +1650,13 @@ def run_ours(args, log):
         kr.run()
         torch.cuda.synchronize()
         kdt = time.perf_counter() - t0
-        return {"metric": "minimizer_data", "reads": cfg.n_reads, "s_per_pass": round(kdt, 3),
-                "mreads_min": round(cfg.n_reads / kdt * 60 / 1e6, 1)}
+        out = {"metric": "minimizer_data", "reads": cfg.n_reads, "s_per_pass": round(kdt, 3),
+               "mreads_min": round(cfg.n_reads / kdt * 60 / 1e6, 1)}
+        if args.kmer_parity_blocks:
+            del kr
+            cells, _ = wl.db.download()
+            out["parity"] = kmer_parity(wl, cells, wl.k2g.MODE_PIPELINED, args.kmer_parity_blocks)
+        return out
     mode = {"plain": wl.k2g.MODE_PLAIN, "persistent": wl.k2g.MODE_PERSISTENT,
             "pipelined": wl.k2g.MODE_PIPELINED}[args.mode]
     runner = DeviceRunner(wl, mode)
@@ -1747,7 +1752,7 @@ def run_ours(args, log):
     cells, _ = wl.db.download()
     log(f"table download {time.time() - t0:.1f}s")
     if kmer is not None:
-        kmer["parity"] = kmer_parity(wl, cells, mode)
+        kmer["parity"] = kmer_parity(wl, cells, mode, args.kmer_parity_blocks or 5)
     n_sample = min(cfg.n_reads, 50_000)
     keys = sample_lookup_keys(wl, n_sample)
     sectors, hit = probe_sectors(cells, cfg.capacity, cfg.key_bits, cfg.value_bits, keys)
@@ -2007,6 +2012,9 @@ def main():
                     help="setup plus the long-read mix in HBM only (for ncu captures)")
     ap.add_argument("--kmer-only", action="store_true",
                     help="setup plus two -K passes only (for ncu captures)")
+    ap.add_argument("--kmer-parity-blocks", type=int, default=0,
+                    help="reader blocks of the -K parity check against the oracle (default 5; "
+                         "with --kmer-only the check runs only when this is given)")
     args = ap.parse_args()
     log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
     out = run_reference(args, log) if args.impl == "reference" else run_ours(args, log)
