@@ -11,15 +11,15 @@ import pytest
 import oracle
 from kraken_io import batch_of, golden_db
 
-PIECE, SEARCH = 1024, 256
+SEARCH = 256
 
 
-def cuts_of(opts, seq: bytes):
+def cuts_of(opts, seq: bytes, piece: int):
     """First-k-mer indices of the pieces after the first, by the cut rule."""
     mins, amb = oracle.scan(opts, seq)
     out, j = [], 1
-    while (j + 1) * PIECE <= len(mins):
-        c = j * PIECE
+    while (j + 1) * piece <= len(mins):
+        c = j * piece
         for i in range(c, min(c + SEARCH, len(mins))):
             if not amb[i - 1] and not amb[i] and mins[i] != mins[i - 1]:
                 out.append(i)
@@ -48,8 +48,9 @@ def classify_all(o, seqs):
     return calls, hg, per
 
 
+@pytest.mark.parametrize("piece", [512, 1024])
 @pytest.mark.parametrize("seed", [1, 2, 3])
-def test_pieces_join_to_the_whole_read(seed):
+def test_pieces_join_to_the_whole_read(seed, piece):
     g = golden_db("db_a")
     o = oracle.Oracle(g.hash.cells, g.hash.capacity, g.hash.key_bits, g.hash.value_bits,
                       g.taxo.parent, oracle.index_opts(g.opts.k, g.opts.l, g.opts.spaced_seed_mask,
@@ -66,7 +67,7 @@ def test_pieces_join_to_the_whole_read(seed):
             buf += parts[int(rng.integers(0, len(parts)))]
         buf = buf[:target]
         # ambiguity and low complexity near the nominal cuts
-        for c in range(PIECE, target - 200, PIECE):
+        for c in range(piece, target - 200, piece):
             at = c + int(rng.integers(-40, 200))
             if r % 3 == 1:
                 ln = int(rng.integers(1, 60))
@@ -77,7 +78,7 @@ def test_pieces_join_to_the_whole_read(seed):
     whole_calls, whole_hg, whole_runs = classify_all(o, reads)
     pieces, owner = [], []
     for i, seq in enumerate(reads):
-        starts = [0] + cuts_of(o.opts, seq)   # a read without a usable cut stays whole
+        starts = [0] + cuts_of(o.opts, seq, piece)   # a read without a usable cut stays whole
         ends = [s + k - 1 for s in starts[1:]] + [len(seq)]   # a piece ends with its last k-mer
         for s, e in zip(starts, ends):
             pieces.append(seq[s:e])
